@@ -1,0 +1,297 @@
+"""Benchmark: permanents per second at n=28 (complex128) on one GB300.
+
+Workload: the leading 28x28 block of a seeded 56x56 Haar-random unitary
+(QR of a complex Gaussian with the phase fix, seed 0), all row and column
+multiplicities 1; one permanent per step, spread over every SM.  This is the
+single-large-permanent configuration at the size the headline metric names.
+
+Prints ONE JSON line (rank 0):
+  value      permanents/s with the input resident on the device: device time
+             of the whole pipeline (queue reset, walk, reductions) per step,
+             CUDA events on the engine's stream, L2 flushed between steps;
+  e2e        the same metric through the public API permanent(matrix, rows,
+             cols) with host buffers: planning, host->device plan copy,
+             kernels and the device->host result copy inside the timed region;
+  roofline   the walk kernel against the measured FP64 FMA peak (algorithmic
+             flops 2^(n-1)*(10n+4) per permanent / walk-kernel event time);
+  cpu_baseline  the reference's CPU method (oracle port, all host threads)
+             on the same input.
+``--impl reference`` times that CPU method alone, on the same workload.
+Multi-GPU (torchrun): independent replicas, one per rank; value = sum.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+
+def haar_unitary(d, seed):
+    rng = np.random.default_rng(seed)
+    Z = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) / np.sqrt(2)
+    Q, R = np.linalg.qr(Z)
+    return Q * (np.diag(R) / np.abs(np.diag(R)))
+
+
+def flops_all_ones(n):
+    return 2.0 ** (n - 1) * (10 * n + 4)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo", init_method="env://")
+        pg = dist
+    return world, rank, local, pg
+
+
+def allreduce_max_sum(pg, vals_max, vals_sum):
+    if pg is None:
+        return vals_max, vals_sum
+    import torch
+
+    t = torch.tensor(vals_max, dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    s = torch.tensor(vals_sum, dtype=torch.float64)
+    pg.all_reduce(s, op=pg.ReduceOp.SUM)
+    return t.tolist(), s.tolist()
+
+
+def cpu_reference_rate(U, ones, reps):
+    """The reference's CPU method (oracle port: std::complex<double>, 4 x
+    hardware threads, OpenMP) on the same input; returns (perm/s, threads)."""
+    import oracle
+
+    oracle.build.build(with_reference=False)
+    oracle.port_permanent(U[:20, :20].copy(), ones[:20], ones[:20])  # warm the thread pool
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.port_permanent(U, ones, ones)
+        times.append(time.perf_counter() - t0)
+    return 1.0 / statistics.median(times), os.cpu_count()
+
+
+def run_reference(args, world, rank, pg):
+    n = args.n
+    if world > 1 and rank != 0:
+        return
+    U = haar_unitary(2 * n, 0)[:n, :n].copy()
+    ones = np.ones(n, dtype=int)
+    import oracle
+
+    oracle.build.build(with_reference=False)
+    for _ in range(args.warmup):
+        oracle.port_permanent(U, ones, ones)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.port_permanent(U, ones, ones)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference",
+        "metric": "permanents_per_second_n%d_complex128" % n,
+        "value": value,
+        "unit": "perm/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c128",
+        "data": "synthetic (seeded Haar unitary)",
+        "config": {"workload": "permanent n=%d complex128, leading block of seeded %dx%d Haar unitary, "
+                               "unit multiplicities" % (n, 2 * n, 2 * n), "n": n},
+        "cpu_baseline": {"value": value, "unit": "perm/s", "cores": cores, "kind": "port",
+                         "sample": "%d full n=%d permanents, reference method (4 x hw threads)" % (args.steps, n)},
+        "e2e": {"value": value, "unit": "perm/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local, pg):
+    import __graft_entry__
+
+    __graft_entry__.build_engine()
+    import piquasso_gb300 as pg_engine
+    import torch
+
+    torch.cuda.set_device(local)
+    n = args.n
+    U = haar_unitary(2 * n, 0)[:n, :n].copy()
+    ones = np.ones(n, dtype=int)
+    if args.dtype == "c64":
+        U = U.astype(np.complex64)
+    peaks = pg_engine.measure_vector_peaks(20.0)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
+
+    for _ in range(args.warmup):
+        pg_engine.permanent(U, ones, ones)
+    torch.cuda.synchronize()
+    if pg is not None:
+        pg.barrier()
+
+    # device-resident value: engine events around the device pipeline
+    launches0 = pg_engine.kernel_launches()
+    dev_ms, walk_ms = [], []
+    e2e_s = []
+    h2d = d2h = 0.0
+    result = None
+    with ClockSampler(local) as clk:
+        t_region = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            result = pg_engine.permanent(U, ones, ones)  # host buffers in, host result out
+            e2e_s.append(time.perf_counter() - t0)
+            tm = pg_engine.last_timing()
+            dev_ms.append(tm["device_ms"])
+            walk_ms.append(tm["walk_ms"])
+            h2d, d2h = tm["h2d_bytes"], tm["d2h_bytes"]
+        torch.cuda.synchronize()
+        region = time.perf_counter() - t_region
+    launches = pg_engine.kernel_launches() - launches0
+    clocks = clk.summary()
+
+    total_dev = sum(dev_ms) / 1e3
+    total_e2e = sum(e2e_s)
+    (max_dev, max_e2e), _ = allreduce_max_sum(pg, [total_dev, total_e2e], [0.0])
+    value = world * args.steps / max_dev
+    e2e = world * args.steps / max_e2e
+    mean_walk_s = statistics.mean(walk_ms) / 1e3
+    F = flops_all_ones(n)
+    achieved = F / mean_walk_s / 1e12
+    peak = peaks["fp64_tflops"] if args.dtype == "c128" else peaks["fp32_tflops"]
+
+    line = {
+        "metric": "permanents_per_second_n%d_%s" % (n, "complex128" if args.dtype == "c128" else "complex64"),
+        "value": value,
+        "unit": "perm/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * max_dev / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": args.dtype,
+        "data": "synthetic (seeded Haar unitary)",
+        "config": {"workload": "permanent n=%d %s, leading block of seeded %dx%d Haar unitary, unit "
+                               "multiplicities, one permanent per launch over all SMs"
+                               % (n, "complex128" if args.dtype == "c128" else "complex64", 2 * n, 2 * n),
+                   "n": n, "l2": "flushed between steps (256 MB write)", "parallelism": "replicas" if world > 1 else "1gpu"},
+        "e2e": {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp64" if args.dtype == "c128" else "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured: engine FMA-chain microkernel (pqg_measure_vector_peaks)",
+                     "flops_per_launch": F, "walk_ms": 1e3 * mean_walk_s},
+        "peaks_measured": peaks,
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "result": [float(np.real(result)), float(np.imag(result))],
+        "timed_region_s": region,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, cores = cpu_reference_rate(U.astype(np.complex128), ones, reps=args.cpu_reps)
+        line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",
+                                "sample": "median of %d full n=%d complex128 permanents, reference method, "
+                                          "4 x hw threads" % (args.cpu_reps, n)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=28)
+    ap.add_argument("--dtype", choices=["c128", "c64"], default="c128")
+    ap.add_argument("--cpu-reps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_ours(args, world, rank, local, pg)
+
+
+if __name__ == "__main__":
+    main()

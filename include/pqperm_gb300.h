@@ -1,0 +1,102 @@
+/*
+ * pqperm_gb300 — C ABI of the GB300 permanent engine.
+ *
+ * Plain pointers and sizes only.  Complex numbers are interleaved (re, im)
+ * pairs in row-major order, exactly numpy's complex128 / complex64 layout, so
+ * a numpy array's data pointer can be passed as is.  Multiplicities are int32.
+ *
+ * Every entry point returns a status code (PQG_OK == 0); pqg_last_error()
+ * returns a message for the calling thread's last failure.
+ *
+ * Each entry point replaces one function of the reference (piquasso 8.0.1,
+ * paths relative to its repository):
+ *   pqg_permanent_c128 / _c64          piquasso/_math/permanent.cpp:26-41,71-78
+ *                                      (permanent_np<double>/<float> -> src/permanent.cpp:49-264)
+ *   pqg_permanent_laplace_c128 / _c64  piquasso/_math/permanent.cpp:43-58,79-84
+ *                                      (permanent_laplace_np -> src/permanent_laplace.cpp:43-240)
+ *   pqg_permanent_batch_c128 / _c64    the per-pattern loop over permanent() in
+ *                                      piquasso/_simulators/passive/utils.py:131-138 and
+ *                                      probabilities.py:26-54 (many output patterns, one matrix)
+ */
+#ifndef PQPERM_GB300_H
+#define PQPERM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define PQG_OK 0
+#define PQG_ERR_SUM_MISMATCH 1 /* sum(rows) != sum(cols): src/permanent.cpp:100-104 throws */
+#define PQG_ERR_INVALID 2      /* negative multiplicity, null pointer, bad size */
+#define PQG_ERR_TOO_LARGE 3    /* > 32 distinct nonzero columns or > 2^50 Gray-code steps */
+#define PQG_ERR_CUDA 4         /* a CUDA runtime call failed */
+#define PQG_ERR_NO_DEVICE 5    /* no CUDA device visible */
+
+/* precision modes for the complex128 entry points */
+#define PQG_MODE_AUTO 0 /* the default: native FP64 (PQG_MODE_FP64) */
+#define PQG_MODE_FP64 1 /* row sums, updates and products in FP64; double-double sums */
+
+/* Message describing the calling thread's last failure ("" if none). */
+const char *pqg_last_error(void);
+
+/* Library version string. */
+const char *pqg_version(void);
+
+/* Number of kernels this library launched since load (all entry points). */
+uint64_t pqg_kernel_launches(void);
+
+/* Permanent of an n_rows x n_cols complex128 matrix with row multiplicities
+ * `rows` (n_rows) and column multiplicities `cols` (n_cols), as
+ * permanent(matrix, rows, cols) in the reference.  `out` receives 2 doubles
+ * (re, im).  `out_lo` (nullable) receives the low words of the double-double
+ * result (re_lo, im_lo).  Host buffers; the call is synchronous. */
+int pqg_permanent_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                       const int32_t *cols, int32_t mode, double *out, double *out_lo);
+
+/* complex64 variant: FP32 row-sum updates and products, FP32 TwoSum-compensated
+ * partial sums folded into per-thread double-double accumulators.  `out`
+ * receives 2 floats (re, im). */
+int pqg_permanent_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                      const int32_t *cols, float *out);
+
+/* Many permanents of ONE matrix: problem b uses rows[b*n_rows ...] and
+ * cols[b*n_cols ...].  `out` receives 2*batch values.  One work queue, one
+ * walk launch and one reduction for the whole batch. */
+int pqg_permanent_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                             const int32_t *cols, int64_t batch, int32_t mode, double *out);
+int pqg_permanent_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                            const int32_t *cols, int64_t batch, float *out);
+
+/* Laplace-expansion permanents: for every column l, the permanent with
+ * cols[l] lowered by one (reference semantics, including a column with
+ * multiplicity 0 contributing exponent 0).  `out` must hold 2*max(n_cols,1)
+ * values; *n_out receives the count written (1 for the empty case, whose value
+ * is 1, as src/permanent_laplace.cpp:52-57). */
+int pqg_permanent_laplace_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                               const int32_t *cols, double *out, int64_t *n_out);
+int pqg_permanent_laplace_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                              const int32_t *cols, float *out, int64_t *n_out);
+
+/* Measured FP64 / FP32 fused-multiply-add throughput of device 0 in TFLOP/s
+ * (2 flops per FMA), from dependent-chain microkernels run over all SMs for
+ * about `ms` milliseconds each.  out2 = {fp64_tflops, fp32_tflops}. */
+int pqg_measure_vector_peaks(double ms, double *out2);
+
+/* Timing of the calling thread's last plain/Laplace/batch call, measured with
+ * CUDA events on the launching stream: `walk_ms` is the walk kernel alone,
+ * `device_ms` the whole device pipeline (queue reset, walk, both reductions,
+ * excluding the host<->device copies).  `steps` is the number of Gray-code
+ * steps walked, `flops` the algorithmic flop count of the call, and
+ * `h2d_bytes` / `d2h_bytes` the bytes the call copied each way.  Any pointer
+ * may be null. */
+int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *flops, double *h2d_bytes,
+                    double *d2h_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PQPERM_GB300_H */

@@ -1,0 +1,21 @@
+"""piquasso_gb300 — a GB300-native (sm_103a) engine for piquasso's permanent hot path.
+
+Public API (drop-in for ``piquasso._math.permanent``):
+    permanent(matrix, rows, cols)
+    permanent_laplace(matrix, rows, cols)
+plus the additive ``permanent_batch`` and the connector in
+``piquasso_gb300.connector``.
+"""
+
+from .permanent import (  # noqa: F401
+    PermanentInputError,
+    PermanentTooLarge,
+    measure_vector_peaks,
+    permanent,
+    permanent_batch,
+    permanent_dd,
+    permanent_laplace,
+)
+from ._lib import EngineUnavailable, kernel_launches, last_timing  # noqa: F401
+
+__version__ = "0.1.0"

@@ -1,0 +1,90 @@
+"""ctypes binding of the C ABI in include/pqperm_gb300.h.
+
+The library is built in-tree (``piquasso_gb300/build.py``) and loaded from
+``piquasso_gb300/_lib/``.  There is no fallback: if it is missing or no CUDA
+device is visible, every entry point raises.
+"""
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpqperm_gb300.so")
+
+PQG_OK = 0
+PQG_ERR_SUM_MISMATCH = 1
+PQG_ERR_INVALID = 2
+PQG_ERR_TOO_LARGE = 3
+PQG_ERR_CUDA = 4
+PQG_ERR_NO_DEVICE = 5
+
+MODE_AUTO = 0
+MODE_FP64 = 1
+
+# (name, argtypes) of every symbol the header declares
+_d = ctypes.POINTER(ctypes.c_double)
+_f = ctypes.POINTER(ctypes.c_float)
+_i32 = ctypes.POINTER(ctypes.c_int32)
+_i64 = ctypes.POINTER(ctypes.c_int64)
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+
+SIGNATURES = {
+    "pqg_last_error": ([], ctypes.c_char_p),
+    "pqg_version": ([], ctypes.c_char_p),
+    "pqg_kernel_launches": ([], ctypes.c_uint64),
+    "pqg_permanent_c128": ([_d, _I64, _I64, _i32, _i32, _I32, _d, _d], ctypes.c_int),
+    "pqg_permanent_c64": ([_f, _I64, _I64, _i32, _i32, _f], ctypes.c_int),
+    "pqg_permanent_batch_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _I32, _d], ctypes.c_int),
+    "pqg_permanent_batch_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f], ctypes.c_int),
+    "pqg_permanent_laplace_c128": ([_d, _I64, _I64, _i32, _i32, _d, _i64], ctypes.c_int),
+    "pqg_permanent_laplace_c64": ([_f, _I64, _I64, _i32, _i32, _f, _i64], ctypes.c_int),
+    "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),
+    "pqg_last_timing": ([_d, _d, _d, _d, _d, _d], ctypes.c_int),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class EngineUnavailable(RuntimeError):
+    """The CUDA engine is not built or no GPU is visible (there is no CPU path)."""
+
+
+def load():
+    """Loads the engine library (building nothing); raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise EngineUnavailable(
+                    "piquasso_gb300 CUDA engine not built (%s missing); run "
+                    "`python -c 'import __graft_entry__ as g; g.build()'`" % LIB_PATH)
+            lib = ctypes.CDLL(LIB_PATH)
+            for name, (args, res) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.argtypes = args
+                fn.restype = res
+            _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    return load().pqg_last_error().decode(errors="replace")
+
+
+def kernel_launches() -> int:
+    return int(load().pqg_kernel_launches())
+
+
+def last_timing():
+    """Event timing of this thread's last call: dict with walk_ms (walk kernel),
+    device_ms (queue reset + walk + reductions), steps, flops and the bytes
+    copied host-to-device / device-to-host."""
+    v = [ctypes.c_double(0.0) for _ in range(6)]
+    load().pqg_last_timing(*[ctypes.byref(x) for x in v])
+    keys = ("walk_ms", "device_ms", "steps", "flops", "h2d_bytes", "d2h_bytes")
+    return {k: x.value for k, x in zip(keys, v)}

@@ -1,0 +1,409 @@
+// Host-side planner for the permanent walk kernels.
+//
+// Reduction and semantics follow the reference (piquasso 8.0.1):
+//   * row reduction: src/permanent.cpp:54-95 (and src/permanent_laplace.cpp:59-100):
+//     a copy of the first row with the smallest nonzero multiplicity becomes
+//     row 0 with multiplicity 1, and that row's multiplicity drops by one;
+//   * sum check: src/permanent.cpp:97-104 (plain form only);
+//   * empty input gives 1: src/permanent.cpp:106-108, permanent_laplace.cpp:52-57;
+//   * normalisation 2^(N-1): src/permanent.cpp:259, permanent_laplace.cpp:227.
+// Digits with multiplicity 0 and columns with multiplicity 0 contribute a
+// factor of one to every term, so the planner drops them (the Laplace form
+// keeps one extra output for zero-multiplicity columns, see below).  The sum
+// is then the same set of terms as the reference's; only the order of
+// summation differs.
+#include "plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace pqg {
+
+namespace {
+
+int64_t binom64(int64_t n, int64_t k) {
+    if (k < 0 || k > n) return 0;
+    if (k > n - k) k = n - k;
+    int64_t r = 1;
+    for (int64_t i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+    return r;
+}
+
+// Error-free sum of doubles (Knuth TwoSum), used to form the FP64 seed rows
+// from a compensated sum.
+struct Kahan2 {
+    double s = 0.0, c = 0.0;
+    void add(double x) {
+        double t = s + x;
+        double bb = t - s;
+        c += (s - (t - bb)) + (x - bb);
+        s = t;
+    }
+    double value() const { return s + c; }
+};
+
+}  // namespace
+
+double algorithmic_flops(const PendingProblem &p, Form form) {
+    if (p.kind != PQG_KIND_WALK) return 0.0;
+    const int nc = p.nc - p.padded_cols;
+    double sum_cm = 0;
+    for (int k = 0; k < nc; ++k) sum_cm += p.cm[k];
+    if (form == Form::PLAIN) return p.S * (4.0 * nc + 6.0 * sum_cm + 4.0);
+    // Laplace: updates, prefix and suffix products over the factors, one
+    // combine per output and a weighted accumulation per output.
+    return p.S * (4.0 * nc + 12.0 * sum_cm + 6.0 * nc + 4.0 * p.n_out);
+}
+
+int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
+                 std::string &err) {
+    PendingProblem p;
+    if (nr < 0 || nc < 0 || (nr > 0 && nc > 0 && a == nullptr) || (nr > 0 && !rows) || (nc > 0 && !cols)) {
+        err = "invalid matrix or multiplicity buffers";
+        return 2;
+    }
+    int64_t sr = 0, sc = 0;
+    for (int64_t i = 0; i < nr; ++i) {
+        if (rows[i] < 0) {
+            err = "row multiplicities must be nonnegative";
+            return 2;
+        }
+        sr += rows[i];
+    }
+    for (int64_t j = 0; j < nc; ++j) {
+        if (cols[j] < 0) {
+            err = "column multiplicities must be nonnegative";
+            return 2;
+        }
+        sc += cols[j];
+    }
+
+    if (form_ == Form::PLAIN) {
+        // src/permanent.cpp:97-104 (the reduction keeps the row sum unchanged)
+        if (sr != sc) {
+            err = "Number of input and output states should be equal";
+            return 1;
+        }
+        if (nr == 0 || nc == 0 || sr == 0) {  // src/permanent.cpp:106-108
+            p.kind = PQG_KIND_CONSTANT;
+            p.n_out = 1;
+            pending.push_back(std::move(p));
+            return 0;
+        }
+    } else {
+        if (nr == 0 || nc == 0 || sr == 0 || sc == 0) {  // src/permanent_laplace.cpp:52-57
+            p.kind = PQG_KIND_CONSTANT;
+            p.n_out = 1;
+            pending.push_back(std::move(p));
+            return 0;
+        }
+    }
+    if (sr > 250) {
+        err = "too many particles";
+        return 3;
+    }
+
+    // columns with nonzero multiplicity
+    std::vector<int> keep;
+    for (int64_t j = 0; j < nc; ++j)
+        if (cols[j] > 0) keep.push_back(static_cast<int>(j));
+    if (keep.empty() || static_cast<int>(keep.size()) > PQG_MAX_COLS) {
+        err = keep.empty() ? "no column with nonzero multiplicity"
+                           : "more than 32 distinct columns with nonzero multiplicity";
+        return keep.empty() ? 2 : 3;
+    }
+    p.nc = static_cast<int>(keep.size());
+    for (int j : keep) {
+        if (cols[j] > 255) {
+            err = "column multiplicity above 255";
+            return 3;
+        }
+        p.cm.push_back(cols[j]);
+    }
+
+    if (form_ == Form::LAPLACE) {
+        // outputs: one per kept column; every zero-multiplicity column shares
+        // one extra output (its exponent stays 0: permanent_laplace.cpp:180,210)
+        p.out_map.assign(static_cast<size_t>(nc), -1);
+        for (int k = 0; k < p.nc; ++k) p.out_map[keep[k]] = k;
+        p.laplace_full = static_cast<int64_t>(keep.size()) < nc;
+        for (int64_t j = 0; j < nc; ++j)
+            if (p.out_map[j] < 0) p.out_map[j] = p.nc;
+        p.n_out = p.nc + (p.laplace_full ? 1 : 0);
+    }
+
+    // row reduction (src/permanent.cpp:54-95)
+    int64_t min_idx = 0;
+    int minelem = 0;
+    for (int64_t i = 0; i < nr; ++i) {
+        if (minelem == 0 || (rows[i] < minelem && rows[i] != 0)) {
+            minelem = rows[i];
+            min_idx = i;
+        }
+    }
+    auto elem = [&](int64_t i, int k, int part) { return a[2 * (i * nc + keep[k]) + part]; };
+    p.a0.resize(2 * p.nc);
+    for (int k = 0; k < p.nc; ++k) {
+        p.a0[2 * k] = elem(min_idx, k, 0);
+        p.a0[2 * k + 1] = elem(min_idx, k, 1);
+    }
+    double S = 1.0;
+    for (int64_t i = 0; i < nr; ++i) {
+        int m = rows[i] - (i == min_idx ? 1 : 0);
+        if (m <= 0) continue;
+        p.m.push_back(m);
+        for (int k = 0; k < p.nc; ++k) {
+            p.rows.push_back(elem(i, k, 0));
+            p.rows.push_back(elem(i, k, 1));
+        }
+        S *= (m + 1);
+    }
+    if (S > std::ldexp(1.0, 50)) {
+        err = "Gray-code space above 2^50 steps";
+        return 3;
+    }
+    p.S = S;
+    p.scale_exp = static_cast<int>(sr - 1);
+    pending.push_back(std::move(p));
+    return 0;
+}
+
+int64_t Planner::align_(size_t al) {
+    size_t n = arena.size();
+    size_t r = (n + al - 1) / al * al;
+    arena.resize(r, 0);
+    return static_cast<int64_t>(r);
+}
+
+int64_t Planner::push_bytes_(const void *p, size_t n) {
+    int64_t off = align_(16);
+    arena.resize(arena.size() + n);
+    std::memcpy(arena.data() + off, p, n);
+    return off;
+}
+
+void Planner::finish() {
+    const size_t np = pending.size();
+    probs.assign(np, PqgProblem{});
+    item_begin.assign(np + 1, 0);
+    chunks.clear();
+    arena.clear();
+    table_cache_.clear();
+    total_items = total_parts = total_outputs = 0;
+    total_steps = total_flops = 0.0;
+    max_nc = 1;
+
+    double S_tot = 0.0;
+    for (auto &p : pending)
+        if (p.kind == PQG_KIND_WALK) S_tot += p.S;
+    // longest inner walk such that the whole plan still has about
+    // items_per_smsp warps of work per SM sub-partition
+    const double lanes_wanted = 32.0 * 4.0 * cfg_.num_sms * static_cast<double>(cfg_.items_per_smsp);
+    double p_cap = S_tot / lanes_wanted;
+    p_cap = std::min<double>(std::max<double>(p_cap, static_cast<double>(cfg_.p_min)), static_cast<double>(cfg_.p_max));
+
+    const bool c128 = prec_ == Precision::C128;
+    const size_t cplx = c128 ? 16 : 8;
+
+    // One walk kernel serves the whole plan and is compiled for an exact column
+    // count, so every problem of a plain-form batch is padded to the largest
+    // column count with neutral columns: multiplicity 1, column sum exactly
+    // 1 + 0i at every step (zero rows), so each term is multiplied by 1 exactly.
+    if (form_ == Form::PLAIN) {
+        int ncmax = 1;
+        for (auto &p : pending)
+            if (p.kind == PQG_KIND_WALK) ncmax = std::max(ncmax, p.nc);
+        for (auto &p : pending) {
+            if (p.kind != PQG_KIND_WALK || p.nc == ncmax) continue;
+            const int old = p.nc, add = ncmax - old;
+            p.cm.resize(ncmax, 1);
+            p.a0.resize(2 * ncmax, 0.0);
+            for (int k = old; k < ncmax; ++k) p.a0[2 * k] = 1.0;
+            std::vector<double> rows;
+            rows.reserve(p.m.size() * 2 * ncmax);
+            for (size_t i = 0; i < p.m.size(); ++i) {
+                rows.insert(rows.end(), p.rows.begin() + i * 2 * old, p.rows.begin() + (i + 1) * 2 * old);
+                rows.insert(rows.end(), static_cast<size_t>(2 * add), 0.0);
+            }
+            p.rows.swap(rows);
+            p.nc = ncmax;
+            p.padded_cols = add;
+        }
+    }
+
+    for (size_t ip = 0; ip < np; ++ip) {
+        PendingProblem &p = pending[ip];
+        PqgProblem &q = probs[ip];
+        std::memset(&q, 0, sizeof(q));
+        q.kind = p.kind;
+        q.n_out = p.n_out;
+        q.out_index = total_outputs;
+        total_outputs += p.n_out;
+        q.item_begin = total_items;
+        q.part_begin = total_parts;
+        q.chunk_begin = static_cast<int64_t>(chunks.size());
+        if (p.kind == PQG_KIND_CONSTANT) {
+            q.cval_re = p.cre;
+            q.cval_im = p.cim;
+            q.P = 1;
+            item_begin[ip + 1] = total_items;
+            continue;
+        }
+        q.nc = p.nc;
+        max_nc = std::max(max_nc, p.nc);
+        q.scale_exp = p.scale_exp;
+        int cm_max = 1;
+        for (int k = 0; k < p.nc; ++k) {
+            q.cm[k] = static_cast<uint8_t>(p.cm[k]);
+            cm_max = std::max(cm_max, p.cm[k]);
+        }
+        q.cm_max = cm_max;
+
+        // inner digits: ascending multiplicity, greedily while the walk fits
+        // both the global cap and a full warp of outer assignments
+        const int nd = static_cast<int>(p.m.size());
+        std::vector<int> order(nd);
+        for (int i = 0; i < nd; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return p.m[x] < p.m[y]; });
+        double target = std::min(p_cap, std::max(1.0, p.S / 32.0));
+        std::vector<int> inner, outer;
+        double P = 1.0;
+        for (int i : order) {
+            if (P * (p.m[i] + 1) <= target && outer.empty())
+            {
+                inner.push_back(i);
+                P *= (p.m[i] + 1);
+            } else {
+                outer.push_back(i);
+            }
+        }
+        if (static_cast<int>(outer.size()) > PQG_MAX_OUTER) {
+            // cannot happen below 2^50 steps with radix >= 2 and <= 60 digits
+            outer.resize(PQG_MAX_OUTER);
+        }
+        q.P = static_cast<int32_t>(P);
+        q.n_outer = static_cast<int32_t>(outer.size());
+        double Q = p.S / P;
+        q.Q = static_cast<int64_t>(std::llround(Q));
+        for (size_t o = 0; o < outer.size(); ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
+
+        // FP64 seed: column sums with every digit at 0, a0 + sum_i m_i a_i
+        std::vector<double> base(2 * p.nc);
+        for (int k = 0; k < 2 * p.nc; ++k) {
+            Kahan2 s;
+            s.add(p.a0[k]);
+            for (int i = 0; i < nd; ++i) s.add(static_cast<double>(p.m[i]) * p.rows[static_cast<size_t>(i) * 2 * p.nc + k]);
+            base[k] = s.value();
+        }
+        q.off_base = push_bytes_(base.data(), base.size() * sizeof(double));
+        std::vector<double> orow;
+        orow.reserve(outer.size() * 2 * p.nc);
+        for (int i : outer)
+            for (int k = 0; k < 2 * p.nc; ++k) orow.push_back(p.rows[static_cast<size_t>(i) * 2 * p.nc + k]);
+        q.off_outer = orow.empty() ? q.off_base : push_bytes_(orow.data(), orow.size() * sizeof(double));
+
+        // D rows of the inner digits, in kernel precision
+        const size_t K = inner.size();
+        if (c128) {
+            std::vector<double> D(std::max<size_t>(1, 2 * K) * 2 * p.nc, 0.0);
+            for (size_t k = 0; k < K; ++k)
+                for (int c = 0; c < 2 * p.nc; ++c) {
+                    double v = 2.0 * p.rows[static_cast<size_t>(inner[k]) * 2 * p.nc + c];
+                    D[(2 * k) * 2 * p.nc + c] = -v;
+                    D[(2 * k + 1) * 2 * p.nc + c] = v;
+                }
+            q.off_D = push_bytes_(D.data(), D.size() * sizeof(double));
+        } else {
+            std::vector<float> D(std::max<size_t>(1, 2 * K) * 2 * p.nc, 0.0f);
+            for (size_t k = 0; k < K; ++k)
+                for (int c = 0; c < 2 * p.nc; ++c) {
+                    double v = 2.0 * p.rows[static_cast<size_t>(inner[k]) * 2 * p.nc + c];
+                    D[(2 * k) * 2 * p.nc + c] = static_cast<float>(-v);
+                    D[(2 * k + 1) * 2 * p.nc + c] = static_cast<float>(v);
+                }
+            q.off_D = push_bytes_(D.data(), D.size() * sizeof(float));
+        }
+
+        // inner step table: keyed by (precision, nc, inner multiplicities);
+        // the reflected mixed-radix Gray code from 0, digit 0 fastest
+        std::vector<int> key;
+        key.push_back(c128 ? 1 : 0);
+        key.push_back(p.nc);
+        for (int i : inner) key.push_back(p.m[i]);
+        auto it = table_cache_.find(key);
+        if (it != table_cache_.end()) {
+            q.off_tab = it->second;
+        } else {
+            const int64_t PP = q.P;
+            std::vector<int> lim(K), chain(K, 0), code(K, 0), mm(K);
+            for (size_t k = 0; k < K; ++k) {
+                mm[k] = p.m[inner[k]];
+                lim[k] = mm[k] + 1;
+            }
+            std::vector<double> w(PP);
+            std::vector<int32_t> drow(PP, 0);
+            w[0] = 1.0;
+            int64_t bc = 1;
+            int parity = 0;
+            for (int64_t t = 1; t < PP; ++t) {
+                size_t k = 0;
+                while (true) {
+                    if (chain[k] < lim[k] - 1) {
+                        chain[k]++;
+                        break;
+                    }
+                    chain[k] = 0;
+                    ++k;
+                }
+                int par = 0, ch = -1, prev = 0, val = 0;
+                for (int i = static_cast<int>(K) - 1; i >= 0; --i) {
+                    int c = par ? lim[i] - 1 - chain[i] : chain[i];
+                    par ^= (c & 1);
+                    if (c != code[i] && ch < 0) {
+                        ch = i;
+                        prev = code[i];
+                        val = c;
+                    }
+                }
+                code[ch] = val;
+                parity ^= 1;
+                bc = val > prev ? bc * (mm[ch] - prev) / val : bc * prev / (mm[ch] - val);
+                w[t] = (parity ? -1.0 : 1.0) * static_cast<double>(bc);
+                drow[t] = static_cast<int32_t>((2 * ch + (val > prev ? 0 : 1)) * p.nc);
+            }
+            if (c128) {
+                std::vector<PqgStep128> tab(PP);
+                for (int64_t t = 0; t < PP; ++t) tab[t] = PqgStep128{w[t], drow[t], 0};
+                q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep128));
+            } else {
+                std::vector<PqgStep64> tab(PP);
+                for (int64_t t = 0; t < PP; ++t) tab[t] = PqgStep64{static_cast<float>(w[t]), drow[t]};
+                q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep64));
+            }
+            table_cache_[key] = q.off_tab;
+        }
+
+        q.n_items = (q.Q + PQG_ITEM_LANES - 1) / PQG_ITEM_LANES;
+        total_items += q.n_items;
+        total_parts += q.n_items * q.n_out;
+        item_begin[ip + 1] = total_items;
+        // level-1 reduction chunks of at most 512 items
+        const int64_t per_chunk = 512;
+        for (int64_t lo = q.item_begin; lo < q.item_begin + q.n_items; lo += per_chunk) {
+            PqgChunk c{};
+            c.item_lo = lo;
+            c.item_hi = std::min(lo + per_chunk, q.item_begin + q.n_items);
+            c.problem = static_cast<int32_t>(ip);
+            chunks.push_back(c);
+        }
+        q.n_chunks = static_cast<int64_t>(chunks.size()) - q.chunk_begin;
+        total_steps += p.S;
+        total_flops += algorithmic_flops(p, form_);
+        (void)cplx;
+    }
+    item_begin[np] = total_items;
+    align_(16);
+}
+
+}  // namespace pqg

@@ -1,0 +1,83 @@
+// Host-side planner: turns (matrix, row multiplicities, column multiplicities)
+// problems into the device work plan described in pqg_plan.h.
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pqg_plan.h"
+
+namespace pqg {
+
+enum class Precision { C128, C64 };
+enum class Form { PLAIN, LAPLACE };
+
+struct PlanConfig {
+    int num_sms = 152;
+    int64_t items_per_smsp = 16;  // work items per SM sub-partition the split aims for
+    int64_t p_min = 64;           // shortest inner walk when the space is large
+    int64_t p_max = 2048;         // longest inner walk (table length)
+};
+
+// One reduced problem before its inner/outer split is fixed.
+struct PendingProblem {
+    int kind = PQG_KIND_WALK;
+    double cre = 1.0, cim = 0.0;
+    int nc = 0;
+    std::vector<int> cm;          // multiplicities of the kept columns
+    std::vector<double> a0;       // 2*nc: the prepended row (multiplicity 1)
+    std::vector<int> m;           // digit multiplicities (>= 1)
+    std::vector<double> rows;     // digits x 2*nc
+    int scale_exp = 0;
+    int n_out = 1;
+    bool laplace_full = false;    // Laplace form with a zero-multiplicity column
+    std::vector<int> out_map;     // Laplace: output slot of every original column
+    double S = 1.0;               // Gray-code space size
+    int padded_cols = 0;          // neutral columns added to reach the plan's column count
+};
+
+class Planner {
+  public:
+    Planner(Precision prec, Form form, const PlanConfig &cfg) : prec_(prec), form_(form), cfg_(cfg) {}
+
+    // Adds one problem; `a` is interleaved complex128 (the complex64 entry
+    // points widen their input first: the seeds are formed in FP64).
+    // Returns PQG_OK or an error status with `err` set.
+    int add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
+            std::string &err);
+
+    // Fixes every problem's split and lays out the arena.
+    void finish();
+
+    void set_config(const PlanConfig &cfg) { cfg_ = cfg; }
+
+    std::vector<PendingProblem> pending;
+    std::vector<PqgProblem> probs;
+    std::vector<int64_t> item_begin;   // n_probs + 1
+    std::vector<PqgChunk> chunks;
+    std::vector<unsigned char> arena;  // data referenced by byte offsets
+    int64_t total_items = 0;
+    int64_t total_parts = 0;           // dd-complex partial slots
+    int64_t total_outputs = 0;
+    int max_nc = 0;
+    double total_steps = 0.0;          // sum over problems of the Gray-code space
+    double total_flops = 0.0;          // algorithmic flop count, see algorithmic_flops()
+
+    Precision precision() const { return prec_; }
+    Form form() const { return form_; }
+
+  private:
+    Precision prec_;
+    Form form_;
+    PlanConfig cfg_;
+    std::map<std::vector<int>, int64_t> table_cache_;
+    int64_t align_(size_t a);
+    int64_t push_bytes_(const void *p, size_t n);
+};
+
+// Algorithmic flops of one problem: S * (4*c + 6*sum(cols) + 4) for the plain
+// permanent (c column-sum updates of 4 flops, one complex multiply of 6 flops
+// per factor, 4 flops for the weighted accumulation).
+double algorithmic_flops(const PendingProblem &p, Form form);
+
+}  // namespace pqg

@@ -1,0 +1,318 @@
+// Laplace-expansion walk kernels: for every column l, the permanent with the
+// multiplicity of column l lowered by one, all from ONE Gray-code walk
+// (Lemma 1 of arXiv:2005.04214, as the reference's
+// src/permanent_laplace.cpp:43-240).  The reference forms each of the nc
+// products separately, O(nc * N) multiplies per step; here a prefix pass and
+// a suffix pass give all nc products in O(nc):
+//     out_l += w * prefix_l * suffix_l * c_l^(m_l - 1),
+// and the final suffix w * prod_l c_l^(m_l) is the value shared by every
+// column of multiplicity zero (their exponent stays 0 in the reference).
+// Work split, seeding and reductions are those of the plain kernels.
+#pragma once
+#include "walk_common.cuh"
+
+namespace pqg {
+
+// Per-thread arrays that live either in registers or in a column-major slice
+// of dynamic shared memory (stride = threads per block).
+template <typename T, int N, bool SMEM>
+struct LaneArray;
+
+template <typename T, int N>
+struct LaneArray<T, N, false> {
+    T v[N];
+    __device__ __forceinline__ void init(T *, int) {}
+    __device__ __forceinline__ T get(int j) const { return v[j]; }
+    __device__ __forceinline__ void set(int j, T x) { v[j] = x; }
+};
+
+template <typename T, int N>
+struct LaneArray<T, N, true> {
+    T *p;
+    __device__ __forceinline__ void init(T *base, int tid) { p = base + tid; }
+    __device__ __forceinline__ T get(int j) const { return p[j * PQG_WALK_THREADS]; }
+    __device__ __forceinline__ void set(int j, T x) { p[j * PQG_WALK_THREADS] = x; }
+};
+
+template <int NC>
+struct LaplaceC128Cfg {
+    static constexpr bool PRE_SMEM = NC > 16;
+    static constexpr bool ACC_SMEM = NC > 20;
+    static constexpr size_t smem_bytes =
+        (PRE_SMEM ? size_t(NC) * PQG_WALK_THREADS * sizeof(double2) : 0) +
+        (ACC_SMEM ? size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) : 0);
+};
+
+// Complex128 Laplace walk.  Per-lane sums are plain FP64 over one inner walk
+// (at most 512 steps), combined across lanes, items and chunks in double-double.
+template <int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c128(WalkArgs A) {
+    using Cfg = LaplaceC128Cfg<NC>;
+    extern __shared__ double2 lap_smem[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<double2, NC, Cfg::PRE_SMEM> pre;
+    LaneArray<double2, NC + 1, Cfg::ACC_SMEM> acc;
+    pre.init(lap_smem, threadIdx.x);
+    acc.init(lap_smem + (Cfg::PRE_SMEM ? NC * PQG_WALK_THREADS : 0), threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t q = local * PQG_ITEM_LANES + lane;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        double wout = 0.0;
+        if (q < pr->Q) {
+            double cr[NC], ci[NC];
+            wout = seed_outer<NC>(pr, A.arena, q, cr, ci);
+            int cm[NC];
+#pragma unroll
+            for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
+            const bool ones = pr->cm_max == 1;
+            const PqgStep128 *tab = reinterpret_cast<const PqgStep128 *>(A.arena + pr->off_tab);
+            const double2 *D = reinterpret_cast<const double2 *>(A.arena + pr->off_D);
+            const int P = pr->P;
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) acc.set(l, make_double2(0.0, 0.0));
+
+            for (int t = 0; t < P; ++t) {
+                const double w = __ldg(&tab[t].w);
+                if (t > 0) {
+                    const double2 *d = D + __ldg(&tab[t].drow);
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) {
+                        const double2 v = __ldg(d + j);
+                        cr[j] = __dadd_rn(cr[j], v.x);
+                        ci[j] = __dadd_rn(ci[j], v.y);
+                    }
+                }
+                // prefix products: pre_l = prod_{k<l} c_k^(m_k)
+                double xr = 1.0, xi = 0.0;
+                pre.set(0, make_double2(1.0, 0.0));
+#pragma unroll
+                for (int j = 0; j + 1 < NC; ++j) {
+                    if (j == 0 && (ones || cm[0] == 1)) {
+                        xr = cr[0];
+                        xi = ci[0];
+                    } else {
+                        const int e = ones ? 1 : cm[j];
+                        for (int r = 0; r < e; ++r) cmul(xr, xi, cr[j], ci[j]);
+                    }
+                    pre.set(j + 1, make_double2(xr, xi));
+                }
+                // suffix pass
+                double sr = w, si = 0.0;
+#pragma unroll
+                for (int l = NC - 1; l >= 0; --l) {
+                    const double2 p = pre.get(l);
+                    double tr, ti;
+                    if (l == NC - 1) {
+                        tr = p.x * w;
+                        ti = p.y * w;
+                    } else if (l == 0) {
+                        tr = sr;
+                        ti = si;
+                    } else {
+                        tr = p.x;
+                        ti = p.y;
+                        cmul(tr, ti, sr, si);
+                    }
+                    if (!ones)
+                        for (int r = 1; r < cm[l]; ++r) cmul(tr, ti, cr[l], ci[l]);
+                    double2 a = acc.get(l);
+                    a.x = __dadd_rn(a.x, tr);
+                    a.y = __dadd_rn(a.y, ti);
+                    acc.set(l, a);
+                    if (l > 0 || full) {
+                        if (l == NC - 1) {
+                            sr = w * cr[l];
+                            si = w * ci[l];
+                            if (!ones)
+                                for (int r = 1; r < cm[l]; ++r) cmul(sr, si, cr[l], ci[l]);
+                        } else {
+                            const int e = ones ? 1 : cm[l];
+                            for (int r = 0; r < e; ++r) cmul(sr, si, cr[l], ci[l]);
+                        }
+                    }
+                }
+                if (full) {
+                    double2 a = acc.get(NC);
+                    a.x = __dadd_rn(a.x, sr);
+                    a.y = __dadd_rn(a.y, si);
+                    acc.set(NC, a);
+                }
+            }
+        }
+        // one output at a time: scale, reduce over the warp, store
+        // (unrolled so that a register-resident accumulator array keeps static indices)
+#pragma unroll
+        for (int l = 0; l <= NC; ++l) {
+            if (l >= n_out) break;
+            ddv r{0.0, 0.0}, i{0.0, 0.0};
+            if (q < pr->Q) {
+                const double2 a = acc.get(l);
+                r = dd_mul_d(ddv{a.x, 0.0}, wout);
+                i = dd_mul_d(ddv{a.y, 0.0}, wout);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r = dd_add(r, dd_shfl_down(r, off));
+                i = dd_add(i, dd_shfl_down(i, off));
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+        }
+    }
+}
+
+template <int NC>
+struct LaplaceC64Cfg {
+    static constexpr bool PRE_SMEM = NC > 16;
+    static constexpr size_t smem_bytes =
+        (PRE_SMEM ? size_t(NC) * PQG_WALK_THREADS * sizeof(float2) : 0) +
+        size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2);
+};
+
+// Complex64 Laplace walk: FP32 updates and products, FP32 partial sums over
+// 32 steps folded into per-lane FP64 sums held in shared memory.
+template <int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c64(WalkArgs A) {
+    using Cfg = LaplaceC64Cfg<NC>;
+    extern __shared__ double2 lap_smem64[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<double2, NC + 1, true> acc64;
+    acc64.init(lap_smem64, threadIdx.x);
+    LaneArray<float2, NC, Cfg::PRE_SMEM> pre;
+    pre.init(reinterpret_cast<float2 *>(lap_smem64 + (NC + 1) * PQG_WALK_THREADS), threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t q = local * PQG_ITEM_LANES + lane;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        double wout = 0.0;
+        if (q < pr->Q) {
+            float cr[NC], ci[NC];
+            {
+                double dr[NC], di[NC];
+                wout = seed_outer<NC>(pr, A.arena, q, dr, di);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    cr[j] = __double2float_rn(dr[j]);
+                    ci[j] = __double2float_rn(di[j]);
+                }
+            }
+            int cm[NC];
+#pragma unroll
+            for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
+            const bool ones = pr->cm_max == 1;
+            const PqgStep64 *tab = reinterpret_cast<const PqgStep64 *>(A.arena + pr->off_tab);
+            const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
+            const int P = pr->P;
+            float ar[NC + 1], ai[NC + 1];
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) {
+                ar[l] = 0.0f;
+                ai[l] = 0.0f;
+                acc64.set(l, make_double2(0.0, 0.0));
+            }
+
+            for (int t = 0; t < P; ++t) {
+                const float2 e = __ldg(reinterpret_cast<const float2 *>(tab + t));
+                const float w = e.x;
+                if (t > 0) {
+                    const float2 *d = D + __float_as_int(e.y);
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) {
+                        const float2 v = __ldg(d + j);
+                        cr[j] = __fadd_rn(cr[j], v.x);
+                        ci[j] = __fadd_rn(ci[j], v.y);
+                    }
+                }
+                float xr = 1.0f, xi = 0.0f;
+                pre.set(0, make_float2(1.0f, 0.0f));
+#pragma unroll
+                for (int j = 0; j + 1 < NC; ++j) {
+                    if (j == 0 && (ones || cm[0] == 1)) {
+                        xr = cr[0];
+                        xi = ci[0];
+                    } else {
+                        const int ee = ones ? 1 : cm[j];
+                        for (int r = 0; r < ee; ++r) cmulf(xr, xi, cr[j], ci[j]);
+                    }
+                    pre.set(j + 1, make_float2(xr, xi));
+                }
+                float sr = w, si = 0.0f;
+#pragma unroll
+                for (int l = NC - 1; l >= 0; --l) {
+                    const float2 p = pre.get(l);
+                    float tr, ti;
+                    if (l == NC - 1) {
+                        tr = p.x * w;
+                        ti = p.y * w;
+                    } else if (l == 0) {
+                        tr = sr;
+                        ti = si;
+                    } else {
+                        tr = p.x;
+                        ti = p.y;
+                        cmulf(tr, ti, sr, si);
+                    }
+                    if (!ones)
+                        for (int r = 1; r < cm[l]; ++r) cmulf(tr, ti, cr[l], ci[l]);
+                    ar[l] += tr;
+                    ai[l] += ti;
+                    if (l > 0 || full) {
+                        if (l == NC - 1) {
+                            sr = w * cr[l];
+                            si = w * ci[l];
+                            if (!ones)
+                                for (int r = 1; r < cm[l]; ++r) cmulf(sr, si, cr[l], ci[l]);
+                        } else {
+                            const int ee = ones ? 1 : cm[l];
+                            for (int r = 0; r < ee; ++r) cmulf(sr, si, cr[l], ci[l]);
+                        }
+                    }
+                }
+                if (full) {
+                    ar[NC] += sr;
+                    ai[NC] += si;
+                }
+                if ((t & 31) == 31 || t == P - 1) {
+#pragma unroll
+                    for (int l = 0; l <= NC; ++l) {
+                        if (l == NC && !full) continue;
+                        double2 a = acc64.get(l);
+                        a.x += static_cast<double>(ar[l]);
+                        a.y += static_cast<double>(ai[l]);
+                        acc64.set(l, a);
+                        ar[l] = 0.0f;
+                        ai[l] = 0.0f;
+                    }
+                }
+            }
+        }
+        for (int l = 0; l < n_out; ++l) {
+            ddv r{0.0, 0.0}, i{0.0, 0.0};
+            if (q < pr->Q) {
+                const double2 a = acc64.get(l);
+                r = dd_mul_d(ddv{a.x, 0.0}, wout);
+                i = dd_mul_d(ddv{a.y, 0.0}, wout);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r = dd_add(r, dd_shfl_down(r, off));
+                i = dd_add(i, dd_shfl_down(i, off));
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+        }
+    }
+}
+
+}  // namespace pqg

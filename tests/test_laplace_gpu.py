@@ -1,0 +1,84 @@
+"""GPU parity of ``permanent_laplace`` against the reference's outputs and the
+double-double oracle, and the reference's seeded sampler golden driven by it.
+
+Tolerance: complex128 max(1e-10*|L_l|, 1e-14*perm(|A|) with column l lowered);
+complex64 max(1e-5*|L_l|, 2^-23*perm(|A|)).
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import as_complex, as_matrix, haar_unitary, load_golden
+from oracle import sampler as osampler
+
+pytestmark = pytest.mark.gpu
+
+
+def _abs_scales(A, rows, cols):
+    A = np.abs(np.asarray(A, dtype=np.complex128)).astype(np.complex128)
+    out = []
+    for l in range(len(cols)):
+        c = np.array(cols).copy()
+        c[l] = max(c[l] - 1, 0)
+        out.append(abs(oracle.permanent_laplace_dd(A, rows, np.array(cols))[l]))
+    return np.array(out)
+
+
+def _check(engine, A, rows, cols, ref=None):
+    A = np.asarray(A)
+    got = engine.permanent_laplace(A, rows, cols)
+    dd = oracle.permanent_laplace_dd(np.asarray(A, dtype=np.complex128), rows, cols)
+    assert got.shape == dd.shape
+    scales = _abs_scales(A, rows, cols)
+    if A.dtype == np.complex64:
+        assert got.dtype == np.complex64
+        t = np.maximum(1e-5 * np.abs(dd), 2.0 ** -23 * scales)
+    else:
+        assert got.dtype == np.complex128
+        t = np.maximum(1e-10 * np.abs(dd), 1e-14 * scales)
+        if ref is not None:
+            assert np.all(np.abs(got - ref) <= t + 1e-300)
+    assert np.all(np.abs(got - dd) <= t + 1e-300), (got, dd, t)
+    return got
+
+
+def test_reference_random_laplace(engine):
+    data = load_golden("random_cases.json")
+    for case in data["laplace"]:
+        A = as_matrix(case["matrix"])
+        ref = np.array([as_complex(z) for z in case["result"]])
+        got = _check(engine, A, case["rows"], case["cols"], ref if A.dtype == np.complex128 else None)
+        assert str(got.dtype) == case["result_dtype"]
+
+
+@pytest.mark.parametrize("k", [2, 5, 9, 14, 18])
+def test_sampler_shaped_laplace(engine, k):
+    # step k of the sampler: (k-1) output photons over k input columns
+    rng = np.random.default_rng(k)
+    d = 2 * k + 2
+    U = haar_unitary(d, k)
+    cols = np.ones(k, dtype=int)
+    sample = np.bincount(rng.integers(0, d, k - 1), minlength=d)
+    A = U[:, :k][sample > 0].copy()
+    rows = sample[sample > 0]
+    _check(engine, A, rows, cols)
+    _check(engine, A.astype(np.complex64), rows, cols)
+
+
+def test_laplace_edge_cases(engine):
+    assert np.array_equal(engine.permanent_laplace(np.eye(2), [0, 0], [1, 1]), np.array([1.0 + 0j]))
+    assert engine.permanent_laplace(np.eye(2, dtype=np.complex64), [1, 0], [1, 1]).dtype == np.complex64
+    # a zero-multiplicity column keeps exponent 0 (reference semantics)
+    A = haar_unitary(4, 1)[:3].copy()
+    _check(engine, A, [1, 1, 0], [1, 2, 0, 0])
+    # repeated columns
+    _check(engine, A, [2, 1, 1], [2, 1, 2, 0])
+
+
+def test_seeded_sampler_golden(engine):
+    g = load_golden("sampler_seeded.json")
+    U = as_matrix(g["U"])
+    samples = osampler.generate_samples(np.array(g["input"]), g["shots"], engine.permanent_laplace, U, g["seed"])
+    assert [list(s) for s in samples] == g["generated_samples"]
+    assert [list(s) for s in osampler.result_samples(samples, g["seed"])] == g["expected_samples"]
