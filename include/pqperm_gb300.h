@@ -80,6 +80,18 @@ int pqg_permanent_laplace_c128(const double *matrix, int64_t n_rows, int64_t n_c
 int pqg_permanent_laplace_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                               const int32_t *cols, float *out, int64_t *n_out);
 
+/* Batched Laplace permanents of one matrix, one walk launch for the batch:
+ * problem b uses rows[b*n_rows ...] and cols[b*n_cols ...] and writes
+ * 2*max(n_cols,1) values at out + 2*max(n_cols,1)*b; n_out (nullable, batch
+ * entries) receives each problem's count (1 for an empty problem, whose single
+ * value is 1).  Replaces the per-step permanent_laplace calls of the
+ * reference's sampler (piquasso/_simulators/passive/sampling.py:723-749),
+ * batched over independent shots. */
+int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                                     const int32_t *cols, int64_t batch, double *out, int64_t *n_out);
+int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                                    const int32_t *cols, int64_t batch, float *out, int64_t *n_out);
+
 /* Measured FP64 / FP32 fused-multiply-add throughput of device 0 in TFLOP/s
  * (2 flops per FMA), from dependent-chain microkernels run over all SMs for
  * about `ms` milliseconds each.  out2 = {fp64_tflops, fp32_tflops}. */

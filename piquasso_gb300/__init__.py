@@ -15,6 +15,7 @@ from .permanent import (  # noqa: F401
     permanent_batch,
     permanent_dd,
     permanent_laplace,
+    permanent_laplace_batch,
 )
 from ._lib import EngineUnavailable, kernel_launches, last_timing  # noqa: F401
 

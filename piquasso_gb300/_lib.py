@@ -40,6 +40,8 @@ SIGNATURES = {
     "pqg_permanent_batch_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f], ctypes.c_int),
     "pqg_permanent_laplace_c128": ([_d, _I64, _I64, _i32, _i32, _d, _i64], ctypes.c_int),
     "pqg_permanent_laplace_c64": ([_f, _I64, _I64, _i32, _i32, _f, _i64], ctypes.c_int),
+    "pqg_permanent_laplace_batch_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _d, _i64], ctypes.c_int),
+    "pqg_permanent_laplace_batch_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f, _i64], ctypes.c_int),
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),
     "pqg_last_timing": ([_d, _d, _d, _d, _d, _d], ctypes.c_int),
 }

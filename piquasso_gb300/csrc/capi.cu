@@ -251,40 +251,56 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     return run_plan<T>(C, pl, out, out_lo);
 }
 
+// Laplace permanents of `batch` problems sharing one matrix; problem b writes
+// 2*nc values at out + 2*nc*b (its count, 1 or nc, to n_out[b]).
 template <typename T>
-int laplace_one(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
-                Precision prec, T *out, int64_t *n_out) {
-    if (nr < 0 || nc < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
+int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
+                  int64_t batch, Precision prec, T *out, int64_t *n_out) {
+    if (nr < 0 || nc < 0 || batch < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
     PlanConfig cfg = C.cfg;
     cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
     Planner pl(prec, Form::LAPLACE, cfg);
-    std::string err;
-    int st = pl.add(matrix, nr, nc, rows, cols, err);
-    if (st) return fail(st, err);
-    st = C.init();
+    for (int64_t b = 0; b < batch; ++b) {
+        std::string err;
+        int st = pl.add(matrix, nr, nc, rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
+        if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
+    }
+    int st = C.init();
     if (st) return st;
     cfg.num_sms = C.cfg.num_sms;
     pl.set_config(cfg);
     pl.finish();
-    const PendingProblem &pp = pl.pending[0];
     std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
     st = run_plan<T>(C, pl, res.data(), nullptr);
     if (st) return st;
-    if (pp.kind == PQG_KIND_CONSTANT) {
-        out[0] = res[0];
-        out[1] = res[1];
-        if (n_out) *n_out = 1;
-        return PQG_OK;
+    const int64_t stride = 2 * std::max<int64_t>(1, nc);
+    for (int64_t b = 0; b < batch; ++b) {
+        const PendingProblem &pp = pl.pending[static_cast<size_t>(b)];
+        const int64_t oi = pl.probs[static_cast<size_t>(b)].out_index;
+        T *o = out + b * stride;
+        if (pp.kind == PQG_KIND_CONSTANT) {
+            for (int64_t j = 0; j < stride; ++j) o[j] = T(0);
+            o[0] = res[2 * oi];
+            o[1] = res[2 * oi + 1];
+            if (n_out) n_out[b] = 1;
+            continue;
+        }
+        for (int64_t j = 0; j < nc; ++j) {
+            const int slot = pp.out_map[static_cast<size_t>(j)];
+            o[2 * j] = res[2 * (oi + slot)];
+            o[2 * j + 1] = res[2 * (oi + slot) + 1];
+        }
+        if (n_out) n_out[b] = nc;
     }
-    for (int64_t j = 0; j < nc; ++j) {
-        const int slot = pp.out_map[static_cast<size_t>(j)];
-        out[2 * j] = res[2 * slot];
-        out[2 * j + 1] = res[2 * slot + 1];
-    }
-    if (n_out) *n_out = nc;
     return PQG_OK;
+}
+
+template <typename T>
+int laplace_one(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
+                Precision prec, T *out, int64_t *n_out) {
+    return laplace_batch<T>(matrix, nr, nc, rows, cols, 1, prec, out, n_out);
 }
 
 // ------------------------------------------------------------ peak probes
@@ -379,6 +395,18 @@ int pqg_permanent_laplace_c64(const float *matrix, int64_t n_rows, int64_t n_col
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return laplace_one<float>(m.data(), n_rows, n_cols, rows, cols, Precision::C64, out, n_out);
+}
+
+int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                                     const int32_t *cols, int64_t batch, double *out, int64_t *n_out) {
+    return laplace_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, Precision::C128, out, n_out);
+}
+
+int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                                    const int32_t *cols, int64_t batch, float *out, int64_t *n_out) {
+    if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
+    std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
+    return laplace_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out, n_out);
 }
 
 int pqg_measure_vector_peaks(double ms, double *out2) {

@@ -207,10 +207,12 @@ void Planner::finish() {
     const size_t cplx = c128 ? 16 : 8;
 
     // One walk kernel serves the whole plan and is compiled for an exact column
-    // count, so every problem of a plain-form batch is padded to the largest
-    // column count with neutral columns: multiplicity 1, column sum exactly
-    // 1 + 0i at every step (zero rows), so each term is multiplied by 1 exactly.
-    if (form_ == Form::PLAIN) {
+    // count, so every problem of a batch is padded to the largest column count
+    // with neutral columns: multiplicity 1, column sum exactly 1 + 0i at every
+    // step (zero rows), so each term is multiplied by 1 exactly.  In the
+    // Laplace form a neutral column's own output is never read, and the shared
+    // output of the zero-multiplicity columns moves behind the padded ones.
+    {
         int ncmax = 1;
         for (auto &p : pending)
             if (p.kind == PQG_KIND_WALK) ncmax = std::max(ncmax, p.nc);
@@ -229,6 +231,11 @@ void Planner::finish() {
             p.rows.swap(rows);
             p.nc = ncmax;
             p.padded_cols = add;
+            if (form_ == Form::LAPLACE) {
+                for (int &slot : p.out_map)
+                    if (slot == old) slot = ncmax;
+                p.n_out = ncmax + (p.laplace_full ? 1 : 0);
+            }
         }
     }
 

@@ -196,3 +196,34 @@ def measure_vector_peaks(ms=20.0):
     if st:
         _raise_for(st)
     return {"fp64_tflops": float(out[0]), "fp32_tflops": float(out[1])}
+
+
+def permanent_laplace_batch(matrix, rows, cols):
+    """Laplace permanents of one matrix for many multiplicity patterns at once.
+
+    ``rows`` (batch, n_rows), ``cols`` (batch, n_cols).  Returns a
+    (batch, n_cols) array; an empty problem (no photons) yields 1 in column 0
+    and zeros elsewhere, matching the reference's one-element ``[1]``.
+    """
+    m = _as_matrix(matrix)
+    R = np.ascontiguousarray(np.asarray(rows).astype(np.int32, casting="unsafe"))
+    C = np.ascontiguousarray(np.asarray(cols).astype(np.int32, casting="unsafe"))
+    if R.ndim != 2 or R.shape[1] != m.shape[0] or C.shape != (R.shape[0], m.shape[1]):
+        raise PermanentInputError("rows must be (batch, %d) and cols (batch, %d)" % m.shape)
+    batch = R.shape[0]
+    nc = max(1, m.shape[1])
+    L = _lib.load()
+    single = m.dtype == np.complex64
+    out = np.zeros(2 * nc * batch, dtype=np.float32 if single else np.float64)
+    if single:
+        st = L.pqg_permanent_laplace_batch_c64(_ptr(m, ctypes.c_float), m.shape[0], m.shape[1],
+                                               _ptr(R, ctypes.c_int32), _ptr(C, ctypes.c_int32), batch,
+                                               _ptr(out, ctypes.c_float), None)
+    else:
+        st = L.pqg_permanent_laplace_batch_c128(_ptr(m, ctypes.c_double), m.shape[0], m.shape[1],
+                                                _ptr(R, ctypes.c_int32), _ptr(C, ctypes.c_int32), batch,
+                                                _ptr(out, ctypes.c_double), None)
+    if st:
+        _raise_for(st)
+    o = out.reshape(batch, nc, 2)
+    return (o[..., 0] + 1j * o[..., 1]).astype(np.complex64 if single else np.complex128)
