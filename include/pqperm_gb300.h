@@ -36,8 +36,11 @@ extern "C" {
 #define PQG_ERR_NO_DEVICE 5    /* no CUDA device visible */
 
 /* precision modes for the complex128 entry points */
-#define PQG_MODE_AUTO 0 /* the default: native FP64 (PQG_MODE_FP64) */
-#define PQG_MODE_FP64 1 /* row sums, updates and products in FP64; double-double sums */
+#define PQG_MODE_AUTO 0 /* default: PQG_MODE_DF where valid (<= 32 particles), else FP64;
+                           the environment variable PQG_C128_MODE=fp64 forces FP64 */
+#define PQG_MODE_FP64 1 /* column sums, updates and products in FP64; double-double sums */
+#define PQG_MODE_DF 2   /* FP64 seeds and double-double sums; updates and products in
+                           double-float (FP32 pairs, ~2^-48 relative per operation) */
 
 /* Message describing the calling thread's last failure ("" if none). */
 const char *pqg_last_error(void);
@@ -91,6 +94,34 @@ int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64
                                      const int32_t *cols, int64_t batch, double *out, int64_t *n_out);
 int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                                     const int32_t *cols, int64_t batch, float *out, int64_t *n_out);
+
+/* Plan handles: plan and upload a batch once, then execute it many times as
+ * one CUDA graph (queue reset, persistent walk, reductions) on the handle's
+ * own stream — the form used for repeated batches (exact probabilities of a
+ * fixed set of output patterns, benchmark loops).  `dtype`: 0 complex128, 1
+ * complex64; `form`: 0 plain permanents (2 values per problem), 1 Laplace
+ * permanents (2*max(n_cols,1) values per problem, laid out as
+ * pqg_permanent_laplace_batch_*); `mode` as for the complex128 entry points.
+ * pqg_plan_launch enqueues one execution and returns; pqg_plan_synchronize
+ * waits for it and reports its device time; pqg_plan_read copies the results
+ * of the last completed execution to host memory.  A handle is used by one
+ * thread at a time. */
+typedef struct pqg_plan_s pqg_plan_t;
+int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
+                    int64_t batch, int32_t dtype, int32_t form, int32_t mode, pqg_plan_t **out_plan);
+int pqg_plan_launch(pqg_plan_t *plan);
+int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms);
+int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values);
+int pqg_plan_info(pqg_plan_t *plan, double *steps, double *flops, int64_t *work_items, int64_t *h2d_bytes);
+int pqg_plan_destroy(pqg_plan_t *plan);
+
+/* Work-split knobs of the planner (process-wide; 0 restores a default):
+ * items_per_smsp — warps of work per SM sub-partition the split aims for
+ * (default 16); p_max — longest inner walk, i.e. step-table length (default
+ * 2048, at most 32768); seed_steps — Gray-code steps per lane that amortise
+ * one seed (default depends on the arithmetic).  The autotuner sets these. */
+int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps);
+int pqg_get_tuning(int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps);
 
 /* Measured FP64 / FP32 fused-multiply-add throughput of device 0 in TFLOP/s
  * (2 flops per FMA), from dependent-chain microkernels run over all SMs for

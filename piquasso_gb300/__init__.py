@@ -17,6 +17,7 @@ from .permanent import (  # noqa: F401
     permanent_laplace,
     permanent_laplace_batch,
 )
-from ._lib import EngineUnavailable, kernel_launches, last_timing  # noqa: F401
+from .plan import PermanentPlan  # noqa: F401
+from ._lib import EngineUnavailable, get_tuning, kernel_launches, last_timing, set_tuning  # noqa: F401
 
 __version__ = "0.1.0"

@@ -21,6 +21,8 @@ PQG_ERR_NO_DEVICE = 5
 
 MODE_AUTO = 0
 MODE_FP64 = 1
+MODE_DF = 2
+MODES = {"auto": MODE_AUTO, "fp64": MODE_FP64, "df": MODE_DF}
 
 # (name, argtypes) of every symbol the header declares
 _d = ctypes.POINTER(ctypes.c_double)
@@ -42,6 +44,15 @@ SIGNATURES = {
     "pqg_permanent_laplace_c64": ([_f, _I64, _I64, _i32, _i32, _f, _i64], ctypes.c_int),
     "pqg_permanent_laplace_batch_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _d, _i64], ctypes.c_int),
     "pqg_permanent_laplace_batch_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f, _i64], ctypes.c_int),
+    "pqg_plan_create": ([ctypes.c_void_p, _I64, _I64, _i32, _i32, _I64, _I32, _I32, _I32,
+                         ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "pqg_plan_launch": ([ctypes.c_void_p], ctypes.c_int),
+    "pqg_plan_synchronize": ([ctypes.c_void_p, _d], ctypes.c_int),
+    "pqg_plan_read": ([ctypes.c_void_p, ctypes.c_void_p, _i64], ctypes.c_int),
+    "pqg_plan_info": ([ctypes.c_void_p, _d, _d, _i64, _i64], ctypes.c_int),
+    "pqg_plan_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "pqg_set_tuning": ([_I64, _I64, _I64], ctypes.c_int),
+    "pqg_get_tuning": ([_i64, _i64, _i64], ctypes.c_int),
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),
     "pqg_last_timing": ([_d, _d, _d, _d, _d, _d], ctypes.c_int),
 }
@@ -90,3 +101,16 @@ def last_timing():
     load().pqg_last_timing(*[ctypes.byref(x) for x in v])
     keys = ("walk_ms", "device_ms", "steps", "flops", "h2d_bytes", "d2h_bytes")
     return {k: x.value for k, x in zip(keys, v)}
+
+
+def set_tuning(items_per_smsp=0, p_max=0, seed_steps=0):
+    """Planner knobs (0 restores the default); see include/pqperm_gb300.h."""
+    st = load().pqg_set_tuning(int(items_per_smsp), int(p_max), int(seed_steps))
+    if st:
+        raise ValueError(last_error())
+
+
+def get_tuning():
+    v = [ctypes.c_int64(0) for _ in range(3)]
+    load().pqg_get_tuning(*[ctypes.byref(x) for x in v])
+    return {"items_per_smsp": v[0].value, "p_max": v[1].value, "seed_steps": v[2].value}

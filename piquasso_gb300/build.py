@@ -23,10 +23,16 @@ LIB = os.path.join(LIBDIR, "libpqperm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = [
     "capi.cu",
-    "k_plain_c128.cu",
-    "k_plain_c64.cu",
-    "k_laplace_c128.cu",
-    "k_laplace_c64.cu",
+    "k_plain_c128_0.cu",
+    "k_plain_c128_1.cu",
+    "k_plain_c64_0.cu",
+    "k_plain_c64_1.cu",
+    "k_plain_df_0.cu",
+    "k_plain_df_1.cu",
+    "k_laplace_c128_0.cu",
+    "k_laplace_c128_1.cu",
+    "k_laplace_c64_0.cu",
+    "k_laplace_c64_1.cu",
 ]
 CPP_SOURCES = ["plan.cpp"]
 

@@ -10,6 +10,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -18,6 +19,7 @@
 #include "../../include/pqperm_gb300.h"
 #include "kernel_table.h"
 #include "plan.hpp"
+#include "delta.cuh"
 #include "reduce.cuh"
 
 namespace pqg {
@@ -71,17 +73,23 @@ struct HostBuf {
     }
 };
 
+// Device buffers of one executable plan.
+struct DeviceBuffers {
+    DevBuf plan, partials, chunk_out, out, counter, delta;
+};
+
 struct Context {
     std::mutex mu;
+    DeviceBuffers bufs;
     bool ready = false;
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, evs = nullptr;
-    DevBuf plan, partials, chunk_out, out, counter;
     HostBuf h_plan, h_out;
     PlanConfig cfg;
-    std::vector<int> occ_cache[4];  // blocks per SM, per kernel table, per column count
+    int blocks_per_sm = 0;  // 0: as many as fit (occupancy)
+    std::vector<int> occ_cache[5];  // blocks per SM, per kernel table, per column count
 
     int init() {
         if (ready) return PQG_OK;
@@ -107,108 +115,195 @@ Context &ctx() {
     return c;
 }
 
-const KernelInfo *table_for(Form form, Precision prec, int *which) {
+// walk kernel for (form, precision, exact column count); `which` indexes the
+// occupancy cache
+const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, int *which) {
     if (form == Form::PLAIN) {
-        *which = prec == Precision::C128 ? 0 : 1;
-        return prec == Precision::C128 ? k_plain_c128 : k_plain_c64;
+        if (prec == Precision::C128DF) {
+            *which = 4;
+            return kernel_for(k_plain_df_0, k_plain_df_1, nc);
+        }
+        if (prec == Precision::C128) {
+            *which = 0;
+            return kernel_for(k_plain_c128_0, k_plain_c128_1, nc);
+        }
+        *which = 1;
+        return kernel_for(k_plain_c64_0, k_plain_c64_1, nc);
     }
-    *which = prec == Precision::C128 ? 2 : 3;
-    return prec == Precision::C128 ? k_laplace_c128 : k_laplace_c64;
+    if (prec == Precision::C64) {
+        *which = 3;
+        return kernel_for(k_laplace_c64_0, k_laplace_c64_1, nc);
+    }
+    *which = 2;
+    return kernel_for(k_laplace_c128_0, k_laplace_c128_1, nc);
 }
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Byte layout of a packed plan (problems | item_begin | chunks | arena) and of
+// its outputs (values in the output type, then the low words in FP64).
+struct PlanLayout {
+    int64_t n_probs = 0;
+    size_t o_probs = 0, o_items = 0, o_chunks = 0, o_arena = 0, total = 0;
+    size_t out_bytes = 0, lo_bytes = 0;
+};
+
+size_t delta_elem_bytes(const Planner &pl) { return pl.precision() == Precision::C64 ? 8 : 16; }
+
+PlanLayout layout_of(const Planner &pl, size_t out_elem) {
+    PlanLayout L;
+    L.n_probs = static_cast<int64_t>(pl.probs.size());
+    L.o_probs = 0;
+    L.o_items = align256(L.o_probs + sizeof(PqgProblem) * L.n_probs);
+    L.o_chunks = align256(L.o_items + sizeof(int64_t) * (L.n_probs + 1));
+    L.o_arena = align256(L.o_chunks + sizeof(PqgChunk) * std::max<size_t>(1, pl.chunks.size()));
+    L.total = align256(L.o_arena + pl.arena.size());
+    L.out_bytes = static_cast<size_t>(pl.total_outputs) * 2 * out_elem;
+    L.lo_bytes = static_cast<size_t>(pl.total_outputs) * 2 * sizeof(double);
+    return L;
+}
+
+void pack_plan(const Planner &pl, const PlanLayout &L, unsigned char *h) {
+    std::memcpy(h + L.o_probs, pl.probs.data(), sizeof(PqgProblem) * L.n_probs);
+    std::memcpy(h + L.o_items, pl.item_begin.data(), sizeof(int64_t) * (L.n_probs + 1));
+    if (!pl.chunks.empty()) std::memcpy(h + L.o_chunks, pl.chunks.data(), sizeof(PqgChunk) * pl.chunks.size());
+    if (!pl.arena.empty()) std::memcpy(h + L.o_arena, pl.arena.data(), pl.arena.size());
+}
+
+int ensure_buffers(DeviceBuffers &B, const Planner &pl, const PlanLayout &L) {
+    PQG_CUDA(B.plan.ensure(L.total));
+    const size_t n_parts = static_cast<size_t>(std::max<int64_t>(1, pl.total_parts));
+    PQG_CUDA(B.partials.ensure(n_parts * 4 * sizeof(double)));
+    PQG_CUDA(B.chunk_out.ensure(std::max<size_t>(1, pl.chunks.size()) * PQG_MAX_OUT * 4 * sizeof(double)));
+    PQG_CUDA(B.out.ensure(align256(L.out_bytes) + L.lo_bytes));
+    PQG_CUDA(B.counter.ensure(256));
+    PQG_CUDA(B.delta.ensure(std::max<size_t>(1, static_cast<size_t>(pl.total_delta)) * delta_elem_bytes(pl)));
+    return PQG_OK;
+}
+
+// Builds the prefix tables of an uploaded plan (one launch; none if empty).
+int enqueue_delta(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayout &L, cudaStream_t s) {
+    if (pl.total_delta <= 0) return PQG_OK;
+    unsigned char *d = static_cast<unsigned char *>(B.plan.p);
+    const PqgProblem *probs = reinterpret_cast<const PqgProblem *>(d + L.o_probs);
+    const int64_t threads = 256;
+    const int64_t blocks = std::min<int64_t>((pl.total_delta + threads - 1) / threads, int64_t(C.num_sms) * 16);
+    const int np = static_cast<int>(L.n_probs);
+    switch (pl.precision()) {
+        case Precision::C128:
+            build_delta<DELTA_F64><<<blocks, threads, 0, s>>>(probs, np, d + L.o_arena, B.delta.p, pl.total_delta);
+            break;
+        case Precision::C64:
+            build_delta<DELTA_F32><<<blocks, threads, 0, s>>>(probs, np, d + L.o_arena, B.delta.p, pl.total_delta);
+            break;
+        default:
+            build_delta<DELTA_DF><<<blocks, threads, 0, s>>>(probs, np, d + L.o_arena, B.delta.p, pl.total_delta);
+    }
+    PQG_CUDA(cudaGetLastError());
+    g_launches++;
+    return PQG_OK;
+}
+
+// Walk kernel of a plan, its dynamic shared memory set up, and its grid size.
+int walk_launch_config(Context &C, const Planner &pl, const KernelInfo **k, int64_t *blocks) {
+    int which = 0;
+    const KernelInfo &kk = kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, &which);
+    int &occ = C.occ_cache[which][pl.max_nc];
+    if (occ < 0) {
+        if (kk.smem_bytes > 48 * 1024)
+            PQG_CUDA(cudaFuncSetAttribute(kk.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(kk.smem_bytes)));
+        int b = 0;
+        PQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kk.fn, PQG_WALK_THREADS, kk.smem_bytes));
+        occ = std::max(1, b);
+    }
+    const int64_t warps_per_block = PQG_WALK_THREADS / 32;
+    int64_t nb = static_cast<int64_t>(C.num_sms) * std::min(occ, C.blocks_per_sm > 0 ? C.blocks_per_sm : occ);
+    nb = std::min<int64_t>(nb, (pl.total_items + warps_per_block - 1) / warps_per_block);
+    *k = &kk;
+    *blocks = std::max<int64_t>(1, nb);
+    return PQG_OK;
+}
+
+// Enqueues the device pipeline of an uploaded plan on stream s: zero the
+// queue head, walk, level-1 and level-2 reductions.  ev_w0 / ev_w1 (nullable)
+// bracket the walk kernel.  Captured as is into a CUDA graph by plan handles.
+template <typename T>
+int enqueue_pipeline(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayout &L, cudaStream_t s,
+                     cudaEvent_t ev_w0, cudaEvent_t ev_w1, const KernelInfo *k, int64_t blocks) {
+    unsigned char *d = static_cast<unsigned char *>(B.plan.p);
+    WalkArgs A;
+    A.probs = reinterpret_cast<const PqgProblem *>(d + L.o_probs);
+    A.item_begin = reinterpret_cast<const int64_t *>(d + L.o_items);
+    A.arena = d + L.o_arena;
+    A.delta = B.delta.p;
+    A.counter = static_cast<unsigned long long *>(B.counter.p);
+    A.partials = static_cast<double *>(B.partials.p);
+    A.total_items = pl.total_items;
+    A.n_probs = static_cast<int32_t>(L.n_probs);
+    A.pad = 0;
+    if (pl.total_items > 0) {
+        PQG_CUDA(cudaMemsetAsync(B.counter.p, 0, sizeof(unsigned long long), s));
+        void *args[] = {&A};
+        if (ev_w0) PQG_CUDA(cudaEventRecord(ev_w0, s));
+        PQG_CUDA(cudaLaunchKernel(k->fn, dim3(static_cast<unsigned>(blocks)), dim3(PQG_WALK_THREADS), args,
+                                  k->smem_bytes, s));
+        if (ev_w1) PQG_CUDA(cudaEventRecord(ev_w1, s));
+        if (!pl.chunks.empty()) {
+            reduce_chunks<<<static_cast<unsigned>(pl.chunks.size()), 256, 0, s>>>(
+                reinterpret_cast<const PqgChunk *>(d + L.o_chunks), A.probs, A.partials,
+                static_cast<double *>(B.chunk_out.p));
+            PQG_CUDA(cudaGetLastError());
+        }
+    }
+    unsigned char *dout = static_cast<unsigned char *>(B.out.p);
+    double *dlo = reinterpret_cast<double *>(dout + align256(L.out_bytes));
+    finish_problems<T><<<static_cast<unsigned>((L.n_probs + 3) / 4), 128, 0, s>>>(
+        A.probs, static_cast<int>(L.n_probs), static_cast<const double *>(B.chunk_out.p), reinterpret_cast<T *>(dout),
+        dlo);
+    PQG_CUDA(cudaGetLastError());
+    return PQG_OK;
+}
+
+// kernels one pipeline launches
+int64_t pipeline_launches(const Planner &pl) {
+    return 1 + (pl.total_items > 0 ? 1 : 0) + (pl.total_items > 0 && !pl.chunks.empty() ? 1 : 0);
+}
 
 // Runs a finished plan; writes n_outputs complex values (2*T each) to host `out`
 // and, if out_lo != nullptr, the low words (2 doubles per output).
 template <typename T>
 int run_plan(Context &C, Planner &pl, T *out, double *out_lo) {
-    const int64_t n_probs = static_cast<int64_t>(pl.probs.size());
-    if (n_probs == 0) return PQG_OK;
-    // pack the plan: problems | item_begin | chunks | arena
-    const size_t o_probs = 0;
-    const size_t o_items = align256(o_probs + sizeof(PqgProblem) * n_probs);
-    const size_t o_chunks = align256(o_items + sizeof(int64_t) * (n_probs + 1));
-    const size_t o_arena = align256(o_chunks + sizeof(PqgChunk) * std::max<size_t>(1, pl.chunks.size()));
-    const size_t total = align256(o_arena + pl.arena.size());
-    PQG_CUDA(C.h_plan.ensure(total));
-    PQG_CUDA(C.plan.ensure(total));
-    unsigned char *h = static_cast<unsigned char *>(C.h_plan.p);
-    std::memcpy(h + o_probs, pl.probs.data(), sizeof(PqgProblem) * n_probs);
-    std::memcpy(h + o_items, pl.item_begin.data(), sizeof(int64_t) * (n_probs + 1));
-    if (!pl.chunks.empty()) std::memcpy(h + o_chunks, pl.chunks.data(), sizeof(PqgChunk) * pl.chunks.size());
-    if (!pl.arena.empty()) std::memcpy(h + o_arena, pl.arena.data(), pl.arena.size());
-    unsigned char *d = static_cast<unsigned char *>(C.plan.p);
-
-    const size_t n_parts = static_cast<size_t>(std::max<int64_t>(1, pl.total_parts));
-    PQG_CUDA(C.partials.ensure(n_parts * 4 * sizeof(double)));
-    PQG_CUDA(C.chunk_out.ensure(std::max<size_t>(1, pl.chunks.size()) * PQG_MAX_OUT * 4 * sizeof(double)));
-    const size_t out_bytes = static_cast<size_t>(pl.total_outputs) * 2 * sizeof(T);
-    const size_t lo_bytes = static_cast<size_t>(pl.total_outputs) * 2 * sizeof(double);
-    PQG_CUDA(C.out.ensure(align256(out_bytes) + lo_bytes));
-    PQG_CUDA(C.h_out.ensure(align256(out_bytes) + lo_bytes));
-    PQG_CUDA(C.counter.ensure(256));
-
+    if (pl.probs.empty()) return PQG_OK;
+    const PlanLayout L = layout_of(pl, sizeof(T));
+    PQG_CUDA(C.h_plan.ensure(L.total));
+    pack_plan(pl, L, static_cast<unsigned char *>(C.h_plan.p));
+    int st = ensure_buffers(C.bufs, pl, L);
+    if (st) return st;
+    PQG_CUDA(C.h_out.ensure(align256(L.out_bytes) + L.lo_bytes));
+    const KernelInfo *k = nullptr;
+    int64_t blocks = 1;
+    if (pl.total_items > 0) {
+        st = walk_launch_config(C, pl, &k, &blocks);
+        if (st) return st;
+    }
     cudaStream_t s = C.stream;
-    PQG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, s));
-
-    WalkArgs A;
-    A.probs = reinterpret_cast<const PqgProblem *>(d + o_probs);
-    A.item_begin = reinterpret_cast<const int64_t *>(d + o_items);
-    A.arena = d + o_arena;
-    A.counter = static_cast<unsigned long long *>(C.counter.p);
-    A.partials = static_cast<double *>(C.partials.p);
-    A.total_items = pl.total_items;
-    A.n_probs = static_cast<int32_t>(n_probs);
-    A.pad = 0;
-
+    PQG_CUDA(cudaMemcpyAsync(C.bufs.plan.p, C.h_plan.p, L.total, cudaMemcpyHostToDevice, s));
     g_walk_ms = 0.0;
     g_dev_ms = 0.0;
     g_walk_steps = pl.total_steps;
     g_walk_flops = pl.total_flops;
-    g_h2d = static_cast<double>(total);
-    g_d2h = static_cast<double>(align256(out_bytes) + lo_bytes);
+    g_h2d = static_cast<double>(L.total);
+    g_d2h = static_cast<double>(align256(L.out_bytes) + L.lo_bytes);
+    st = enqueue_delta(C, C.bufs, pl, L, s);
+    if (st) return st;
     PQG_CUDA(cudaEventRecord(C.evs, s));
-    if (pl.total_items > 0) {
-        int which = 0;
-        const KernelInfo *tab = table_for(pl.form(), pl.precision(), &which);
-        const KernelInfo &k = tab[pl.max_nc];
-        int &occ = C.occ_cache[which][pl.max_nc];
-        if (occ < 0) {
-            if (k.smem_bytes > 48 * 1024)
-                PQG_CUDA(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(k.smem_bytes)));
-            int b = 0;
-            PQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k.fn, PQG_WALK_THREADS, k.smem_bytes));
-            occ = std::max(1, b);
-        }
-        const int64_t warps_per_block = PQG_WALK_THREADS / 32;
-        int64_t blocks = static_cast<int64_t>(C.num_sms) * occ;
-        blocks = std::min<int64_t>(blocks, (pl.total_items + warps_per_block - 1) / warps_per_block);
-        PQG_CUDA(cudaMemsetAsync(C.counter.p, 0, sizeof(unsigned long long), s));
-        void *args[] = {&A};
-        PQG_CUDA(cudaEventRecord(C.ev0, s));
-        PQG_CUDA(cudaLaunchKernel(k.fn, dim3(static_cast<unsigned>(blocks)), dim3(PQG_WALK_THREADS), args,
-                                  k.smem_bytes, s));
-        PQG_CUDA(cudaEventRecord(C.ev1, s));
-        g_launches++;
-        if (!pl.chunks.empty()) {
-            reduce_chunks<<<static_cast<unsigned>(pl.chunks.size()), 256, 0, s>>>(
-                reinterpret_cast<const PqgChunk *>(d + o_chunks), A.probs, A.partials,
-                static_cast<double *>(C.chunk_out.p));
-            PQG_CUDA(cudaGetLastError());
-            g_launches++;
-        }
-    }
-    unsigned char *dout = static_cast<unsigned char *>(C.out.p);
-    double *dlo = reinterpret_cast<double *>(dout + align256(out_bytes));
-    finish_problems<T><<<static_cast<unsigned>((n_probs + 3) / 4), 128, 0, s>>>(
-        A.probs, static_cast<int>(n_probs), static_cast<const double *>(C.chunk_out.p), reinterpret_cast<T *>(dout),
-        dlo);
-    PQG_CUDA(cudaGetLastError());
-    g_launches++;
+    st = enqueue_pipeline<T>(C, C.bufs, pl, L, s, C.ev0, C.ev1, k, blocks);
+    if (st) return st;
+    g_launches += pipeline_launches(pl);
     PQG_CUDA(cudaEventRecord(C.ev2, s));
     unsigned char *hout = static_cast<unsigned char *>(C.h_out.p);
-    PQG_CUDA(cudaMemcpyAsync(hout, dout, align256(out_bytes) + lo_bytes, cudaMemcpyDeviceToHost, s));
+    PQG_CUDA(cudaMemcpyAsync(hout, C.bufs.out.p, align256(L.out_bytes) + L.lo_bytes, cudaMemcpyDeviceToHost, s));
     PQG_CUDA(cudaStreamSynchronize(s));
     if (pl.total_items > 0) {
         float ms = 0.0f;
@@ -220,8 +315,8 @@ int run_plan(Context &C, Planner &pl, T *out, double *out_lo) {
         PQG_CUDA(cudaEventElapsedTime(&ms, C.evs, C.ev2));
         g_dev_ms = ms;
     }
-    std::memcpy(out, hout, out_bytes);
-    if (out_lo) std::memcpy(out_lo, hout + align256(out_bytes), lo_bytes);
+    std::memcpy(out, hout, L.out_bytes);
+    if (out_lo) std::memcpy(out_lo, hout + align256(L.out_bytes), L.lo_bytes);
     return PQG_OK;
 }
 
@@ -229,6 +324,16 @@ std::vector<double> widen(const float *m, int64_t n) {
     std::vector<double> v(static_cast<size_t>(n));
     for (int64_t i = 0; i < n; ++i) v[i] = static_cast<double>(m[i]);
     return v;
+}
+
+// Precision of a complex128 call: the explicit mode, else PQG_C128_MODE from the
+// environment ("fp64", "df" or "auto"), else auto (double-float where valid).
+Precision c128_precision(int32_t mode) {
+    if (mode == PQG_MODE_FP64) return Precision::C128;
+    if (mode == PQG_MODE_DF) return Precision::C128DF;
+    const char *env = std::getenv("PQG_C128_MODE");
+    if (env && std::strcmp(env, "fp64") == 0) return Precision::C128;
+    return Precision::C128DF;
 }
 
 template <typename T>
@@ -248,6 +353,11 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     if (st) return st;
     pl.set_config(C.cfg);
     pl.finish();
+    if (prec == Precision::C128DF && !pl.df_ok) {
+        // outside the double-float domain: the FP64 walk
+        pl.set_precision(Precision::C128);
+        pl.finish();
+    }
     return run_plan<T>(C, pl, out, out_lo);
 }
 
@@ -325,8 +435,8 @@ int time_fma(Context &C, double target_ms, double *tflops) {
     int occ = 0;
     PQG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fma_chains<F, CHAINS>, threads, 0));
     const int blocks = C.num_sms * std::max(1, occ);
-    PQG_CUDA(C.out.ensure(1024));
-    F *o = static_cast<F *>(C.out.p);
+    PQG_CUDA(C.bufs.out.ensure(1024));
+    F *o = static_cast<F *>(C.bufs.out.p);
     int iters = 256;
     for (int rep = 0; rep < 8; ++rep) {
         fma_chains<F, CHAINS><<<blocks, threads, 0, C.stream>>>(o, iters, static_cast<F>(0.999999), static_cast<F>(1e-7));
@@ -342,6 +452,66 @@ int time_fma(Context &C, double target_ms, double *tflops) {
         if (ms >= 0.5 * target_ms || iters > (1 << 28)) break;
         iters = static_cast<int>(std::min<double>(iters * std::max(2.0, target_ms / std::max(ms, 1e-3f)), 1 << 29));
     }
+    return PQG_OK;
+}
+
+// ------------------------------------------------------------ plan handles
+// A plan handle owns a planned, uploaded batch, its device buffers, a stream
+// and a CUDA graph of its device pipeline, so that repeated executions cost
+// one graph launch (no planning, no copies).
+struct PlanHandle {
+    Planner pl{Precision::C128, Form::PLAIN, PlanConfig{}};
+    PlanLayout L;
+    DeviceBuffers B;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool single = false;      // complex64 outputs
+    bool launched = false;
+    int64_t n_cols = 0;       // Laplace: outputs per problem in the caller's layout
+    ~PlanHandle() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (stream) cudaStreamDestroy(stream);
+        for (DevBuf *b : {&B.plan, &B.partials, &B.chunk_out, &B.out, &B.counter, &B.delta})
+            if (b->p) cudaFree(b->p);
+    }
+};
+
+template <typename T>
+int plan_build(Context &C, PlanHandle *h) {
+    h->L = layout_of(h->pl, sizeof(T));
+    int st = ensure_buffers(h->B, h->pl, h->L);
+    if (st) return st;
+    PQG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    PQG_CUDA(cudaEventCreate(&h->e0));
+    PQG_CUDA(cudaEventCreate(&h->e1));
+    std::vector<unsigned char> hp(h->L.total);
+    pack_plan(h->pl, h->L, hp.data());
+    PQG_CUDA(cudaMemcpyAsync(h->B.plan.p, hp.data(), h->L.total, cudaMemcpyHostToDevice, h->stream));
+    st = enqueue_delta(C, h->B, h->pl, h->L, h->stream);
+    if (st) return st;
+    PQG_CUDA(cudaStreamSynchronize(h->stream));
+    const KernelInfo *k = nullptr;
+    int64_t blocks = 1;
+    if (h->pl.total_items > 0) {
+        st = walk_launch_config(C, h->pl, &k, &blocks);
+        if (st) return st;
+    }
+    PQG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    st = enqueue_pipeline<T>(C, h->B, h->pl, h->L, h->stream, nullptr, nullptr, k, blocks);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (st) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(PQG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    h->graph = g;
+    PQG_CUDA(cudaGraphInstantiate(&h->exec, h->graph, 0));
     return PQG_OK;
 }
 
@@ -361,8 +531,7 @@ uint64_t pqg_kernel_launches(void) { return g_launches.load(); }
 
 int pqg_permanent_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
                        int32_t mode, double *out, double *out_lo) {
-    (void)mode;
-    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, 1, Precision::C128, out, out_lo);
+    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, 1, c128_precision(mode), out, out_lo);
 }
 
 int pqg_permanent_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
@@ -374,8 +543,7 @@ int pqg_permanent_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const
 
 int pqg_permanent_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                              const int32_t *cols, int64_t batch, int32_t mode, double *out) {
-    (void)mode;
-    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, Precision::C128, out, nullptr);
+    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(mode), out, nullptr);
 }
 
 int pqg_permanent_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
@@ -409,6 +577,27 @@ int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t
     return laplace_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out, n_out);
 }
 
+int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    if (items_per_smsp < 0 || p_max < 0 || p_max > 32768 || seed_steps < 0)
+        return fail(PQG_ERR_INVALID, "invalid tuning values");
+    PlanConfig d;
+    C.cfg.items_per_smsp = items_per_smsp ? items_per_smsp : d.items_per_smsp;
+    C.cfg.p_max = p_max ? p_max : d.p_max;
+    C.cfg.seed_steps = seed_steps;
+    return PQG_OK;
+}
+
+int pqg_get_tuning(int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps) {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    if (items_per_smsp) *items_per_smsp = C.cfg.items_per_smsp;
+    if (p_max) *p_max = C.cfg.p_max;
+    if (seed_steps) *seed_steps = C.cfg.seed_steps;
+    return PQG_OK;
+}
+
 int pqg_measure_vector_peaks(double ms, double *out2) {
     if (!out2) return fail(PQG_ERR_INVALID, "null output");
     Context &C = ctx();
@@ -428,6 +617,128 @@ int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *f
     if (device_ms) *device_ms = g_dev_ms;
     if (steps) *steps = g_walk_steps;
     if (flops) *flops = g_walk_flops;
+    return PQG_OK;
+}
+
+int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
+                    int64_t batch, int32_t dtype, int32_t form, int32_t mode, pqg_plan_t **out_plan) {
+    if (!out_plan || batch < 0 || n_rows < 0 || n_cols < 0 || (dtype != 0 && dtype != 1) || (form != 0 && form != 1))
+        return fail(PQG_ERR_INVALID, "invalid arguments");
+    *out_plan = nullptr;
+    std::vector<double> widened;
+    const double *m = static_cast<const double *>(matrix);
+    if (dtype == 1) {
+        widened = widen(static_cast<const float *>(matrix), 2 * n_rows * n_cols);
+        m = widened.data();
+    }
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    const Precision prec = dtype == 1 ? Precision::C64 : c128_precision(mode);
+    const Form fm = form == 1 ? Form::LAPLACE : Form::PLAIN;
+    PlanHandle *h = new PlanHandle();
+    h->pl = Planner(prec, fm, C.cfg);
+    h->single = dtype == 1;
+    h->n_cols = n_cols;
+    for (int64_t b = 0; b < batch; ++b) {
+        std::string err;
+        int st = h->pl.add(m, n_rows, n_cols, rows ? rows + b * n_rows : nullptr, cols ? cols + b * n_cols : nullptr, err);
+        if (st) {
+            delete h;
+            return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
+        }
+    }
+    int st = C.init();
+    if (st) {
+        delete h;
+        return st;
+    }
+    h->pl.set_config(C.cfg);
+    h->pl.finish();
+    if (prec == Precision::C128DF && !h->pl.df_ok) {
+        h->pl.set_precision(Precision::C128);
+        h->pl.finish();
+    }
+    st = h->single ? plan_build<float>(C, h) : plan_build<double>(C, h);
+    if (st) {
+        delete h;
+        return st;
+    }
+    *out_plan = reinterpret_cast<pqg_plan_t *>(h);
+    return PQG_OK;
+}
+
+int pqg_plan_launch(pqg_plan_t *plan) {
+    PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
+    if (!h) return fail(PQG_ERR_INVALID, "null plan");
+    PQG_CUDA(cudaEventRecord(h->e0, h->stream));
+    PQG_CUDA(cudaGraphLaunch(h->exec, h->stream));
+    PQG_CUDA(cudaEventRecord(h->e1, h->stream));
+    g_launches += pipeline_launches(h->pl);
+    h->launched = true;
+    return PQG_OK;
+}
+
+int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms) {
+    PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
+    if (!h) return fail(PQG_ERR_INVALID, "null plan");
+    PQG_CUDA(cudaStreamSynchronize(h->stream));
+    if (device_ms) {
+        float ms = 0.0f;
+        if (h->launched) PQG_CUDA(cudaEventElapsedTime(&ms, h->e0, h->e1));
+        *device_ms = ms;
+    }
+    return PQG_OK;
+}
+
+int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) {
+    PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
+    if (!h || !out) return fail(PQG_ERR_INVALID, "null argument");
+    std::vector<unsigned char> tmp(h->L.out_bytes);
+    if (h->L.out_bytes) {
+        PQG_CUDA(cudaMemcpyAsync(tmp.data(), h->B.out.p, h->L.out_bytes, cudaMemcpyDeviceToHost, h->stream));
+        PQG_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    const size_t es = h->single ? sizeof(float) : sizeof(double);
+    if (h->pl.form() == Form::PLAIN) {
+        std::memcpy(out, tmp.data(), h->L.out_bytes);
+        if (n_values) *n_values = static_cast<int64_t>(h->pl.probs.size());
+        return PQG_OK;
+    }
+    // Laplace: scatter every problem's outputs to the caller's column layout
+    const int64_t stride = std::max<int64_t>(1, h->n_cols);
+    unsigned char *o = static_cast<unsigned char *>(out);
+    for (size_t b = 0; b < h->pl.pending.size(); ++b) {
+        const PendingProblem &pp = h->pl.pending[b];
+        const int64_t oi = h->pl.probs[b].out_index;
+        unsigned char *ob = o + b * stride * 2 * es;
+        std::memset(ob, 0, stride * 2 * es);
+        if (pp.kind == PQG_KIND_CONSTANT) {
+            std::memcpy(ob, tmp.data() + oi * 2 * es, 2 * es);
+            continue;
+        }
+        for (int64_t j = 0; j < h->n_cols; ++j)
+            std::memcpy(ob + j * 2 * es, tmp.data() + (oi + pp.out_map[j]) * 2 * es, 2 * es);
+    }
+    if (n_values) *n_values = static_cast<int64_t>(h->pl.pending.size()) * stride;
+    return PQG_OK;
+}
+
+int pqg_plan_info(pqg_plan_t *plan, double *steps, double *flops, int64_t *work_items, int64_t *h2d_bytes) {
+    PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
+    if (!h) return fail(PQG_ERR_INVALID, "null plan");
+    if (steps) *steps = h->pl.total_steps;
+    if (flops) *flops = h->pl.total_flops;
+    if (work_items) *work_items = h->pl.total_items;
+    if (h2d_bytes) *h2d_bytes = static_cast<int64_t>(h->L.total);
+    return PQG_OK;
+}
+
+int pqg_plan_destroy(pqg_plan_t *plan) {
+    PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
+    if (h) {
+        cudaStreamSynchronize(h->stream);
+        delete h;
+    }
     return PQG_OK;
 }
 

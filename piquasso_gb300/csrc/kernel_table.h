@@ -1,4 +1,6 @@
-// Kernel tables: one walk-kernel instantiation per exact column count.
+// Kernel tables: one walk-kernel instantiation per exact column count,
+// compiled in two halves per arithmetic (k_<form>_<prec>_0.cu: 1..16,
+// k_<form>_<prec>_1.cu: 17..32) so that the build runs in parallel.
 #pragma once
 #include <stddef.h>
 
@@ -11,9 +13,20 @@ struct KernelInfo {
     size_t smem_bytes;  // dynamic shared memory per block
 };
 
-extern const KernelInfo k_plain_c128[PQG_MAX_COLS + 1];
-extern const KernelInfo k_plain_c64[PQG_MAX_COLS + 1];
-extern const KernelInfo k_laplace_c128[PQG_MAX_COLS + 1];
-extern const KernelInfo k_laplace_c64[PQG_MAX_COLS + 1];
+extern const KernelInfo k_plain_c128_0[16];
+extern const KernelInfo k_plain_c128_1[16];
+extern const KernelInfo k_plain_c64_0[16];
+extern const KernelInfo k_plain_c64_1[16];
+extern const KernelInfo k_plain_df_0[16];
+extern const KernelInfo k_plain_df_1[16];
+extern const KernelInfo k_laplace_c128_0[16];
+extern const KernelInfo k_laplace_c128_1[16];
+extern const KernelInfo k_laplace_c64_0[16];
+extern const KernelInfo k_laplace_c64_1[16];
+
+// the instantiation for exactly nc columns (1 <= nc <= 32)
+inline const KernelInfo &kernel_for(const KernelInfo *lo_half, const KernelInfo *hi_half, int nc) {
+    return nc <= 16 ? lo_half[nc - 1] : hi_half[nc - 17];
+}
 
 }  // namespace pqg

@@ -103,6 +103,9 @@ int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, c
         err = "too many particles";
         return 3;
     }
+    // the double-float kernel keeps typical terms (>= N^(-N/2) after column
+    // scaling) far above the FP32 underflow threshold only for N <= 32
+    if (sr > 32) df_ok_add_ = false;
 
     // columns with nonzero multiplicity
     std::vector<int> keep;
@@ -163,6 +166,16 @@ int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, c
         err = "Gray-code space above 2^50 steps";
         return 3;
     }
+    // the binomial weights prod C(m_i, g_i) must stay exact integers in FP64
+    // and in the kernels' int64 products
+    {
+        double wmax = 1.0;
+        for (int m : p.m) wmax *= static_cast<double>(binom64(m, m / 2));
+        if (wmax > 9.0e15) {
+            err = "binomial weights of the row multiplicities exceed 2^53";
+            return 3;
+        }
+    }
     p.S = S;
     p.scale_exp = static_cast<int>(sr - 1);
     pending.push_back(std::move(p));
@@ -183,6 +196,63 @@ int64_t Planner::push_bytes_(const void *p, size_t n) {
     return off;
 }
 
+namespace {
+
+// Steps per lane below which the per-lane seeding (about 2 x NC flops per
+// nonzero outer digit, at 48 bits or more) stops being small next to the walk.
+int64_t min_steps_per_seed(Precision prec) {
+    switch (prec) {
+        case Precision::C128: return 512;     // FP64 seed, FP64 steps
+        case Precision::C128DF: return 256;   // double-float seed and steps
+        default: return 1024;                 // double-float seed, FP32 steps
+    }
+}
+
+// Signed binomial weights (-1)^sum(g) prod C(m, g) of the reflected
+// mixed-radix Gray code over the inner digits (digit 0 fastest), from code 0.
+std::vector<double> build_weights(const std::vector<int> &mm, int64_t P) {
+    const size_t K = mm.size();
+    std::vector<int> lim(K), chain(K, 0), code(K, 0);
+    for (size_t k = 0; k < K; ++k) lim[k] = mm[k] + 1;
+    std::vector<double> w(P, 1.0);
+    int64_t bc = 1;
+    int parity = 0;
+    for (int64_t t = 1; t < P; ++t) {
+        size_t k = 0;
+        while (true) {
+            if (chain[k] < lim[k] - 1) {
+                chain[k]++;
+                break;
+            }
+            chain[k] = 0;
+            ++k;
+        }
+        int par = 0, ch = -1, prev = 0, val = 0;
+        for (int i = static_cast<int>(K) - 1; i >= 0; --i) {
+            const int c = par ? lim[i] - 1 - chain[i] : chain[i];
+            par ^= (c & 1);
+            if (c != code[i] && ch < 0) {
+                ch = i;
+                prev = code[i];
+                val = c;
+            }
+        }
+        code[ch] = val;
+        parity ^= 1;
+        bc = val > prev ? bc * (mm[ch] - prev) / val : bc * prev / (mm[ch] - val);
+        w[t] = (parity ? -1.0 : 1.0) * static_cast<double>(bc);
+    }
+    return w;
+}
+
+void push_df(std::vector<float> &v, double x) {
+    const float hi = static_cast<float>(x);
+    v.push_back(hi);
+    v.push_back(static_cast<float>(x - static_cast<double>(hi)));
+}
+
+}  // namespace
+
 void Planner::finish() {
     const size_t np = pending.size();
     probs.assign(np, PqgProblem{});
@@ -191,20 +261,14 @@ void Planner::finish() {
     arena.clear();
     table_cache_.clear();
     total_items = total_parts = total_outputs = 0;
+    total_delta = 0;
     total_steps = total_flops = 0.0;
     max_nc = 1;
-
-    double S_tot = 0.0;
-    for (auto &p : pending)
-        if (p.kind == PQG_KIND_WALK) S_tot += p.S;
-    // longest inner walk such that the whole plan still has about
-    // items_per_smsp warps of work per SM sub-partition
-    const double lanes_wanted = 32.0 * 4.0 * cfg_.num_sms * static_cast<double>(cfg_.items_per_smsp);
-    double p_cap = S_tot / lanes_wanted;
-    p_cap = std::min<double>(std::max<double>(p_cap, static_cast<double>(cfg_.p_min)), static_cast<double>(cfg_.p_max));
+    df_ok = df_ok_add_;
 
     const bool c128 = prec_ == Precision::C128;
-    const size_t cplx = c128 ? 16 : 8;
+    const bool df = prec_ == Precision::C128DF;
+    const bool laplace = form_ == Form::LAPLACE;
 
     // One walk kernel serves the whole plan and is compiled for an exact column
     // count, so every problem of a batch is padded to the largest column count
@@ -231,13 +295,26 @@ void Planner::finish() {
             p.rows.swap(rows);
             p.nc = ncmax;
             p.padded_cols = add;
-            if (form_ == Form::LAPLACE) {
+            if (laplace) {
                 for (int &slot : p.out_map)
                     if (slot == old) slot = ncmax;
                 p.n_out = ncmax + (p.laplace_full ? 1 : 0);
             }
         }
     }
+
+    // Steps per lane: about items_per_smsp warps of work per SM sub-partition
+    // for balance, but at least enough steps to amortise the seeding.
+    double S_tot = 0.0;
+    for (auto &p : pending)
+        if (p.kind == PQG_KIND_WALK) S_tot += p.S;
+    const double resident_warps = 4.0 * cfg_.num_sms * 3.0;
+    const double balance = S_tot / (32.0 * 4.0 * cfg_.num_sms * static_cast<double>(cfg_.items_per_smsp));
+    const double seed_floor = std::min<double>(static_cast<double>(cfg_.seed_steps > 0 ? cfg_.seed_steps
+                                                                                    : min_steps_per_seed(prec_)),
+                                               S_tot / (32.0 * resident_warps));
+    const double steps_per_lane = std::max({balance, seed_floor, 1.0});
+    const int64_t p_max = laplace ? std::min<int64_t>(cfg_.p_max, 512) : cfg_.p_max;
 
     for (size_t ip = 0; ip < np; ++ip) {
         PendingProblem &p = pending[ip];
@@ -250,10 +327,12 @@ void Planner::finish() {
         q.item_begin = total_items;
         q.part_begin = total_parts;
         q.chunk_begin = static_cast<int64_t>(chunks.size());
+        q.delta_begin = total_delta;  // kept monotone for the device's binary search
         if (p.kind == PQG_KIND_CONSTANT) {
             q.cval_re = p.cre;
             q.cval_im = p.cim;
             q.P = 1;
+            q.R = 1;
             item_begin[ip + 1] = total_items;
             continue;
         }
@@ -267,131 +346,137 @@ void Planner::finish() {
         }
         q.cm_max = cm_max;
 
-        // inner digits: ascending multiplicity, greedily while the walk fits
-        // both the global cap and a full warp of outer assignments
+        // this problem's steps per lane: the plan's, but never so many that
+        // the problem fills less than one warp
+        const double lane_steps = std::max(1.0, std::min(steps_per_lane, p.S / 32.0));
+        // inner digits: ascending multiplicity, greedily while the inner walk
+        // fits both the lane's steps and the table limit
         const int nd = static_cast<int>(p.m.size());
         std::vector<int> order(nd);
         for (int i = 0; i < nd; ++i) order[i] = i;
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return p.m[x] < p.m[y]; });
-        double target = std::min(p_cap, std::max(1.0, p.S / 32.0));
+        const double p_target = std::min<double>(static_cast<double>(p_max), lane_steps);
         std::vector<int> inner, outer;
         double P = 1.0;
         for (int i : order) {
-            if (P * (p.m[i] + 1) <= target && outer.empty())
-            {
+            if (outer.empty() && inner.size() < PQG_MAX_INNER && P * (p.m[i] + 1) <= p_target) {
                 inner.push_back(i);
                 P *= (p.m[i] + 1);
             } else {
                 outer.push_back(i);
             }
         }
-        if (static_cast<int>(outer.size()) > PQG_MAX_OUTER) {
-            // cannot happen below 2^50 steps with radix >= 2 and <= 60 digits
-            outer.resize(PQG_MAX_OUTER);
-        }
-        q.P = static_cast<int32_t>(P);
-        q.n_outer = static_cast<int32_t>(outer.size());
-        double Q = p.S / P;
-        q.Q = static_cast<int64_t>(std::llround(Q));
-        for (size_t o = 0; o < outer.size(); ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
-
-        // FP64 seed: column sums with every digit at 0, a0 + sum_i m_i a_i
-        std::vector<double> base(2 * p.nc);
-        for (int k = 0; k < 2 * p.nc; ++k) {
-            Kahan2 s;
-            s.add(p.a0[k]);
-            for (int i = 0; i < nd; ++i) s.add(static_cast<double>(p.m[i]) * p.rows[static_cast<size_t>(i) * 2 * p.nc + k]);
-            base[k] = s.value();
-        }
-        q.off_base = push_bytes_(base.data(), base.size() * sizeof(double));
-        std::vector<double> orow;
-        orow.reserve(outer.size() * 2 * p.nc);
-        for (int i : outer)
-            for (int k = 0; k < 2 * p.nc; ++k) orow.push_back(p.rows[static_cast<size_t>(i) * 2 * p.nc + k]);
-        q.off_outer = orow.empty() ? q.off_base : push_bytes_(orow.data(), orow.size() * sizeof(double));
-
-        // D rows of the inner digits, in kernel precision
         const size_t K = inner.size();
+        q.P = static_cast<int32_t>(P);
+        q.K = static_cast<int32_t>(K);
+        q.n_outer = static_cast<int32_t>(outer.size());
+        q.Q = static_cast<int64_t>(std::llround(p.S / P));
+        // laplace kernels walk one outer position per lane
+        q.R = laplace ? 1 : std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
+        q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / 32));
+        for (size_t o = 0; o < outer.size(); ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
+        for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
+
+        // Double-float plans scale column j by 2^-e_j so that no column sum
+        // can exceed 1 in magnitude: |c_j| <= |a0_j| + sum_i m_i |a_ij| <= 1.
+        // Powers of two are exact; the result is multiplied back through the
+        // final 2^-scale_exp factor.
+        std::vector<double> cscale(p.nc, 1.0);
+        if (df) {
+            int shift = 0;
+            for (int k = 0; k < p.nc; ++k) {
+                double B = std::hypot(p.a0[2 * k], p.a0[2 * k + 1]);
+                for (int i = 0; i < nd; ++i) {
+                    const double *r = &p.rows[static_cast<size_t>(i) * 2 * p.nc + 2 * k];
+                    B += p.m[i] * std::hypot(r[0], r[1]);
+                }
+                int e = 0;
+                if (B > 0.0) std::frexp(B, &e);  // B in [2^(e-1), 2^e)
+                cscale[k] = std::ldexp(1.0, -e);
+                shift += e * p.cm[k];
+            }
+            q.scale_exp = p.scale_exp - shift;
+        }
+        auto row = [&](int i, int c) { return p.rows[static_cast<size_t>(i) * 2 * p.nc + c] * cscale[c / 2]; };
+
+        // seeds: column sums with every digit at 0, a0 + sum_i m_i a_i (compensated)
+        std::vector<double> base(2 * p.nc);
+        for (int c = 0; c < 2 * p.nc; ++c) {
+            Kahan2 s;
+            s.add(p.a0[c] * cscale[c / 2]);
+            for (int i = 0; i < nd; ++i) s.add(static_cast<double>(p.m[i]) * row(i, c));
+            base[c] = s.value();
+        }
+        std::vector<double> orow, irow;
+        for (int i : outer)
+            for (int c = 0; c < 2 * p.nc; ++c) orow.push_back(row(i, c));
+        for (int i : inner)
+            for (int c = 0; c < 2 * p.nc; ++c) irow.push_back(row(i, c));
+        q.off_inner64 = irow.empty() ? 0 : push_bytes_(irow.data(), irow.size() * sizeof(double));
+        q.off_base64 = push_bytes_(base.data(), base.size() * sizeof(double));
+        q.off_outer64 = orow.empty() ? q.off_base64 : push_bytes_(orow.data(), orow.size() * sizeof(double));
+        {
+            std::vector<float> bdf, odf;
+            for (double v : base) push_df(bdf, v);
+            for (double v : orow) push_df(odf, v);
+            q.off_base_df = push_bytes_(bdf.data(), bdf.size() * sizeof(float));
+            q.off_outer_df = odf.empty() ? q.off_base_df : push_bytes_(odf.data(), odf.size() * sizeof(float));
+        }
+
+        // D rows of the outer digits, in kernel precision
+        const std::vector<int> &digits = outer;
+        const size_t nrows = std::max<size_t>(1, 2 * digits.size());
         if (c128) {
-            std::vector<double> D(std::max<size_t>(1, 2 * K) * 2 * p.nc, 0.0);
-            for (size_t k = 0; k < K; ++k)
+            std::vector<double> D(nrows * 2 * p.nc, 0.0);
+            for (size_t k = 0; k < digits.size(); ++k)
                 for (int c = 0; c < 2 * p.nc; ++c) {
-                    double v = 2.0 * p.rows[static_cast<size_t>(inner[k]) * 2 * p.nc + c];
+                    const double v = 2.0 * row(digits[k], c);
                     D[(2 * k) * 2 * p.nc + c] = -v;
                     D[(2 * k + 1) * 2 * p.nc + c] = v;
                 }
             q.off_D = push_bytes_(D.data(), D.size() * sizeof(double));
+        } else if (df) {
+            std::vector<float> D;
+            D.reserve(nrows * 4 * p.nc);
+            for (size_t k = 0; k < digits.size(); ++k)
+                for (int sgn = 0; sgn < 2; ++sgn)
+                    for (int c = 0; c < 2 * p.nc; ++c) push_df(D, (sgn ? 2.0 : -2.0) * row(digits[k], c));
+            if (D.empty()) D.assign(4 * p.nc, 0.0f);
+            q.off_D = push_bytes_(D.data(), D.size() * sizeof(float));
         } else {
-            std::vector<float> D(std::max<size_t>(1, 2 * K) * 2 * p.nc, 0.0f);
-            for (size_t k = 0; k < K; ++k)
+            std::vector<float> D(nrows * 2 * p.nc, 0.0f);
+            for (size_t k = 0; k < digits.size(); ++k)
                 for (int c = 0; c < 2 * p.nc; ++c) {
-                    double v = 2.0 * p.rows[static_cast<size_t>(inner[k]) * 2 * p.nc + c];
+                    const double v = 2.0 * row(digits[k], c);
                     D[(2 * k) * 2 * p.nc + c] = static_cast<float>(-v);
                     D[(2 * k + 1) * 2 * p.nc + c] = static_cast<float>(v);
                 }
             q.off_D = push_bytes_(D.data(), D.size() * sizeof(float));
         }
+        q.delta_begin = total_delta;
+        total_delta += static_cast<int64_t>(q.P) * p.nc;
 
-        // inner step table: keyed by (precision, nc, inner multiplicities);
-        // the reflected mixed-radix Gray code from 0, digit 0 fastest
-        std::vector<int> key;
-        key.push_back(c128 ? 1 : 0);
-        key.push_back(p.nc);
-        for (int i : inner) key.push_back(p.m[i]);
-        auto it = table_cache_.find(key);
+        // the weight table depends only on the inner multiplicities
+        std::vector<int> mm;
+        for (int i : inner) mm.push_back(p.m[i]);
+        auto it = table_cache_.find(mm);
         if (it != table_cache_.end()) {
             q.off_tab = it->second;
         } else {
-            const int64_t PP = q.P;
-            std::vector<int> lim(K), chain(K, 0), code(K, 0), mm(K);
-            for (size_t k = 0; k < K; ++k) {
-                mm[k] = p.m[inner[k]];
-                lim[k] = mm[k] + 1;
+            const std::vector<double> w = build_weights(mm, q.P);
+            std::vector<PqgStep> tab(q.P);
+            for (int64_t t = 0; t < q.P; ++t) {
+                tab[t].wd = w[t];
+                tab[t].wf = static_cast<float>(w[t]);
+                tab[t].pad = 0.0f;
+                if (df && std::fabs(w[t]) > 16777216.0) df_ok = false;  // not exact in FP32
             }
-            std::vector<double> w(PP);
-            std::vector<int32_t> drow(PP, 0);
-            w[0] = 1.0;
-            int64_t bc = 1;
-            int parity = 0;
-            for (int64_t t = 1; t < PP; ++t) {
-                size_t k = 0;
-                while (true) {
-                    if (chain[k] < lim[k] - 1) {
-                        chain[k]++;
-                        break;
-                    }
-                    chain[k] = 0;
-                    ++k;
-                }
-                int par = 0, ch = -1, prev = 0, val = 0;
-                for (int i = static_cast<int>(K) - 1; i >= 0; --i) {
-                    int c = par ? lim[i] - 1 - chain[i] : chain[i];
-                    par ^= (c & 1);
-                    if (c != code[i] && ch < 0) {
-                        ch = i;
-                        prev = code[i];
-                        val = c;
-                    }
-                }
-                code[ch] = val;
-                parity ^= 1;
-                bc = val > prev ? bc * (mm[ch] - prev) / val : bc * prev / (mm[ch] - val);
-                w[t] = (parity ? -1.0 : 1.0) * static_cast<double>(bc);
-                drow[t] = static_cast<int32_t>((2 * ch + (val > prev ? 0 : 1)) * p.nc);
-            }
-            if (c128) {
-                std::vector<PqgStep128> tab(PP);
-                for (int64_t t = 0; t < PP; ++t) tab[t] = PqgStep128{w[t], drow[t], 0};
-                q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep128));
-            } else {
-                std::vector<PqgStep64> tab(PP);
-                for (int64_t t = 0; t < PP; ++t) tab[t] = PqgStep64{static_cast<float>(w[t]), drow[t]};
-                q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep64));
-            }
-            table_cache_[key] = q.off_tab;
+            q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep));
+            table_cache_[mm] = q.off_tab;
         }
 
-        q.n_items = (q.Q + PQG_ITEM_LANES - 1) / PQG_ITEM_LANES;
+        const int64_t lanes = (q.Q + q.R - 1) / q.R;
+        q.n_items = (lanes + PQG_ITEM_LANES - 1) / PQG_ITEM_LANES;
         total_items += q.n_items;
         total_parts += q.n_items * q.n_out;
         item_begin[ip + 1] = total_items;
@@ -407,7 +492,6 @@ void Planner::finish() {
         q.n_chunks = static_cast<int64_t>(chunks.size()) - q.chunk_begin;
         total_steps += p.S;
         total_flops += algorithmic_flops(p, form_);
-        (void)cplx;
     }
     item_begin[np] = total_items;
     align_(16);

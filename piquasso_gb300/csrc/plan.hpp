@@ -9,14 +9,16 @@
 
 namespace pqg {
 
-enum class Precision { C128, C64 };
+// C128: FP64 walk.  C64: FP32 walk.  C128DF: complex128 accuracy from
+// double-float (FP32 pair) updates and products, FP64 seeds and sums.
+enum class Precision { C128, C64, C128DF };
 enum class Form { PLAIN, LAPLACE };
 
 struct PlanConfig {
     int num_sms = 152;
     int64_t items_per_smsp = 16;  // work items per SM sub-partition the split aims for
-    int64_t p_min = 64;           // shortest inner walk when the space is large
     int64_t p_max = 2048;         // longest inner walk (table length)
+    int64_t seed_steps = 0;       // steps per lane that amortise a seed; 0: per-precision default
 };
 
 // One reduced problem before its inner/outer split is fixed.
@@ -59,11 +61,17 @@ class Planner {
     int64_t total_items = 0;
     int64_t total_parts = 0;           // dd-complex partial slots
     int64_t total_outputs = 0;
+    int64_t total_delta = 0;           // prefix-table elements (sum of P x nc)
     int max_nc = 0;
     double total_steps = 0.0;          // sum over problems of the Gray-code space
     double total_flops = 0.0;          // algorithmic flop count, see algorithmic_flops()
 
     Precision precision() const { return prec_; }
+    void set_precision(Precision p) { prec_ = p; }
+    // C128DF plans only: false when some problem falls outside the double-float
+    // kernel's validity domain (more than 32 particles, or an inner weight that
+    // is not exact in FP32); the caller then plans in C128 instead.
+    bool df_ok = true;
     Form form() const { return form_; }
 
   private:
@@ -71,6 +79,7 @@ class Planner {
     Form form_;
     PlanConfig cfg_;
     std::map<std::vector<int>, int64_t> table_cache_;
+    bool df_ok_add_ = true;
     int64_t align_(size_t a);
     int64_t push_bytes_(const void *p, size_t n);
 };

@@ -5,16 +5,23 @@
 // BB/FG-Glynn form, Eq. (8) of arXiv:2309.07027, as in the reference's
 // src/permanent.cpp:49-264).  The planner splits the Gray-code digits of every
 // problem into
-//   * inner digits: walked by every lane of a warp in lock step, from the same
-//     start, along one precomputed table of (changed row, signed weight) steps;
-//   * outer digits: one assignment per lane, decoded from the lane's segment
-//     index, seeded from scratch in FP64 at the segment start.
-// A work item is one warp: 32 consecutive outer assignments of one problem.
+//   * K inner digits, whose reflected Gray code (P codes) all lanes of a warp
+//     walk in lock step, forward from code 0 or backward from code P-1.  The
+//     column sums at inner code t are seed + Delta(t), with the prefix table
+//     Delta(t) = sum_k -2 g_k(t) a_k built once per problem on the device, so
+//     a step is one addition per column and rounding errors never accumulate;
+//   * outer digits: each lane owns R consecutive positions of the reflected
+//     mixed-radix Gray code over the outer digits.  It seeds its column sums
+//     from scratch at its first position, walks the inner codes, then moves to
+//     the next outer position with a one-digit update of the seed and walks
+//     the inner codes in the other direction, R times.
+// A work item is one warp: 32 lanes x R outer positions of one problem.
 #pragma once
 #include <stdint.h>
 
 #define PQG_MAX_COLS 32
 #define PQG_MAX_OUTER 60
+#define PQG_MAX_INNER 16
 #define PQG_ITEM_LANES 32
 
 enum PqgProblemKind : int32_t {
@@ -24,21 +31,26 @@ enum PqgProblemKind : int32_t {
 
 struct PqgProblem {
     int32_t kind;       // PqgProblemKind
-    int32_t nc;         // distinct columns with nonzero multiplicity (<= PQG_MAX_COLS)
+    int32_t nc;         // columns (nonzero multiplicity, padded to the plan's count)
     int32_t n_outer;    // outer digits
-    int32_t P;          // inner walk length = table entries (>= 1)
-    int32_t scale_exp;  // sum of multiplicities minus one: result = sum / 2^scale_exp
+    int32_t P;          // inner codes = table entries (>= 1)
+    int32_t K;          // inner digits
+    int32_t scale_exp;  // result = sum / 2^scale_exp (sum of multiplicities - 1, less column scales)
     int32_t cm_max;     // largest column multiplicity
-    int32_t n_out;      // outputs of this problem (1, or nc for the Laplace form)
-    int32_t pad0;
-    int64_t Q;          // outer assignments (lanes)
+    int32_t n_out;      // outputs of this problem (1, or the Laplace count)
+    int64_t Q;          // outer positions
+    int64_t R;          // outer positions per lane
     int64_t item_begin; // first work item
-    int64_t n_items;    // ceil(Q / 32)
-    int64_t off_base;   // byte offset: nc x double2, FP64 column sums with every digit at 0
-    int64_t off_outer;  // byte offset: n_outer x nc x double2, FP64 rows of the outer digits
-    int64_t off_D;      // byte offset: 2*K x nc complex in kernel precision (K inner digits);
-                        //   row 2k = -2 a_k (digit k steps up), row 2k+1 = +2 a_k (steps down)
-    int64_t off_tab;    // byte offset: P table entries
+    int64_t n_items;    // ceil(Q / (32 R))
+    int64_t off_base64;   // byte offsets into the arena:  nc x double2, column sums with every digit 0
+    int64_t off_outer64;  //   n_outer x nc x double2, rows a_o of the outer digits
+    int64_t off_base_df;  //   nc x float4 {re_hi, re_lo, im_hi, im_lo}, the same column sums
+    int64_t off_outer_df; //   n_outer x nc x float4, the same rows
+    int64_t off_inner64;  //   K x nc x double2, rows a_k of the inner digits
+    int64_t off_D;        //   2 n_outer x nc elements in kernel precision: row 2o = -2 a_o
+                          //   (outer digit o steps up), row 2o+1 = +2 a_o (steps down)
+    int64_t off_tab;      //   P x PqgStep
+    int64_t delta_begin;  // first element of this problem's P x nc prefix table (delta buffer)
     int64_t out_index;  // first output slot of this problem
     int64_t part_begin; // first partial slot (n_out dd-complex slots per item)
     int64_t chunk_begin;// first level-1 reduction chunk
@@ -46,21 +58,16 @@ struct PqgProblem {
     double cval_re, cval_im;          // PQG_KIND_CONSTANT value
     uint8_t cm[PQG_MAX_COLS];         // column multiplicities
     uint8_t outer_m[PQG_MAX_OUTER];   // outer digit multiplicities (radix m + 1)
+    uint8_t inner_m[PQG_MAX_INNER];   // inner digit multiplicities
     uint8_t pad1[4];
 };
 
-// One inner step, complex128 kernels: add row D[drow .. drow+nc) to the column
-// sums, then accumulate w * product.  Entry 0 is the start (drow unused).
-struct PqgStep128 {
-    double w;
-    int32_t drow;  // element offset into the problem's D block
-    int32_t pad;
-};
-
-// One inner step, complex64 kernels.
-struct PqgStep64 {
-    float w;
-    int32_t drow;
+// Inner code t: its signed binomial weight (-1)^sum(g) prod C(m, g), in FP64
+// and FP32.
+struct PqgStep {
+    double wd;
+    float wf;
+    float pad;
 };
 
 // Level-1 reduction chunk: items [item_lo, item_hi) of one problem.

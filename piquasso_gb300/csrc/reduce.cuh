@@ -39,18 +39,16 @@ __global__ void reduce_chunks(const PqgChunk *__restrict__ chunks, const PqgProb
     const PqgChunk c = chunks[blockIdx.x];
     const PqgProblem *pr = probs + c.problem;
     const int n_out = pr->n_out;
-    const double4 *part = reinterpret_cast<const double4 *>(partials);
     for (int o = 0; o < n_out; ++o) {
         ddv r{0.0, 0.0}, i{0.0, 0.0};
         for (int64_t it = c.item_lo + threadIdx.x; it < c.item_hi; it += blockDim.x) {
-            const double4 v = part[pr->part_begin + (it - pr->item_begin) * n_out + o];
-            r = dd_add(r, ddv{v.x, v.y});
-            i = dd_add(i, ddv{v.z, v.w});
+            ddv a, b;
+            load_partial(partials, pr->part_begin + (it - pr->item_begin) * n_out + o, a, b);
+            r = dd_add(r, a);
+            i = dd_add(i, b);
         }
         block_reduce_dd(r, i, scratch);
-        if (threadIdx.x == 0)
-            reinterpret_cast<double4 *>(chunk_out)[static_cast<int64_t>(blockIdx.x) * PQG_MAX_OUT + o] =
-                make_double4(r.hi, r.lo, i.hi, i.lo);
+        if (threadIdx.x == 0) store_partial(chunk_out, static_cast<int64_t>(blockIdx.x) * PQG_MAX_OUT + o, r, i);
     }
 }
 
@@ -74,14 +72,13 @@ __global__ void finish_problems(const PqgProblem *__restrict__ probs, int n_prob
         }
         return;
     }
-    const double4 *co = reinterpret_cast<const double4 *>(chunk_out);
-    const double scale = ldexp(1.0, -pr->scale_exp);
     for (int o = 0; o < pr->n_out; ++o) {
         ddv r{0.0, 0.0}, i{0.0, 0.0};
         for (int64_t c = pr->chunk_begin + lane; c < pr->chunk_begin + pr->n_chunks; c += 32) {
-            const double4 v = co[c * PQG_MAX_OUT + o];
-            r = dd_add(r, ddv{v.x, v.y});
-            i = dd_add(i, ddv{v.z, v.w});
+            ddv a, b;
+            load_partial(chunk_out, c * PQG_MAX_OUT + o, a, b);
+            r = dd_add(r, a);
+            i = dd_add(i, b);
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
@@ -89,8 +86,10 @@ __global__ void finish_problems(const PqgProblem *__restrict__ probs, int n_prob
             i = dd_add(i, dd_shfl_down(i, off));
         }
         if (lane == 0) {
-            // scaling by a power of two is exact in both words
-            const double rh = r.hi * scale, rl = r.lo * scale, ih = i.hi * scale, il = i.lo * scale;
+            // scaling by a power of two is exact in both words; ldexp avoids an
+            // intermediate 2^-scale_exp that would itself overflow
+            const int e = -pr->scale_exp;
+            const double rh = ldexp(r.hi, e), rl = ldexp(r.lo, e), ih = ldexp(i.hi, e), il = ldexp(i.lo, e);
             if constexpr (sizeof(T) == 8) {
                 out[2 * (oi + o)] = rh;
                 out[2 * (oi + o) + 1] = ih;

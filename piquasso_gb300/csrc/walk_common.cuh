@@ -102,6 +102,7 @@ struct WalkArgs {
     const PqgProblem *probs;
     const int64_t *item_begin;
     const unsigned char *arena;
+    const void *delta;            // prefix tables, kernel precision, indexed by delta_begin
     unsigned long long *counter;  // work-queue head, zeroed before the launch
     double *partials;             // 4 doubles per slot: re_hi, re_lo, im_hi, im_lo
     int64_t total_items;
@@ -117,45 +118,36 @@ __device__ __forceinline__ int64_t next_item(unsigned long long *counter, int la
 }
 
 __device__ __forceinline__ void store_partial(double *partials, int64_t slot, ddv re, ddv im) {
-    double4 v = make_double4(re.hi, re.lo, im.hi, im.lo);
-    reinterpret_cast<double4 *>(partials)[slot] = v;
+    double2 *p = reinterpret_cast<double2 *>(partials) + 2 * slot;
+    p[0] = make_double2(re.hi, re.lo);
+    p[1] = make_double2(im.hi, im.lo);
 }
 
-// Seeds the FP64 column sums of outer assignment q: base - 2 * sum_o g_o a_o,
-// and returns the signed binomial weight (-1)^sum(g) * prod C(m_o, g_o).
-template <int NC>
-__device__ __forceinline__ double seed_outer(const PqgProblem *__restrict__ pr, const unsigned char *__restrict__ arena,
-                                             int64_t q, double (&cr)[NC], double (&ci)[NC]) {
-    const double2 *base = reinterpret_cast<const double2 *>(arena + pr->off_base);
-#pragma unroll
-    for (int j = 0; j < NC; ++j) {
-        double2 v = __ldg(base + j);
-        cr[j] = v.x;
-        ci[j] = v.y;
+__device__ __forceinline__ void load_partial(const double *partials, int64_t slot, ddv &re, ddv &im) {
+    const double2 *p = reinterpret_cast<const double2 *>(partials) + 2 * slot;
+    const double2 a = p[0], b = p[1];
+    re = ddv{a.x, a.y};
+    im = ddv{b.x, b.y};
+}
+
+// Reflected mixed-radix Gray code of position r over `n` digits with
+// multiplicities m (radix m + 1, digit 0 fastest): counter digits, then the
+// code from the top digit down (src/n_aryGrayCodeCounter.hpp:170-194 of the
+// reference, with a 64-bit position).  Writes the code digits to g.
+__device__ __forceinline__ void gray_decode(const uint8_t *__restrict__ m, int n, int64_t r, uint8_t *g) {
+    uint8_t c[PQG_MAX_OUTER];
+    for (int o = 0; o < n; ++o) {
+        const int L = m[o] + 1;
+        c[o] = static_cast<uint8_t>(r % L);
+        r /= L;
     }
-    const double2 *orow = reinterpret_cast<const double2 *>(arena + pr->off_outer);
-    const int n_outer = pr->n_outer;
-    double w = 1.0;
-    int par = 0;
-    int64_t rem = q;
-    for (int o = 0; o < n_outer; ++o) {
-        const int m = pr->outer_m[o];
-        const int g = static_cast<int>(rem % (m + 1));
-        rem /= (m + 1);
-        if (g) {
-            const double f = -2.0 * g;
-            const double2 *r = orow + static_cast<int64_t>(o) * NC;
-#pragma unroll
-            for (int j = 0; j < NC; ++j) {
-                double2 v = __ldg(r + j);
-                cr[j] = __fma_rn(f, v.x, cr[j]);
-                ci[j] = __fma_rn(f, v.y, ci[j]);
-            }
-            w *= static_cast<double>(binom64(m, g));
-            par += g;
-        }
+    int parity = 0;
+    for (int o = n - 1; o >= 0; --o) {
+        const int L = m[o] + 1;
+        const int code = parity ? L - 1 - c[o] : c[o];
+        g[o] = static_cast<uint8_t>(code);
+        parity ^= (code & 1);
     }
-    return (par & 1) ? -w : w;
 }
 
 }  // namespace pqg

@@ -1,0 +1,101 @@
+// Complex128-accurate walk on the FP32 pipes ("double-float").
+//
+// GB300 executes FP64 at about 1/61 of its FP32 rate, so the plain
+// complex128 walk is FP64-pipe bound.  This kernel keeps the FP64 steps the
+// method's stability needs — the per-segment seeding of the column sums and
+// the double-double accumulation across steps, lanes and blocks — and does the
+// per-step column updates and products in double-float arithmetic: every real
+// number is an unevaluated sum hi + lo of two floats, with the error-free
+// transforms TwoSum (Knuth) and FMA-based TwoProduct, giving about 2^-48
+// relative precision per operation (T. J. Dekker, "A floating-point technique
+// for extending the available precision", Numer. Math. 18, 1971).
+//
+// FP32 has an 8-bit exponent, so the planner scales every column by a power of
+// two such that no column sum can exceed 1 in magnitude (|c_j| <= sum_i m_i
+// |a_ij| <= 1); the scale is undone exactly in the final 2^-e factor.  The
+// planner only selects this arithmetic when the typical term stays far above
+// the FP32 underflow threshold (see plan.cpp).  The kernel itself is the
+// generic walk of walk_plain.cuh with the ArDF policy.
+#pragma once
+#include "walk_common.cuh"
+
+namespace pqg {
+
+struct dfl {
+    float hi, lo;
+};
+
+// a + b, both double-float; TwoSum on the high words, then renormalise
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float v = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+    const float l = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+    const float h = __fadd_rn(s, l);
+    return {h, __fsub_rn(l, __fsub_rn(h, s))};
+}
+
+// real part of a product: ah*bh - ch*dh (+ low-order cross terms), with
+// (ah + al), (bh + bl), (ch + cl), (dh + dl) double-float operands
+__device__ __forceinline__ dfl df_mul_sub(dfl a, dfl b, dfl c, dfl d) {
+    const float p1 = __fmul_rn(a.hi, b.hi);
+    const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+    const float p2 = __fmul_rn(c.hi, d.hi);
+    const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+    const float s = __fsub_rn(p1, p2);
+    const float v = __fsub_rn(s, p1);
+    const float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(-p2, v));
+    float low = __fadd_rn(__fsub_rn(e1, e2), t);
+    low = __fmaf_rn(a.hi, b.lo, low);
+    low = __fmaf_rn(a.lo, b.hi, low);
+    low = __fmaf_rn(-c.hi, d.lo, low);
+    low = __fmaf_rn(-c.lo, d.hi, low);
+    const float h = __fadd_rn(s, low);
+    return {h, __fsub_rn(low, __fsub_rn(h, s))};
+}
+
+// imaginary part: ah*bh + ch*dh (+ cross terms)
+__device__ __forceinline__ dfl df_mul_add(dfl a, dfl b, dfl c, dfl d) {
+    const float p1 = __fmul_rn(a.hi, b.hi);
+    const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+    const float p2 = __fmul_rn(c.hi, d.hi);
+    const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+    const float s = __fadd_rn(p1, p2);
+    const float v = __fsub_rn(s, p1);
+    const float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
+    float low = __fadd_rn(__fadd_rn(e1, e2), t);
+    low = __fmaf_rn(a.hi, b.lo, low);
+    low = __fmaf_rn(a.lo, b.hi, low);
+    low = __fmaf_rn(c.hi, d.lo, low);
+    low = __fmaf_rn(c.lo, d.hi, low);
+    const float h = __fadd_rn(s, low);
+    return {h, __fsub_rn(low, __fsub_rn(h, s))};
+}
+
+// (xr + i xi) *= (yr + i yi)
+__device__ __forceinline__ void df_cmul(dfl &xr, dfl &xi, dfl yr, dfl yi) {
+    const dfl r = df_mul_sub(xr, yr, xi, yi);
+    const dfl i = df_mul_add(xr, yi, xi, yr);
+    xr = r;
+    xi = i;
+}
+
+// w * x for a float w that is an exact small integer
+__device__ __forceinline__ dfl df_scale(dfl x, float w) {
+    const float p = __fmul_rn(w, x.hi);
+    const float e = __fmaf_rn(w, x.hi, -p);
+    const float l = __fmaf_rn(w, x.lo, e);
+    const float h = __fadd_rn(p, l);
+    return {h, __fsub_rn(l, __fsub_rn(h, p))};
+}
+
+__device__ __forceinline__ dfl df_split(double x) {
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - static_cast<double>(h))};
+}
+
+__device__ __forceinline__ ddv dd_add_df(ddv a, dfl x) {
+    return dd_add_d(dd_add_d(a, static_cast<double>(x.hi)), static_cast<double>(x.lo));
+}
+
+}  // namespace pqg

@@ -7,9 +7,10 @@
 //     out_l += w * prefix_l * suffix_l * c_l^(m_l - 1),
 // and the final suffix w * prod_l c_l^(m_l) is the value shared by every
 // column of multiplicity zero (their exponent stays 0 in the reference).
-// Work split, seeding and reductions are those of the plain kernels.
+// Work split (with one outer position per lane), seeding, prefix tables and
+// reductions are those of the plain kernels.
 #pragma once
-#include "walk_common.cuh"
+#include "walk_plain.cuh"
 
 namespace pqg {
 
@@ -43,10 +44,12 @@ struct LaplaceC128Cfg {
         (ACC_SMEM ? size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) : 0);
 };
 
-// Complex128 Laplace walk.  Per-lane sums are plain FP64 over one inner walk
-// (at most 512 steps), combined across lanes, items and chunks in double-double.
+// Complex128 Laplace walk.  One outer position per lane (R = 1), seeded in
+// FP64; the column sums of inner code t are seed + Delta(t).  Per-lane sums are
+// plain FP64 over one inner walk (at most 512 codes), combined across lanes,
+// items and chunks in double-double.
 template <int NC>
-__global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c128(WalkArgs A) {
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 1) walk_laplace_c128(WalkArgs A) {
     using Cfg = LaplaceC128Cfg<NC>;
     extern __shared__ double2 lap_smem[];
     const int lane = threadIdx.x & 31;
@@ -66,40 +69,52 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c128(WalkArgs A
         const bool full = n_out > NC;
         double wout = 0.0;
         if (q < pr->Q) {
-            double cr[NC], ci[NC];
-            wout = seed_outer<NC>(pr, A.arena, q, cr, ci);
+            double sr0[NC], si0[NC];  // FP64 seed of this lane's outer position
+            {
+                OuterState st;
+                outer_decode(pr, q, st);
+                ArF64::cs_t s[NC];
+                seed_lane<ArF64, NC>(pr, A.arena, st, s);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
+                }
+                wout = outer_weight(pr, st);
+            }
             int cm[NC];
 #pragma unroll
             for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
             const bool ones = pr->cm_max == 1;
-            const PqgStep128 *tab = reinterpret_cast<const PqgStep128 *>(A.arena + pr->off_tab);
-            const double2 *D = reinterpret_cast<const double2 *>(A.arena + pr->off_D);
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const double2 *delta = reinterpret_cast<const double2 *>(A.delta) + pr->delta_begin;
             const int P = pr->P;
 #pragma unroll
             for (int l = 0; l <= NC; ++l) acc.set(l, make_double2(0.0, 0.0));
 
             for (int t = 0; t < P; ++t) {
-                const double w = __ldg(&tab[t].w);
-                if (t > 0) {
-                    const double2 *d = D + __ldg(&tab[t].drow);
-#pragma unroll
-                    for (int j = 0; j < NC; ++j) {
-                        const double2 v = __ldg(d + j);
-                        cr[j] = __dadd_rn(cr[j], v.x);
-                        ci[j] = __dadd_rn(ci[j], v.y);
-                    }
-                }
+                const double w = __ldg(&tab[t].wd);
+                // column sums of inner code t are seed + prefix-table row t,
+                // formed where they are used (no per-step array of sums)
+                const double2 *d = delta + static_cast<int64_t>(t) * NC;
+                auto col = [&](int j, double &cr, double &ci) {
+                    const double2 v = __ldg(d + j);
+                    cr = __dadd_rn(sr0[j], v.x);
+                    ci = __dadd_rn(si0[j], v.y);
+                };
                 // prefix products: pre_l = prod_{k<l} c_k^(m_k)
                 double xr = 1.0, xi = 0.0;
                 pre.set(0, make_double2(1.0, 0.0));
 #pragma unroll
                 for (int j = 0; j + 1 < NC; ++j) {
+                    double cr, ci;
+                    col(j, cr, ci);
                     if (j == 0 && (ones || cm[0] == 1)) {
-                        xr = cr[0];
-                        xi = ci[0];
+                        xr = cr;
+                        xi = ci;
                     } else {
                         const int e = ones ? 1 : cm[j];
-                        for (int r = 0; r < e; ++r) cmul(xr, xi, cr[j], ci[j]);
+                        for (int r = 0; r < e; ++r) cmul(xr, xi, cr, ci);
                     }
                     pre.set(j + 1, make_double2(xr, xi));
                 }
@@ -107,6 +122,8 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c128(WalkArgs A
                 double sr = w, si = 0.0;
 #pragma unroll
                 for (int l = NC - 1; l >= 0; --l) {
+                    double cr, ci;
+                    col(l, cr, ci);
                     const double2 p = pre.get(l);
                     double tr, ti;
                     if (l == NC - 1) {
@@ -121,20 +138,20 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c128(WalkArgs A
                         cmul(tr, ti, sr, si);
                     }
                     if (!ones)
-                        for (int r = 1; r < cm[l]; ++r) cmul(tr, ti, cr[l], ci[l]);
+                        for (int r = 1; r < cm[l]; ++r) cmul(tr, ti, cr, ci);
                     double2 a = acc.get(l);
                     a.x = __dadd_rn(a.x, tr);
                     a.y = __dadd_rn(a.y, ti);
                     acc.set(l, a);
                     if (l > 0 || full) {
                         if (l == NC - 1) {
-                            sr = w * cr[l];
-                            si = w * ci[l];
+                            sr = w * cr;
+                            si = w * ci;
                             if (!ones)
-                                for (int r = 1; r < cm[l]; ++r) cmul(sr, si, cr[l], ci[l]);
+                                for (int r = 1; r < cm[l]; ++r) cmul(sr, si, cr, ci);
                         } else {
                             const int e = ones ? 1 : cm[l];
-                            for (int r = 0; r < e; ++r) cmul(sr, si, cr[l], ci[l]);
+                            for (int r = 0; r < e; ++r) cmul(sr, si, cr, ci);
                         }
                     }
                 }
@@ -175,10 +192,11 @@ struct LaplaceC64Cfg {
         size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2);
 };
 
-// Complex64 Laplace walk: FP32 updates and products, FP32 partial sums over
-// 32 steps folded into per-lane FP64 sums held in shared memory.
+// Complex64 Laplace walk: seed in double-float rounded to FP32, column sums
+// seed + Delta(t) and products in FP32, FP32 partial sums over 32 codes folded
+// into per-lane FP64 sums held in shared memory.
 template <int NC>
-__global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c64(WalkArgs A) {
+__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_laplace_c64(WalkArgs A) {
     using Cfg = LaplaceC64Cfg<NC>;
     extern __shared__ double2 lap_smem64[];
     const int lane = threadIdx.x & 31;
@@ -198,22 +216,25 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c64(WalkArgs A)
         const bool full = n_out > NC;
         double wout = 0.0;
         if (q < pr->Q) {
-            float cr[NC], ci[NC];
+            float sr0[NC], si0[NC];  // seed of this lane's outer position (double-float, rounded)
             {
-                double dr[NC], di[NC];
-                wout = seed_outer<NC>(pr, A.arena, q, dr, di);
+                OuterState st;
+                outer_decode(pr, q, st);
+                ArF32::cs_t s[NC];
+                seed_lane<ArF32, NC>(pr, A.arena, st, s);
 #pragma unroll
                 for (int j = 0; j < NC; ++j) {
-                    cr[j] = __double2float_rn(dr[j]);
-                    ci[j] = __double2float_rn(di[j]);
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
                 }
+                wout = outer_weight(pr, st);
             }
             int cm[NC];
 #pragma unroll
             for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
             const bool ones = pr->cm_max == 1;
-            const PqgStep64 *tab = reinterpret_cast<const PqgStep64 *>(A.arena + pr->off_tab);
-            const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const float2 *delta = reinterpret_cast<const float2 *>(A.delta) + pr->delta_begin;
             const int P = pr->P;
             float ar[NC + 1], ai[NC + 1];
 #pragma unroll
@@ -224,33 +245,33 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c64(WalkArgs A)
             }
 
             for (int t = 0; t < P; ++t) {
-                const float2 e = __ldg(reinterpret_cast<const float2 *>(tab + t));
-                const float w = e.x;
-                if (t > 0) {
-                    const float2 *d = D + __float_as_int(e.y);
-#pragma unroll
-                    for (int j = 0; j < NC; ++j) {
-                        const float2 v = __ldg(d + j);
-                        cr[j] = __fadd_rn(cr[j], v.x);
-                        ci[j] = __fadd_rn(ci[j], v.y);
-                    }
-                }
+                const float w = __ldg(&tab[t].wf);
+                const float2 *d = delta + static_cast<int64_t>(t) * NC;
+                auto col = [&](int j, float &cr, float &ci) {
+                    const float2 v = __ldg(d + j);
+                    cr = __fadd_rn(sr0[j], v.x);
+                    ci = __fadd_rn(si0[j], v.y);
+                };
                 float xr = 1.0f, xi = 0.0f;
                 pre.set(0, make_float2(1.0f, 0.0f));
 #pragma unroll
                 for (int j = 0; j + 1 < NC; ++j) {
+                    float cr, ci;
+                    col(j, cr, ci);
                     if (j == 0 && (ones || cm[0] == 1)) {
-                        xr = cr[0];
-                        xi = ci[0];
+                        xr = cr;
+                        xi = ci;
                     } else {
                         const int ee = ones ? 1 : cm[j];
-                        for (int r = 0; r < ee; ++r) cmulf(xr, xi, cr[j], ci[j]);
+                        for (int r = 0; r < ee; ++r) cmulf(xr, xi, cr, ci);
                     }
                     pre.set(j + 1, make_float2(xr, xi));
                 }
                 float sr = w, si = 0.0f;
 #pragma unroll
                 for (int l = NC - 1; l >= 0; --l) {
+                    float cr, ci;
+                    col(l, cr, ci);
                     const float2 p = pre.get(l);
                     float tr, ti;
                     if (l == NC - 1) {
@@ -265,18 +286,18 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_laplace_c64(WalkArgs A)
                         cmulf(tr, ti, sr, si);
                     }
                     if (!ones)
-                        for (int r = 1; r < cm[l]; ++r) cmulf(tr, ti, cr[l], ci[l]);
+                        for (int r = 1; r < cm[l]; ++r) cmulf(tr, ti, cr, ci);
                     ar[l] += tr;
                     ai[l] += ti;
                     if (l > 0 || full) {
                         if (l == NC - 1) {
-                            sr = w * cr[l];
-                            si = w * ci[l];
+                            sr = w * cr;
+                            si = w * ci;
                             if (!ones)
-                                for (int r = 1; r < cm[l]; ++r) cmulf(sr, si, cr[l], ci[l]);
+                                for (int r = 1; r < cm[l]; ++r) cmulf(sr, si, cr, ci);
                         } else {
                             const int ee = ones ? 1 : cm[l];
-                            for (int r = 0; r < ee; ++r) cmulf(sr, si, cr[l], ci[l]);
+                            for (int r = 0; r < ee; ++r) cmulf(sr, si, cr, ci);
                         }
                     }
                 }

@@ -1,95 +1,301 @@
-// Plain permanent walk kernels (one output per problem).
+// Plain permanent walk kernels (one output per problem), one template for the
+// three arithmetics:
+//   ArF64 — complex128: FP64 column sums, updates and products;
+//   ArF32 — complex64: FP32 updates and products, FP32 TwoSum-compensated sums;
+//   ArDF  — complex128 accuracy on the FP32 pipes: double-float updates and
+//           products (see walk_df.cuh).
+// All seeds are formed at 48 bits or more (FP64 for ArF64, double-float for the
+// FP32-pipe kernels, whose FP64 pipe runs at 1/61 of the FP32 rate on GB300),
+// and every segment's sum is folded into a per-lane double-double.
 //
-// Persistent grid; every warp pulls work items (one problem, 32 consecutive
-// outer assignments) from a device queue.  Each lane seeds its column sums in
-// FP64 from scratch, then all 32 lanes walk the problem's inner Gray-code
-// table in lock step: per step one column update (the changed row is the same
-// for the whole warp, so its values are broadcast loads) and one product over
-// the columns with their multiplicities.  The weighted terms are summed in
-// short blocks and folded into a per-lane double-double; lanes are combined by
-// a double-double warp reduction and the item's result is written to its
-// partial slot.  Method: src/permanent.cpp:155-250 of the reference, with the
-// Gray-code space split into a lock-step inner walk and per-lane outer seeds.
+// Schedule (method of the reference's src/permanent.cpp:155-250, with the
+// Gray-code space split into a lock-step inner walk and per-lane outer runs):
+// a persistent grid; every warp pulls work items (one problem, 32 lanes x R
+// outer positions) from a device queue.  Each lane seeds its column sums at
+// its first outer position, then for each of its R positions walks the
+// problem's P inner codes — forward, then backward, alternately — and between
+// positions applies the one-digit outer update of the reflected Gray code to
+// its seed.  At inner code t the column sums are seed + Delta(t): one prefix-
+// table row, the same for the whole warp (broadcast loads), one addition per
+// column, no accumulated rounding; then one product over the columns.
 #pragma once
 #include "walk_common.cuh"
+#include "walk_df.cuh"
 
 namespace pqg {
 
-// Complex128: FP64 column sums, updates and products.
-template <int NC>
-__global__ void __launch_bounds__(PQG_WALK_THREADS) walk_plain_c128(WalkArgs A) {
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-        const int64_t item = next_item(A.counter, lane);
-        if (item >= A.total_items) return;
-        const int ip = find_problem(A.item_begin, A.n_probs, item);
-        const PqgProblem *pr = A.probs + ip;
-        const int64_t local = item - pr->item_begin;
-        const int64_t q = local * PQG_ITEM_LANES + lane;
-        ddv sr{0.0, 0.0}, si{0.0, 0.0};
-        if (q < pr->Q) {
-            double cr[NC], ci[NC];
-            const double wout = seed_outer<NC>(pr, A.arena, q, cr, ci);
-            int cm[NC];
-#pragma unroll
-            for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
-            const bool ones = pr->cm_max == 1;
-            const PqgStep128 *tab = reinterpret_cast<const PqgStep128 *>(A.arena + pr->off_tab);
-            const double2 *D = reinterpret_cast<const double2 *>(A.arena + pr->off_D);
-            const int P = pr->P;
+// ------------------------------------------------------------------ policies
+struct ArF64 {
+    struct cs_t {
+        double r, i;
+    };
+    using d_t = double2;
+    struct acc_t {
+        double r, i;
+    };
+    static constexpr bool kDfSeed = false;
+    static constexpr bool kTwoChains = false;  // FP64-pipe bound: one chain
+    __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {r, i}; }
+    __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r.hi, i.hi}; }
+    __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
+        c.r = __dadd_rn(c.r, d.x);
+        c.i = __dadd_rn(c.i, d.y);
+    }
+    __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
+        return {__dadd_rn(c.r, d.x), __dadd_rn(c.i, d.y)};
+    }
+    __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { cmul(x.r, x.i, y.r, y.i); }
+    __device__ __forceinline__ static acc_t zero() { return {0.0, 0.0}; }
+    __device__ __forceinline__ static void accumulate(acc_t &a, const cs_t &x, const PqgStep &s) {
+        a.r = __fma_rn(s.wd, x.r, a.r);
+        a.i = __fma_rn(s.wd, x.i, a.i);
+    }
+    __device__ __forceinline__ static void fold(ddv &sr, ddv &si, const acc_t &a, double w) {
+        sr = dd_add(sr, dd_mul_d(ddv{a.r, 0.0}, w));
+        si = dd_add(si, dd_mul_d(ddv{a.i, 0.0}, w));
+    }
+};
 
-            auto product = [&](double &xr, double &xi) {
-                xr = cr[0];
-                xi = ci[0];
-                if (ones) {
-#pragma unroll
-                    for (int j = 1; j < NC; ++j) cmul(xr, xi, cr[j], ci[j]);
-                } else {
-                    for (int r = 1; r < cm[0]; ++r) cmul(xr, xi, cr[0], ci[0]);
-#pragma unroll
-                    for (int j = 1; j < NC; ++j)
-                        for (int r = 0; r < cm[j]; ++r) cmul(xr, xi, cr[j], ci[j]);
-                }
-            };
+struct ArF32 {
+    struct cs_t {
+        float r, i;
+    };
+    using d_t = float2;
+    struct acc_t {
+        float r, cr, i, ci;  // TwoSum-compensated partial sums
+    };
+    static constexpr bool kDfSeed = true;
+    static constexpr bool kTwoChains = true;
+    __device__ __forceinline__ static cs_t from_seed64(double r, double i) {
+        return {__double2float_rn(r), __double2float_rn(i)};
+    }
+    __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) {
+        return {__fadd_rn(r.hi, r.lo), __fadd_rn(i.hi, i.lo)};
+    }
+    __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
+        c.r = __fadd_rn(c.r, d.x);
+        c.i = __fadd_rn(c.i, d.y);
+    }
+    __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
+        return {__fadd_rn(c.r, d.x), __fadd_rn(c.i, d.y)};
+    }
+    __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { cmulf(x.r, x.i, y.r, y.i); }
+    __device__ __forceinline__ static acc_t zero() { return {0.0f, 0.0f, 0.0f, 0.0f}; }
+    __device__ __forceinline__ static void accumulate(acc_t &a, const cs_t &x, const PqgStep &s) {
+        f_two_sum_acc(a.r, a.cr, __fmul_rn(s.wf, x.r));
+        f_two_sum_acc(a.i, a.ci, __fmul_rn(s.wf, x.i));
+    }
+    __device__ __forceinline__ static void fold(ddv &sr, ddv &si, const acc_t &a, double w) {
+        const ddv r = dd_add_d(ddv{static_cast<double>(a.r), 0.0}, static_cast<double>(a.cr));
+        const ddv i = dd_add_d(ddv{static_cast<double>(a.i), 0.0}, static_cast<double>(a.ci));
+        sr = dd_add(sr, dd_mul_d(r, w));
+        si = dd_add(si, dd_mul_d(i, w));
+    }
+};
 
-            double ar, ai;
-            product(ar, ai);  // step 0: weight 1
-            for (int t = 1; t < P; ++t) {
-                const double w = __ldg(&tab[t].w);
-                const double2 *d = D + __ldg(&tab[t].drow);
-#pragma unroll
-                for (int j = 0; j < NC; ++j) {
-                    const double2 v = __ldg(d + j);
-                    cr[j] = __dadd_rn(cr[j], v.x);
-                    ci[j] = __dadd_rn(ci[j], v.y);
-                }
-                double xr, xi;
-                product(xr, xi);
-                ar = __fma_rn(w, xr, ar);
-                ai = __fma_rn(w, xi, ai);
-                if ((t & 63) == 0) {
-                    sr = dd_add_d(sr, ar);
-                    si = dd_add_d(si, ai);
-                    ar = 0.0;
-                    ai = 0.0;
-                }
-            }
-            sr = dd_mul_d(dd_add_d(sr, ar), wout);
-            si = dd_mul_d(dd_add_d(si, ai), wout);
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            sr = dd_add(sr, dd_shfl_down(sr, off));
-            si = dd_add(si, dd_shfl_down(si, off));
-        }
-        if (lane == 0) store_partial(A.partials, pr->part_begin + local, sr, si);
+struct ArDF {
+    struct cs_t {
+        dfl r, i;
+    };
+    using d_t = float4;  // re_hi, re_lo, im_hi, im_lo
+    struct acc_t {
+        dfl r, i;
+    };
+    static constexpr bool kDfSeed = true;
+    static constexpr bool kTwoChains = true;
+    __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {df_split(r), df_split(i)}; }
+    __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r, i}; }
+    __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
+        c.r = df_add(c.r, dfl{d.x, d.y});
+        c.i = df_add(c.i, dfl{d.z, d.w});
+    }
+    __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
+        return {df_add(c.r, dfl{d.x, d.y}), df_add(c.i, dfl{d.z, d.w})};
+    }
+    __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { df_cmul(x.r, x.i, y.r, y.i); }
+    __device__ __forceinline__ static acc_t zero() { return {{0.0f, 0.0f}, {0.0f, 0.0f}}; }
+    __device__ __forceinline__ static void accumulate(acc_t &a, const cs_t &x, const PqgStep &s) {
+        a.r = df_add(a.r, df_scale(x.r, s.wf));
+        a.i = df_add(a.i, df_scale(x.i, s.wf));
+    }
+    __device__ __forceinline__ static void fold(ddv &sr, ddv &si, const acc_t &a, double w) {
+        const ddv r = dd_add_d(ddv{static_cast<double>(a.r.hi), 0.0}, static_cast<double>(a.r.lo));
+        const ddv i = dd_add_d(ddv{static_cast<double>(a.i.hi), 0.0}, static_cast<double>(a.i.lo));
+        sr = dd_add(sr, dd_mul_d(r, w));
+        si = dd_add(si, dd_mul_d(i, w));
+    }
+};
+
+// --------------------------------------------------------- outer Gray state
+// Per-lane position in the reflected mixed-radix Gray code over the outer
+// digits (digit 0 fastest): counter digits c and code digits g.
+struct OuterState {
+    uint8_t c[PQG_MAX_OUTER];
+    uint8_t g[PQG_MAX_OUTER];
+};
+
+// Decodes position r into the counter digits c and the reflected code g.
+__device__ __forceinline__ void outer_decode(const PqgProblem *__restrict__ pr, int64_t r, OuterState &st) {
+    const int n = pr->n_outer;
+    for (int o = 0; o < n; ++o) {
+        const int L = pr->outer_m[o] + 1;
+        st.c[o] = static_cast<uint8_t>(r % L);
+        r /= L;
+    }
+    int parity = 0;
+    for (int o = n - 1; o >= 0; --o) {
+        const int L = pr->outer_m[o] + 1;
+        const int code = parity ? L - 1 - st.c[o] : st.c[o];
+        st.g[o] = static_cast<uint8_t>(code);
+        parity ^= (code & 1);
     }
 }
 
-// Complex64: FP32 column updates and products; FP32 TwoSum-compensated
-// partial sums folded into a per-lane double-double every 128 steps.
+// Advances to the next position: the incremented counter digit k is the only
+// code digit that changes, by +1 when the higher code digits sum to an even
+// number, else by -1.  Returns k; *up receives the direction.
+__device__ __forceinline__ int outer_next(const PqgProblem *__restrict__ pr, OuterState &st, bool *up) {
+    const int n = pr->n_outer;
+    int k = 0;
+    while (k < n - 1 && st.c[k] == pr->outer_m[k]) {
+        st.c[k] = 0;
+        ++k;
+    }
+    st.c[k] = static_cast<uint8_t>(st.c[k] + 1);
+    int par = 0;
+    for (int o = k + 1; o < n; ++o) par ^= (st.g[o] & 1);
+    *up = (par == 0);
+    st.g[k] = static_cast<uint8_t>(st.g[k] + (*up ? 1 : -1));
+    return k;
+}
+
+// signed weight of the current outer code: (-1)^sum(g) prod C(m, g)
+__device__ __forceinline__ double outer_weight(const PqgProblem *__restrict__ pr, const OuterState &st) {
+    int64_t w = 1;
+    int par = 0;
+    for (int o = 0; o < pr->n_outer; ++o) {
+        const int g = st.g[o];
+        if (g) {
+            w *= binom64(pr->outer_m[o], g);
+            par += g;
+        }
+    }
+    return (par & 1) ? -static_cast<double>(w) : static_cast<double>(w);
+}
+
+template <class Ar, int NC>
+__device__ __forceinline__ void seed_lane(const PqgProblem *__restrict__ pr, const unsigned char *__restrict__ arena,
+                                          const OuterState &st, typename Ar::cs_t (&cs)[NC]) {
+    if constexpr (Ar::kDfSeed) {
+        // double-float seed on the FP32 pipes: base - 2 sum_o g_o a_o
+        const float4 *base = reinterpret_cast<const float4 *>(arena + pr->off_base_df);
+        const float4 *orow = reinterpret_cast<const float4 *>(arena + pr->off_outer_df);
+        dfl sr[NC], si[NC];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            const float4 v = __ldg(base + j);
+            sr[j] = dfl{v.x, v.y};
+            si[j] = dfl{v.z, v.w};
+        }
+        for (int o = 0; o < pr->n_outer; ++o) {
+            const int g = st.g[o];
+            if (!g) continue;
+            const float f = -2.0f * static_cast<float>(g);
+            const float4 *r = orow + static_cast<int64_t>(o) * NC;
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+                const float4 v = __ldg(r + j);
+                sr[j] = df_add(sr[j], df_scale(dfl{v.x, v.y}, f));
+                si[j] = df_add(si[j], df_scale(dfl{v.z, v.w}, f));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NC; ++j) cs[j] = Ar::from_seed_df(sr[j], si[j]);
+    } else {
+        const double2 *base = reinterpret_cast<const double2 *>(arena + pr->off_base64);
+        const double2 *orow = reinterpret_cast<const double2 *>(arena + pr->off_outer64);
+        double cr[NC], ci[NC];
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            const double2 v = __ldg(base + j);
+            cr[j] = v.x;
+            ci[j] = v.y;
+        }
+        for (int o = 0; o < pr->n_outer; ++o) {
+            const int g = st.g[o];
+            if (!g) continue;
+            const double f = -2.0 * g;
+            const double2 *r = orow + static_cast<int64_t>(o) * NC;
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+                const double2 v = __ldg(r + j);
+                cr[j] = __fma_rn(f, v.x, cr[j]);
+                ci[j] = __fma_rn(f, v.y, ci[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NC; ++j) cs[j] = Ar::from_seed64(cr[j], ci[j]);
+    }
+}
+
+// Product of the column sums seed_j + delta_j (delta_j: the inner code's
+// prefix-table row) with their multiplicities.  Each column sum is formed
+// right before it enters the product, so a loaded table value is consumed at
+// once.  FP32-pipe arithmetics multiply even and odd columns in two independent
+// chains (twice the instruction-level parallelism of one serial chain) and
+// join them at the end.
+template <class Ar, int NC>
+__device__ __forceinline__ typename Ar::cs_t row_product(const typename Ar::cs_t (&seed)[NC],
+                                                         const typename Ar::d_t *__restrict__ d,
+                                                         const uint8_t *__restrict__ cm, bool ones) {
+    using cs_t = typename Ar::cs_t;
+    constexpr bool two = Ar::kTwoChains && NC >= 4;
+    const cs_t c0 = Ar::sum(seed[0], d[0]);
+    cs_t x = c0;
+    cs_t y;
+    if constexpr (two) y = Ar::sum(seed[1], d[1]);
+    if (ones) {
+#pragma unroll
+        for (int j = two ? 2 : 1; j < NC; ++j) {
+            const cs_t c = Ar::sum(seed[j], d[j]);
+            if (two && (j & 1))
+                Ar::mul(y, c);
+            else
+                Ar::mul(x, c);
+        }
+    } else {
+        for (int r = 1; r < cm[0]; ++r) Ar::mul(x, c0);
+        if constexpr (two) {
+            const cs_t c1 = y;
+            for (int r = 1; r < cm[1]; ++r) Ar::mul(y, c1);
+        }
+#pragma unroll
+        for (int j = two ? 2 : 1; j < NC; ++j) {
+            const cs_t c = Ar::sum(seed[j], d[j]);
+            for (int r = 0; r < cm[j]; ++r) {
+                if (two && (j & 1))
+                    Ar::mul(y, c);
+                else
+                    Ar::mul(x, c);
+            }
+        }
+    }
+    if constexpr (two) Ar::mul(x, y);
+    return x;
+}
+
+// Blocks per SM the register allocation must allow: the column sums of the
+// wider kernels need up to 255 registers per thread, and a spill inside the
+// step loop costs more than the occupancy it buys.
 template <int NC>
-__global__ void __launch_bounds__(PQG_WALK_THREADS) walk_plain_c64(WalkArgs A) {
+constexpr int walk_min_blocks() {
+    return NC <= 8 ? 4 : (NC <= 16 ? 3 : 2);
+}
+
+template <class Ar, int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_plain(WalkArgs A) {
+    using cs_t = typename Ar::cs_t;
+    using d_t = typename Ar::d_t;
     const int lane = threadIdx.x & 31;
     for (;;) {
         const int64_t item = next_item(A.counter, lane);
@@ -97,68 +303,50 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS) walk_plain_c64(WalkArgs A) {
         const int ip = find_problem(A.item_begin, A.n_probs, item);
         const PqgProblem *pr = A.probs + ip;
         const int64_t local = item - pr->item_begin;
-        const int64_t q = local * PQG_ITEM_LANES + lane;
+        const int64_t R = pr->R;
+        const int64_t Q = pr->Q;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
         ddv sr{0.0, 0.0}, si{0.0, 0.0};
-        if (q < pr->Q) {
-            float cr[NC], ci[NC];
-            double wout;
-            {
-                double dr[NC], di[NC];
-                wout = seed_outer<NC>(pr, A.arena, q, dr, di);
-#pragma unroll
-                for (int j = 0; j < NC; ++j) {
-                    cr[j] = __double2float_rn(dr[j]);
-                    ci[j] = __double2float_rn(di[j]);
-                }
-            }
-            int cm[NC];
-#pragma unroll
-            for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
+        if (r0 < Q) {
+            OuterState st;
+            outer_decode(pr, r0, st);
+            cs_t seed[NC];
+            seed_lane<Ar, NC>(pr, A.arena, st, seed);
+            double wout = outer_weight(pr, st);
+            // column multiplicities are read from the problem (L1) only when
+            // some exceed 1; keeping them out of registers leaves room for the sums
+            const uint8_t *cm = pr->cm;
             const bool ones = pr->cm_max == 1;
-            const PqgStep64 *tab = reinterpret_cast<const PqgStep64 *>(A.arena + pr->off_tab);
-            const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const d_t *D = reinterpret_cast<const d_t *>(A.arena + pr->off_D);
+            const d_t *delta = reinterpret_cast<const d_t *>(A.delta) + pr->delta_begin;
             const int P = pr->P;
-
-            auto product = [&](float &xr, float &xi) {
-                xr = cr[0];
-                xi = ci[0];
-                if (ones) {
-#pragma unroll
-                    for (int j = 1; j < NC; ++j) cmulf(xr, xi, cr[j], ci[j]);
+            // lanes of a problem's last item may own fewer positions and stop
+            // early; inner walks never synchronise across lanes
+            const int64_t my_R = (Q - r0 < R) ? (Q - r0) : R;
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+                typename Ar::acc_t acc = Ar::zero();
+                if ((seg & 1) == 0) {
+                    for (int t = 0; t < P; ++t) {
+                        const cs_t x = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(t) * NC, cm, ones);
+                        Ar::accumulate(acc, x, tab[t]);
+                    }
                 } else {
-                    for (int r = 1; r < cm[0]; ++r) cmulf(xr, xi, cr[0], ci[0]);
-#pragma unroll
-                    for (int j = 1; j < NC; ++j)
-                        for (int r = 0; r < cm[j]; ++r) cmulf(xr, xi, cr[j], ci[j]);
+                    for (int t = P - 1; t >= 0; --t) {
+                        const cs_t x = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(t) * NC, cm, ones);
+                        Ar::accumulate(acc, x, tab[t]);
+                    }
                 }
-            };
-
-            float ar, ai, er = 0.0f, ei = 0.0f;
-            product(ar, ai);
-            for (int t = 1; t < P; ++t) {
-                const float2 e = __ldg(reinterpret_cast<const float2 *>(tab + t));
-                const float w = e.x;
-                const float2 *d = D + __float_as_int(e.y);
+                Ar::fold(sr, si, acc, wout);
+                if (seg + 1 < my_R) {
+                    bool up = false;
+                    const int k = outer_next(pr, st, &up);
+                    const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
 #pragma unroll
-                for (int j = 0; j < NC; ++j) {
-                    const float2 v = __ldg(d + j);
-                    cr[j] = __fadd_rn(cr[j], v.x);
-                    ci[j] = __fadd_rn(ci[j], v.y);
-                }
-                float xr, xi;
-                product(xr, xi);
-                f_two_sum_acc(ar, er, __fmul_rn(w, xr));
-                f_two_sum_acc(ai, ei, __fmul_rn(w, xi));
-                if ((t & 127) == 0) {
-                    sr = dd_add_d(dd_add_d(sr, static_cast<double>(ar)), static_cast<double>(er));
-                    si = dd_add_d(dd_add_d(si, static_cast<double>(ai)), static_cast<double>(ei));
-                    ar = ai = er = ei = 0.0f;
+                    for (int j = 0; j < NC; ++j) Ar::update(seed[j], d[j]);
+                    wout = outer_weight(pr, st);
                 }
             }
-            sr = dd_add_d(dd_add_d(sr, static_cast<double>(ar)), static_cast<double>(er));
-            si = dd_add_d(dd_add_d(si, static_cast<double>(ai)), static_cast<double>(ei));
-            sr = dd_mul_d(sr, wout);
-            si = dd_mul_d(si, wout);
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {

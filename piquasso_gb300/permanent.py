@@ -111,8 +111,10 @@ def permanent(matrix, rows, cols):
     return np.array(complex(out[0], out[1]), dtype=np.complex128)
 
 
-def permanent_dd(matrix, rows, cols):
-    """complex128 permanent with its double-double low words: (value, low)."""
+def permanent_dd(matrix, rows, cols, mode="auto"):
+    """complex128 permanent with its double-double low words: (value, low).
+
+    ``mode``: "auto" (double-float where valid, else FP64), "fp64" or "df"."""
     m = _as_matrix(np.asarray(matrix, dtype=np.complex128))
     r = _as_mult(rows, m.shape[0], "rows")
     c = _as_mult(cols, m.shape[1], "cols")
@@ -120,7 +122,7 @@ def permanent_dd(matrix, rows, cols):
     lo = np.zeros(2)
     st = _lib.load().pqg_permanent_c128(
         _ptr(m, ctypes.c_double), m.shape[0], m.shape[1], _ptr(r, ctypes.c_int32),
-        _ptr(c, ctypes.c_int32), _lib.MODE_AUTO, _ptr(out, ctypes.c_double),
+        _ptr(c, ctypes.c_int32), _lib.MODES[mode], _ptr(out, ctypes.c_double),
         _ptr(lo, ctypes.c_double))
     if st:
         _raise_for(st)
@@ -152,13 +154,14 @@ def permanent_laplace(matrix, rows, cols):
     return (o[0::2] + 1j * o[1::2]).astype(np.complex64 if single else np.complex128)
 
 
-def permanent_batch(matrix, rows, cols):
+def permanent_batch(matrix, rows, cols, mode="auto"):
     """Permanents of one matrix for many multiplicity patterns at once.
 
     ``rows`` has shape (batch, n_rows) and ``cols`` shape (batch, n_cols) (or
     (n_cols,), shared by every pattern).  Returns a (batch,) array of the
     matrix's complex dtype.  One work queue, one walk launch and one
-    reduction serve the whole batch.
+    reduction serve the whole batch.  ``mode`` selects the complex128
+    arithmetic ("auto", "fp64" or "df").
     """
     m = _as_matrix(matrix)
     R = np.ascontiguousarray(np.asarray(rows).astype(np.int32, casting="unsafe"))
@@ -182,7 +185,7 @@ def permanent_batch(matrix, rows, cols):
         out = np.zeros(2 * batch, dtype=np.float64)
         st = L.pqg_permanent_batch_c128(_ptr(m, ctypes.c_double), m.shape[0], m.shape[1],
                                         _ptr(R, ctypes.c_int32), _ptr(C, ctypes.c_int32), batch,
-                                        _lib.MODE_AUTO, _ptr(out, ctypes.c_double))
+                                        _lib.MODES[mode], _ptr(out, ctypes.c_double))
         cdt = np.complex128
     if st:
         _raise_for(st)
