@@ -138,6 +138,30 @@ int pqg_measure_vector_peaks(double ms, double *out2);
 int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *flops, double *h2d_bytes,
                     double *d2h_bytes);
 
+/* Allocation-free permanent — no counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: applications whose own
+ * allocator has already reserved the GPU, latency-critical code that cannot
+ * afford an allocation's implicit synchronisation, code running while its
+ * stream is being recorded.  Computes the permanent of an n x n complex128
+ * matrix with every row and column taken once (rows = cols = 1) from DEVICE
+ * pointers: `d_matrix` (n*n interleaved re/im, row-major) and `d_out` (2
+ * doubles), enqueued on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream) and returning without waiting.  The FP64 walk is used.
+ *
+ * It allocates no device memory: all intermediate data lives in one
+ * file-scope device array of PQG_NOALLOC_SCRATCH_BYTES, held by every GPU that
+ * loads the library until the process exits.  The first call on a device looks
+ * that array's address up (cudaGetSymbolAddress) with the device current; make
+ * that first call before any stream capture.  Every call on a device shares
+ * the array, so calls whose executions overlap on the GPU (different streams,
+ * or threads) race and give wrong results: order them on one stream.
+ * n must be between 1 and PQG_NOALLOC_MAX_N; larger sizes are rejected with
+ * PQG_ERR_TOO_LARGE. */
+#define PQG_NOALLOC_MAX_N 32
+#define PQG_NOALLOC_SCRATCH_BYTES (4u << 20)
+int pqg_permanent_unit_c128_noalloc(const double *d_matrix, int64_t n, double *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,7 @@ SIGNATURES = {
     "pqg_plan_read": ([ctypes.c_void_p, ctypes.c_void_p, _i64], ctypes.c_int),
     "pqg_plan_info": ([ctypes.c_void_p, _d, _d, _i64, _i64], ctypes.c_int),
     "pqg_plan_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "pqg_permanent_unit_c128_noalloc": ([ctypes.c_void_p, _I64, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "pqg_set_tuning": ([_I64, _I64, _I64], ctypes.c_int),
     "pqg_get_tuning": ([_i64, _i64, _i64], ctypes.c_int),
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),

@@ -23,6 +23,7 @@ LIB = os.path.join(LIBDIR, "libpqperm_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = [
     "capi.cu",
+    "noalloc.cu",
     "k_plain_c128_0.cu",
     "k_plain_c128_1.cu",
     "k_plain_c64_0.cu",

@@ -517,6 +517,8 @@ int plan_build(Context &C, PlanHandle *h) {
 
 }  // namespace
 
+void set_last_error(const char *msg) { g_err = msg; }
+
 }  // namespace pqg
 
 using namespace pqg;
