@@ -587,6 +587,7 @@ int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) {
     PlanConfig d;
     C.cfg.items_per_smsp = items_per_smsp ? items_per_smsp : d.items_per_smsp;
     C.cfg.p_max = p_max ? p_max : d.p_max;
+    C.cfg.p_max_user = p_max != 0;
     C.cfg.seed_steps = seed_steps;
     return PQG_OK;
 }
@@ -635,8 +636,9 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     }
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
-    const Precision prec = dtype == 1 ? Precision::C64 : c128_precision(mode);
     const Form fm = form == 1 ? Form::LAPLACE : Form::PLAIN;
+    // the Laplace walk has FP64 and FP32 kernels only
+    const Precision prec = dtype == 1 ? Precision::C64 : (fm == Form::LAPLACE ? Precision::C128 : c128_precision(mode));
     PlanHandle *h = new PlanHandle();
     h->pl = Planner(prec, fm, C.cfg);
     h->single = dtype == 1;

@@ -314,7 +314,13 @@ void Planner::finish() {
                                                                                     : min_steps_per_seed(prec_)),
                                                S_tot / (32.0 * resident_warps));
     const double steps_per_lane = std::max({balance, seed_floor, 1.0});
-    const int64_t p_max = laplace ? std::min<int64_t>(cfg_.p_max, 512) : cfg_.p_max;
+    // longest inner walk: the problem's prefix table (P x nc elements) should
+    // stay resident in L1 next to the other warps' tables; the FP64 walk is
+    // bound by its arithmetic pipe and tolerates longer tables
+    int64_t p_cap = prec_ == Precision::C128 ? 512 : 256;
+    if (cfg_.p_max_user) p_cap = cfg_.p_max;
+    const int64_t p_max = laplace ? std::min<int64_t>(std::min<int64_t>(cfg_.p_max, p_cap), 512)
+                                  : std::min<int64_t>(cfg_.p_max, p_cap);
 
     for (size_t ip = 0; ip < np; ++ip) {
         PendingProblem &p = pending[ip];

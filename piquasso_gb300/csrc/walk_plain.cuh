@@ -35,6 +35,7 @@ struct ArF64 {
     };
     static constexpr bool kDfSeed = false;
     static constexpr bool kTwoChains = false;  // FP64-pipe bound: one chain
+    static constexpr bool kPairSteps = false;
     __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {r, i}; }
     __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r.hi, i.hi}; }
     __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
@@ -66,6 +67,7 @@ struct ArF32 {
     };
     static constexpr bool kDfSeed = true;
     static constexpr bool kTwoChains = true;
+    static constexpr bool kPairSteps = true;  // latency bound: two codes per iteration
     __device__ __forceinline__ static cs_t from_seed64(double r, double i) {
         return {__double2float_rn(r), __double2float_rn(i)};
     }
@@ -103,6 +105,7 @@ struct ArDF {
     };
     static constexpr bool kDfSeed = true;
     static constexpr bool kTwoChains = true;
+    static constexpr bool kPairSteps = false;  // enough independent work per code already
     __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {df_split(r), df_split(i)}; }
     __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r, i}; }
     __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
@@ -326,16 +329,25 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
             const int64_t my_R = (Q - r0 < R) ? (Q - r0) : R;
             for (int64_t seg = 0; seg < my_R; ++seg) {
                 typename Ar::acc_t acc = Ar::zero();
-                if ((seg & 1) == 0) {
-                    for (int t = 0; t < P; ++t) {
-                        const cs_t x = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(t) * NC, cm, ones);
-                        Ar::accumulate(acc, x, tab[t]);
+                // inner codes in walk order: t = s (forward) or P-1-s (backward);
+                // FP32-pipe walks take two codes per iteration (independent
+                // products, same accumulation order)
+                const bool back = (seg & 1) != 0;
+                int s = 0;
+                if constexpr (Ar::kPairSteps) {
+                    for (; s + 1 < P; s += 2) {
+                        const int ta = back ? P - 1 - s : s;
+                        const int tb = back ? ta - 1 : ta + 1;
+                        const cs_t xa = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(ta) * NC, cm, ones);
+                        const cs_t xb = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(tb) * NC, cm, ones);
+                        Ar::accumulate(acc, xa, tab[ta]);
+                        Ar::accumulate(acc, xb, tab[tb]);
                     }
-                } else {
-                    for (int t = P - 1; t >= 0; --t) {
-                        const cs_t x = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(t) * NC, cm, ones);
-                        Ar::accumulate(acc, x, tab[t]);
-                    }
+                }
+                for (; s < P; ++s) {
+                    const int t = back ? P - 1 - s : s;
+                    const cs_t x = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(t) * NC, cm, ones);
+                    Ar::accumulate(acc, x, tab[t]);
                 }
                 Ar::fold(sr, si, acc, wout);
                 if (seg + 1 < my_R) {
