@@ -209,6 +209,58 @@ def time_calls(pg_engine, torch, flush, U, ones, steps, mode):
     return dev, walk, e2e, tm, res
 
 
+def batch_workload():
+    """4096 output patterns drawn uniformly from the compositions of 20 photons
+    into 40 modes with at most 4 per mode; seeded 40x40 Haar unitary; one
+    photon in each of modes 0..19."""
+    from piquasso_gb300 import workloads
+
+    U = workloads.haar_unitary(40, 1)
+    inp = np.array([1] * 20 + [0] * 20)
+    pats = workloads.capped_compositions(20, 40, 4, 4096, seed=1)
+    return U, inp, pats
+
+
+def bench_batch(pg_engine, torch, flush, args, cpu=True):
+    """Batched probabilities: one plan, executed as one CUDA graph per step."""
+    U, inp, pats = batch_workload()
+    plan = pg_engine.PermanentPlan(U, pats, inp)
+    info = plan.info()
+    for _ in range(2):
+        plan.run()
+    ms = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        plan.launch()
+        ms.append(plan.synchronize())
+    vals = plan.read()
+    plan.close()
+    # end to end through the public batch call (planning and copies included)
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        v2 = pg_engine.permanent_batch(U, pats, inp)
+    e2e_s = (time.perf_counter() - t0) / reps
+    out = {"value": len(pats) / (statistics.mean(ms) / 1e3), "unit": "perm/s",
+           "graph_ms": statistics.mean(ms), "e2e": {"value": len(pats) / e2e_s, "unit": "perm/s"},
+           "gray_steps": info["steps"], "algorithmic_tflops": info["flops"] / (statistics.mean(ms) / 1e3) / 1e12,
+           "max_rel_diff_e2e_vs_graph": float(np.max(np.abs(v2 - vals) / np.abs(vals))),
+           "workload": "4096 uniform capped compositions (n=20, d=40, <= 4 per mode), seeded Haar(40), "
+                       "complex128 (double-float walk), one graph-captured launch"}
+    if cpu:
+        import oracle
+
+        k = 256
+        t0 = time.perf_counter()
+        for p in pats[:k]:
+            oracle.port_permanent(U, p, inp)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": k / dt, "unit": "perm/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": "first %d of the 4096 patterns, one reference-method call each" % k}
+    return out
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__
 
@@ -307,6 +359,8 @@ def run_ours(args, world, rank, local, pg):
                                   "achieved_tflops": F / w / 1e12, "peak_fp32_tflops": peaks["fp32_tflops"],
                                   "frac": F / w / 1e12 / peaks["fp32_tflops"],
                                   "rel_diff_vs_default": abs(complex(r32) - complex(result)) / abs(complex(result))}
+    if not args.no_variants:
+        line["batch_4096_d40_n20"] = bench_batch(pg_engine, torch, flush, args, cpu=(rank == 0 and not args.no_cpu_baseline))
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
         line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",

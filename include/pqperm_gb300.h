@@ -138,6 +138,47 @@ int pqg_measure_vector_peaks(double ms, double *out2);
 int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *flops, double *h2d_bytes,
                     double *d2h_bytes);
 
+/* Learned proposal (no counterpart in the reference): kernels of the
+ * autoregressive MLP over output occupations used as the independence
+ * proposal of the Metropolis boson sampler.  All pointers are DEVICE pointers;
+ * `stream` is a cudaStream_t (NULL: legacy default stream); the calls enqueue
+ * and return.
+ *
+ * pqg_mlp_gemm: C[M x N] = sum_k A(m,k) B(k,n) in BF16 tensor-core MMAs with
+ * FP32 accumulation; A(m,k) = a[m*a_s_row + k*a_s_col] (BF16 if a_bf16, else
+ * FP32, rounded to BF16 on load), likewise B.  epilogue 0: C = acc (FP32);
+ * 1: C = acc + bias (pre-activation), act_bf16 = GELU(C); 2: split-K over
+ * `splits` ranges of K through `splitk_scratch` (splits*M*N floats), then a
+ * fixed-order sum into C (weight gradients); 3: C = acc + bias.
+ * pqg_mlp_gelu_backward: d *= GELU'(pre).  pqg_mlp_bias_grad: db = column
+ * sums of d (M x N).  pqg_mlp_softmax_xent: per row m, softmax over classes
+ * lo[m]..hi[m] of logits (row stride ld), loss = -log p(target), dlogits =
+ * (p - onehot) * scale.  pqg_mlp_adam: one Adam step on FP32 weights (and
+ * their BF16 copy, nullable), bias-corrected with `step`. */
+int pqg_mlp_gemm(const void *a, int32_t a_bf16, int64_t a_s_row, int64_t a_s_col, const void *b, int32_t b_bf16,
+                 int64_t b_s_row, int64_t b_s_col, int64_t M, int64_t N, int64_t K, int32_t epilogue, float *c,
+                 void *act_bf16, const float *bias, float *splitk_scratch, int32_t splits, void *stream);
+int pqg_mlp_gelu_backward(float *d, const float *pre, int64_t n, void *stream);
+int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, void *stream);
+int pqg_mlp_softmax_xent(const float *logits, int64_t M, int32_t ld, int32_t classes, const int8_t *lo,
+                         const int8_t *hi, const int8_t *target, float scale, float *loss, float *dlogits,
+                         void *stream);
+int pqg_mlp_adam(float *w, void *w_bf16, const float *g, float *m1, float *m2, int64_t n, float lr, float b1,
+                 float b2, float eps, int64_t step, void *stream);
+
+/* Autoregressive proposal step for B chains at output mode j (d modes, n
+ * photons): pqg_proposal_features writes the 16 BF16 features of mode j and
+ * the feasible occupation range [lo, hi]; pqg_proposal_sample draws mode j's
+ * occupation from the masked softmax of `logits` (row stride 8) with a
+ * counter-based generator (seed, chain, j), adds its log-probability to logq,
+ * and updates samples, n_rem and the mean shifts of the later modes (C: d x d
+ * mode covariances; mode_stats: 8 floats per mode). */
+int pqg_proposal_features(int32_t j, int32_t B, int32_t d, int32_t n, const float *mode_stats, const int32_t *n_rem,
+                          const float *shift, void *X_bf16, int8_t *lo, int8_t *hi, void *stream);
+int pqg_proposal_sample(int32_t j, int32_t B, int32_t d, const float *logits, const int8_t *lo, const int8_t *hi,
+                        uint64_t seed, int8_t *samples, int32_t *n_rem, float *shift, const float *C,
+                        const float *mode_stats, float *logq, void *stream);
+
 /* Allocation-free permanent — no counterpart in the reference.
  *
  * For callers that cannot allocate device memory: applications whose own

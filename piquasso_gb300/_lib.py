@@ -29,6 +29,7 @@ _d = ctypes.POINTER(ctypes.c_double)
 _f = ctypes.POINTER(ctypes.c_float)
 _i32 = ctypes.POINTER(ctypes.c_int32)
 _i64 = ctypes.POINTER(ctypes.c_int64)
+_i8 = ctypes.POINTER(ctypes.c_int8)
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
 
@@ -52,6 +53,18 @@ SIGNATURES = {
     "pqg_plan_info": ([ctypes.c_void_p, _d, _d, _i64, _i64], ctypes.c_int),
     "pqg_plan_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "pqg_permanent_unit_c128_noalloc": ([ctypes.c_void_p, _I64, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_gemm": ([ctypes.c_void_p, _I32, _I64, _I64, ctypes.c_void_p, _I32, _I64, _I64, _I64, _I64, _I64,
+                      _I32, _f, ctypes.c_void_p, _f, _f, _I32, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_gelu_backward": ([_f, _f, _I64, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_bias_grad": ([_f, _I64, _I64, _f, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_softmax_xent": ([_f, _I64, _I32, _I32, _i8, _i8, _i8, ctypes.c_float, _f, _f, ctypes.c_void_p],
+                             ctypes.c_int),
+    "pqg_mlp_adam": ([_f, ctypes.c_void_p, _f, _f, _f, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                      ctypes.c_float, _I64, ctypes.c_void_p], ctypes.c_int),
+    "pqg_proposal_features": ([_I32, _I32, _I32, _I32, _f, _i32, _f, ctypes.c_void_p, _i8, _i8, ctypes.c_void_p],
+                              ctypes.c_int),
+    "pqg_proposal_sample": ([_I32, _I32, _I32, _f, _i8, _i8, ctypes.c_uint64, _i8, _i32, _f, _f, _f, _f,
+                             ctypes.c_void_p], ctypes.c_int),
     "pqg_set_tuning": ([_I64, _I64, _I64], ctypes.c_int),
     "pqg_get_tuning": ([_i64, _i64, _i64], ctypes.c_int),
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),

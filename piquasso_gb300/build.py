@@ -24,6 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = [
     "capi.cu",
     "noalloc.cu",
+    "mlp.cu",
+    "proposal.cu",
     "k_plain_c128_0.cu",
     "k_plain_c128_1.cu",
     "k_plain_c64_0.cu",

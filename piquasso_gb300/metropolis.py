@@ -1,0 +1,160 @@
+"""Independence Metropolis boson sampling with a learned proposal.
+
+B chains run in lock step.  Every step draws B proposals y from the
+autoregressive MLP (proposal.py) on the device — features, network and draw
+for one output mode at a time — together with their exact log q(y), and
+accepts y over the chain state x with probability
+
+    min(1, p(y) q(x) / (p(x) q(y))),   p(y) = |Per(U[y, in])|^2 / prod_i y_i!
+
+(the output probability of ideal boson sampling with single-photon inputs,
+as in the reference's passive/utils.py:131-138 and probabilities.py:26-54).
+The target probabilities come from ONE batched complex64 permanent launch per
+step (FP32 products with FP64-class seeds and double-double sums).  Patterns
+with a mode holding more than 4 photons cannot be proposed: the chain samples
+the target restricted to occupations <= 4, whose distance from the exact
+distribution the two-mode-marginal TVD against the exact marginals measures.
+
+`baseline=True` replaces the network by the exact one-mode marginals
+(logits log p_j(k)): the same sampler without the learned part.
+"""
+
+import ctypes
+import time
+from math import lgamma
+
+import numpy as np
+
+from . import _lib
+from .permanent import permanent_batch
+from .proposal import CAP, CLASSES, F, LD, ModeStats
+
+
+def _fp(t):
+    return ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))
+
+
+def _i8(t):
+    return ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_int8))
+
+
+def _i32(t):
+    return ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_int32))
+
+
+class ProposalSampler:
+    """Draws B patterns and their log q on the device."""
+
+    def __init__(self, mlp, stats: ModeStats, B, baseline=False, device="cuda"):
+        import torch
+
+        self.torch = torch
+        self.mlp = mlp
+        self.stats = stats
+        self.B = B
+        self.d = stats.d
+        self.n = stats.n
+        self.baseline = baseline
+        ms = np.zeros((self.d, 8), dtype=np.float32)
+        ms[:, :5] = stats.p
+        ms[:, 5] = stats.mu
+        ms[:, 6] = stats.var
+        ms[:, 7] = stats.mu_suffix[: self.d]
+        self.ms = torch.from_numpy(ms).to(device)
+        self.C = torch.from_numpy(stats.C.astype(np.float32)).to(device)
+        self.X = torch.zeros(B, F, dtype=torch.bfloat16, device=device)
+        self.lo = torch.zeros(B, dtype=torch.int8, device=device)
+        self.hi = torch.zeros(B, dtype=torch.int8, device=device)
+        self.samples = torch.zeros(B, self.d, dtype=torch.int8, device=device)
+        self.n_rem = torch.zeros(B, dtype=torch.int32, device=device)
+        self.shift = torch.zeros(B, self.d, dtype=torch.float32, device=device)
+        self.logq = torch.zeros(B, dtype=torch.float32, device=device)
+        if baseline:
+            lg = np.full((self.d, LD), -30.0, dtype=np.float32)
+            lg[:, :CLASSES] = np.log(np.maximum(stats.p, 1e-30))
+            self.base_logits = torch.from_numpy(lg).to(device)
+
+    def propose(self, seed):
+        L = _lib.load()
+        self.n_rem.fill_(self.n)
+        self.shift.zero_()
+        self.logq.zero_()
+        B, d, n = self.B, self.d, self.n
+        for j in range(d):
+            st = L.pqg_proposal_features(j, B, d, n, _fp(self.ms), _i32(self.n_rem), _fp(self.shift),
+                                         ctypes.c_void_p(self.X.data_ptr()), _i8(self.lo), _i8(self.hi), None)
+            if st:
+                raise RuntimeError(_lib.last_error())
+            if self.baseline:
+                logits = self.base_logits[j].expand(B, LD).contiguous()
+            else:
+                logits = self.mlp.forward(self.X)
+            st = L.pqg_proposal_sample(j, B, d, _fp(logits), _i8(self.lo), _i8(self.hi), ctypes.c_uint64(seed),
+                                       _i8(self.samples), _i32(self.n_rem), _fp(self.shift), _fp(self.C),
+                                       _fp(self.ms), _fp(self.logq), None)
+            if st:
+                raise RuntimeError(_lib.last_error())
+        return self.samples, self.logq
+
+
+def log_target(U64, patterns, inp):
+    """log p(y) = log |Per(U[y, in])|^2 - sum log y!  for every row of patterns."""
+    perms = permanent_batch(U64, patterns, inp)
+    lf = np.array([lgamma(k + 1.0) for k in range(int(np.max(patterns)) + 2)])
+    with np.errstate(divide="ignore"):
+        return 2.0 * np.log(np.abs(perms).astype(np.float64)) - lf[patterns].sum(axis=1)
+
+
+def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, seed=0, baseline=False,
+               record=True):
+    """Runs `chains` independent chains for `steps` steps; returns a dict with
+    the recorded states (after burn-in), acceptance rate and timings."""
+    import torch
+
+    inp = np.asarray(input_photons, dtype=int)
+    U = np.asarray(U, dtype=np.complex128)
+    U64 = U.astype(np.complex64)
+    stats = ModeStats(U, inp)
+    sampler = ProposalSampler(mlp, stats, chains, baseline=baseline)
+    rng = np.random.default_rng(seed)
+    t0 = time.perf_counter()
+    y, lq = sampler.propose(seed * 1000003 + 1)
+    x = y.cpu().numpy().astype(np.int64)
+    logq_x = lq.cpu().numpy().astype(np.float64)
+    logp_x = log_target(U64, x, inp)
+    accepted = 0
+    proposals = 0
+    kept = []
+    t_prop = t_perm = 0.0
+    for step in range(steps):
+        ta = time.perf_counter()
+        y_d, lq_d = sampler.propose(seed * 1000003 + 2 + step)
+        y = y_d.cpu().numpy().astype(np.int64)
+        logq_y = lq_d.cpu().numpy().astype(np.float64)
+        tb = time.perf_counter()
+        logp_y = log_target(U64, y, inp)
+        tc = time.perf_counter()
+        t_prop += tb - ta
+        t_perm += tc - tb
+        log_alpha = (logp_y - logp_x) - (logq_y - logq_x)
+        acc = np.log(rng.random(chains)) < log_alpha
+        x[acc] = y[acc]
+        logp_x[acc] = logp_y[acc]
+        logq_x[acc] = logq_y[acc]
+        accepted += int(acc.sum())
+        proposals += chains
+        if record and step >= burn_in:
+            kept.append(x.copy())
+    torch.cuda.synchronize()
+    total = time.perf_counter() - t0
+    out = {
+        "acceptance": accepted / max(1, proposals),
+        "chain_steps": proposals,
+        "seconds": total,
+        "samples_per_s": proposals / total,
+        "propose_s": t_prop,
+        "target_s": t_perm,
+    }
+    if record:
+        out["samples"] = np.concatenate(kept) if kept else np.zeros((0, len(inp)), dtype=np.int64)
+    return out

@@ -1,0 +1,231 @@
+"""Learned proposal for Metropolis boson sampling: an autoregressive MLP over
+output occupations.
+
+The model walks the output modes j = 0..d-1 in order and predicts the
+occupation s_j in {0, ..., 4} from a fixed-size feature vector of mode j and
+of the occupations already chosen, so one network serves any (n, d).  It is
+trained by maximum likelihood on exact samples, and its log-probability
+log q(s) = sum_j log softmax_j(s_j) is exact (every step is a normalised,
+masked softmax), as an independence Metropolis proposal requires.
+
+Per-mode inputs, computed once per interferometer from the exact one- and
+two-mode statistics of the output (binomial moments, see marginals.py):
+  * p_j(k): the exact one-mode marginal Pr(X_j = k), k = 0..4;
+  * mu_j = E[X_j], var_j = Var[X_j];
+  * C_kj = Cov(X_k, X_j) = |T_kj|^2 - 2 Q_kj for single-photon inputs, with
+    T_kj = sum_a U_ka conj(U_ja) and Q_kj = sum_a |U_ka|^2 |U_ja|^2 over the
+    occupied input modes a (the z_k z_j w_k w_j coefficient of the generating
+    function of marginals.py).
+Per-step state: photons left, modes left, and the linear-regression shift of
+mode j's mean given the chosen occupations, sum_{k<j} C_kj (s_k - mu_k)/var_k.
+
+Network: F = 16 features -> 256 -> 256 -> 256 -> 8 logits (GELU, BF16
+weights and activations, FP32 accumulation and master weights), of which the
+first 5 are the occupations; classes that cannot complete a pattern (more
+photons than are left, or too few to fill the remaining modes with at most 4
+each) are masked.  The GEMMs, GELU backward, masked softmax cross-entropy and
+Adam run as this package's CUDA kernels (pqg_mlp_* in the C ABI); PyTorch
+only holds the device buffers.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .marginals import marginal
+
+F = 16          # features per (sample, mode)
+HIDDEN = 256
+CLASSES = 5     # occupations 0..4
+LD = 8          # padded logit width
+CAP = 4
+
+
+class ModeStats:
+    """Per-interferometer statistics feeding the features (single-photon inputs
+    or general inputs for p_j and mu_j; C uses the single-photon formula)."""
+
+    def __init__(self, U, input_photons):
+        U = np.asarray(U, dtype=np.complex128)
+        inp = np.asarray(input_photons, dtype=int)
+        self.d = len(inp)
+        self.n = int(inp.sum())
+        act = np.nonzero(inp)[0]
+        W = U[:, act]                        # U[output j, input a]
+        P = np.abs(W) ** 2 * inp[act][None, :]
+        self.mu = P.sum(axis=1)              # E[X_j]
+        self.p = np.zeros((self.d, CLASSES))
+        self.var = np.zeros(self.d)
+        for j in range(self.d):
+            m = marginal(inp, U, (j,))
+            self.p[j] = m[:CLASSES]
+            k = np.arange(len(m))
+            self.var[j] = float((m * k * k).sum() - (m * k).sum() ** 2)
+        self.var = np.maximum(self.var, 1e-6)
+        T = W @ W.conj().T                   # T_kj = sum_a U_ka conj(U_ja)
+        Q = (np.abs(W) ** 2) @ (np.abs(W) ** 2).T
+        self.C = np.abs(T) ** 2 - 2.0 * Q
+        np.fill_diagonal(self.C, 0.0)
+        self.mu_suffix = np.concatenate([np.cumsum(self.mu[::-1])[::-1], [0.0]])
+
+
+def features(stats, samples):
+    """Training features for every (sample, mode): array (S, d, F) float32,
+    plus the class masks lo/hi (S, d) int8 and targets (S, d) int8."""
+    S = np.asarray(samples, dtype=np.int64)
+    ns, d = S.shape
+    n = stats.n
+    used = np.concatenate([np.zeros((ns, 1), dtype=np.int64), np.cumsum(S, axis=1)[:, :-1]], axis=1)
+    n_rem = n - used                                     # photons left before mode j
+    j = np.arange(d)[None, :]
+    left = d - j                                         # modes left including j
+    z = (S - stats.mu[None, :]) / stats.var[None, :]
+    shift = z @ np.triu(stats.C, 1)                      # sum_{k<j} C_kj z_k
+    X = np.zeros((ns, d, F), dtype=np.float32)
+    X[..., 0] = 1.0
+    X[..., 1] = n_rem / n
+    X[..., 2] = left / d
+    X[..., 3] = n_rem / left
+    X[..., 4:9] = stats.p[None, :, :]
+    X[..., 9] = stats.mu[None, :]
+    X[..., 10] = (n_rem - stats.mu_suffix[None, :d]) / np.sqrt(n)
+    X[..., 11] = shift
+    X[..., 12] = stats.mu[None, :] + shift
+    X[..., 13] = n_rem * stats.mu[None, :] / np.maximum(stats.mu_suffix[None, :d], 1e-12)
+    X[..., 14] = stats.var[None, :]
+    lo = np.maximum(0, n_rem - CAP * (left - 1)).astype(np.int8)
+    hi = np.minimum(CAP, n_rem).astype(np.int8)
+    return X, lo, hi, S.astype(np.int8)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class MLP:
+    """Weights and the forward/backward passes on the engine's BF16 kernels."""
+
+    def __init__(self, seed=0, device="cuda"):
+        import torch
+
+        self.torch = torch
+        g = torch.Generator().manual_seed(seed)
+        dims = [(F, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, LD)]
+        self.W, self.Wb, self.b, self.mW, self.vW, self.mb, self.vb = [], [], [], [], [], [], []
+        for (fi, fo) in dims:
+            w = torch.randn(fi, fo, generator=g) * (2.0 / fi) ** 0.5
+            if fo == LD:
+                w *= 0.1
+            w = w.to(device)
+            self.W.append(w)
+            self.Wb.append(w.to(torch.bfloat16))
+            self.b.append(torch.zeros(fo, device=device))
+            self.mW.append(torch.zeros_like(w))
+            self.vW.append(torch.zeros_like(w))
+            self.mb.append(torch.zeros(fo, device=device))
+            self.vb.append(torch.zeros(fo, device=device))
+        self.step = 0
+        self.device = device
+
+    def state_dict(self):
+        return {"W": [w.cpu().numpy() for w in self.W], "b": [b.cpu().numpy() for b in self.b], "step": self.step}
+
+    def load_state_dict(self, sd):
+        torch = self.torch
+        for i in range(4):
+            self.W[i] = torch.from_numpy(np.asarray(sd["W"][i], dtype=np.float32)).to(self.device)
+            self.Wb[i] = self.W[i].to(torch.bfloat16)
+            self.b[i] = torch.from_numpy(np.asarray(sd["b"][i], dtype=np.float32)).to(self.device)
+        self.step = int(sd.get("step", 0))
+
+    # ---------------------------------------------------------------- kernels
+    def _gemm(self, A, A_bf16, a_rows, a_cols, B, B_bf16, b_rows, b_cols, M, N, K, epi, C,
+              act=None, bias=None, scratch=None, splits=0, stream=None):
+        L = _lib.load()
+        st = L.pqg_mlp_gemm(_ptr(A), int(A_bf16), a_rows, a_cols, _ptr(B), int(B_bf16), b_rows, b_cols,
+                            M, N, K, epi, ctypes.cast(C.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                            _ptr(act) if act is not None else None,
+                            ctypes.cast(bias.data_ptr(), ctypes.POINTER(ctypes.c_float)) if bias is not None else None,
+                            ctypes.cast(scratch.data_ptr(), ctypes.POINTER(ctypes.c_float)) if scratch is not None else None,
+                            int(splits), stream)
+        if st:
+            raise RuntimeError("pqg_mlp_gemm failed: " + _lib.last_error())
+
+    def forward(self, Xb, keep=False):
+        """Xb: (M, F) bf16 -> logits (M, LD) fp32 (+ activations if keep)."""
+        torch = self.torch
+        M = Xb.shape[0]
+        acts = [Xb]
+        pres = []
+        h = Xb
+        for i in range(3):
+            pre = torch.empty(M, HIDDEN, device=self.device, dtype=torch.float32)
+            act = torch.empty(M, HIDDEN, device=self.device, dtype=torch.bfloat16)
+            fi = h.shape[1]
+            self._gemm(h, 1, fi, 1, self.Wb[i], 1, HIDDEN, 1, M, HIDDEN, fi, 1, pre, act=act, bias=self.b[i])
+            pres.append(pre)
+            acts.append(act)
+            h = act
+        logits = torch.empty(M, LD, device=self.device, dtype=torch.float32)
+        self._gemm(h, 1, HIDDEN, 1, self.Wb[3], 1, LD, 1, M, LD, HIDDEN, 3, logits, bias=self.b[3])
+        if keep:
+            return logits, acts, pres
+        return logits
+
+    def loss_and_grads(self, Xb, lo, hi, target):
+        """Mean masked cross-entropy (nats per mode) and weight gradients."""
+        torch = self.torch
+        L = _lib.load()
+        M = Xb.shape[0]
+        logits, acts, pres = self.forward(Xb, keep=True)
+        loss = torch.empty(M, device=self.device, dtype=torch.float32)
+        dz = torch.empty(M, LD, device=self.device, dtype=torch.float32)
+        st = L.pqg_mlp_softmax_xent(ctypes.cast(logits.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, LD, CLASSES,
+                                    ctypes.cast(lo.data_ptr(), ctypes.POINTER(ctypes.c_int8)),
+                                    ctypes.cast(hi.data_ptr(), ctypes.POINTER(ctypes.c_int8)),
+                                    ctypes.cast(target.data_ptr(), ctypes.POINTER(ctypes.c_int8)), 1.0 / M,
+                                    ctypes.cast(loss.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                                    ctypes.cast(dz.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
+        if st:
+            raise RuntimeError(_lib.last_error())
+        grads_W, grads_b = [None] * 4, [None] * 4
+        splits = max(1, min(64, M // 4096))
+        d_out = dz
+        for i in (3, 2, 1, 0):
+            fi, fo = self.W[i].shape
+            h_in = acts[i]
+            # dW = h_in^T d_out  (K = M, split over the batch)
+            gW = torch.empty(fi, fo, device=self.device, dtype=torch.float32)
+            scratch = torch.empty(splits * fi * fo, device=self.device, dtype=torch.float32)
+            self._gemm(h_in, 1, 1, fi, d_out, 0, fo, 1, fi, fo, M, 2, gW, scratch=scratch, splits=splits)
+            gb = torch.empty(fo, device=self.device, dtype=torch.float32)
+            st = L.pqg_mlp_bias_grad(ctypes.cast(d_out.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, fo,
+                                     ctypes.cast(gb.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
+            if st:
+                raise RuntimeError(_lib.last_error())
+            grads_W[i], grads_b[i] = gW, gb
+            if i == 0:
+                break
+            # d h_in = d_out W^T, then through GELU'(pre)
+            dh = torch.empty(M, fi, device=self.device, dtype=torch.float32)
+            self._gemm(d_out, 0, fo, 1, self.Wb[i], 1, 1, fo, M, fi, fo, 0, dh)
+            st = L.pqg_mlp_gelu_backward(ctypes.cast(dh.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                                         ctypes.cast(pres[i - 1].data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                                         dh.numel(), None)
+            if st:
+                raise RuntimeError(_lib.last_error())
+            d_out = dh
+        return loss, grads_W, grads_b
+
+    def adam(self, grads_W, grads_b, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        L = _lib.load()
+        self.step += 1
+        fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))  # noqa: E731
+        for i in range(4):
+            st = L.pqg_mlp_adam(fp(self.W[i]), _ptr(self.Wb[i]), fp(grads_W[i]), fp(self.mW[i]), fp(self.vW[i]),
+                                self.W[i].numel(), lr, b1, b2, eps, self.step, None)
+            st |= L.pqg_mlp_adam(fp(self.b[i]), None, fp(grads_b[i]), fp(self.mb[i]), fp(self.vb[i]),
+                                 self.b[i].numel(), lr, b1, b2, eps, self.step, None)
+            if st:
+                raise RuntimeError(_lib.last_error())

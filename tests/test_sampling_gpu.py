@@ -52,3 +52,20 @@ def test_laplace_batch_matches_oracle(engine, dtype):
         nz = C[b] > 0
         rt = 1e-4 if dtype == np.complex64 else 1e-10
         assert np.allclose(got[b][nz], want[nz], rtol=rt, atol=rt * 1e-3), b
+
+
+def test_batched_sampler_matches_exact_marginals(engine):
+    """The throughput sampler draws from the exact distribution: its one- and
+    two-mode marginals agree with the binomial-moment marginals to within the
+    sampling noise of 20000 samples."""
+    from piquasso_gb300 import marginals, sampling
+
+    d, n = 8, 4
+    U = haar_unitary(d, 31)
+    inp = [1] * n + [0] * (d - n)
+    S = sampling.generate_samples_batched(inp, 20000, U, seed=5)
+    assert S.shape == (20000, d) and np.all(S.sum(axis=1) == n)
+    tv2 = marginals.tvd_two_mode(S, inp, U, [(0, 1), (2, 7), (5, 6)])
+    tv1 = marginals.tvd_one_mode(S, inp, U, range(d))
+    assert np.all(tv2 < 0.02), tv2
+    assert np.all(tv1 < 0.015), tv1
