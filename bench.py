@@ -261,6 +261,42 @@ def bench_batch(pg_engine, torch, flush, args, cpu=True):
     return out
 
 
+def bench_sampling(args):
+    """Boson sampling at n=24 photons in d=48 modes (seeded Haar(48), seed 3,
+    one photon in each of modes 0..23): the exact GPU sampler against the
+    learned-proposal Metropolis sampler (1024 chains, the shipped network) and
+    the same Metropolis sampler without the network; two-mode-marginal TVD
+    against the exact marginals on 16 random mode pairs."""
+    import os as _os
+
+    from piquasso_gb300 import marginals, metropolis, proposal, sampling, workloads
+
+    U = workloads.haar_unitary(48, 3)
+    inp = np.array([1] * 24 + [0] * 24)
+    out = {"workload": "n=24, d=48, Haar(48) seed 3, inputs in modes 0..23; complex64 permanents"}
+    res = {}
+    have = _os.path.exists(proposal.DEFAULT_WEIGHTS)
+    mlp = proposal.load_mlp() if have else None
+    runs = (("metropolis_learned", dict(mlp=mlp)),) if have else ()
+    runs += (("metropolis_no_network", dict(baseline=True)),)
+    pairs = None
+    for name, kw in runs:
+        r = metropolis.evaluate(U, inp, chains=1024, steps=args.mcmc_steps, burn_in=30, seed=4, **kw)
+        pairs = [tuple(p) for p in r.pop("pairs")]
+        res[name] = r
+    tm = {}
+    S = sampling.generate_samples_batched(inp, args.exact_samples, U.astype(np.complex64), 21, batch_size=4096,
+                                          timings=tm)
+    tv = marginals.tvd_two_mode(S, inp, U, pairs)
+    res["exact"] = {"samples_per_s": args.exact_samples / tm["total_s"], "tvd_mean": float(tv.mean()),
+                    "tvd_max": float(tv.max()), "samples": args.exact_samples, **tm}
+    for name in res:
+        if name != "exact":
+            res[name]["speedup_vs_exact"] = res[name]["samples_per_s"] / res["exact"]["samples_per_s"]
+    out.update(res)
+    return out
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__
 
@@ -361,6 +397,8 @@ def run_ours(args, world, rank, local, pg):
                                   "rel_diff_vs_default": abs(complex(r32) - complex(result)) / abs(complex(result))}
     if not args.no_variants:
         line["batch_4096_d40_n20"] = bench_batch(pg_engine, torch, flush, args, cpu=(rank == 0 and not args.no_cpu_baseline))
+    if not args.no_variants and not args.no_sampling:
+        line["sampling_n24_d48"] = bench_sampling(args)
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
         line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",
@@ -381,6 +419,9 @@ def main():
     ap.add_argument("--cpu-reps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-sampling", action="store_true")
+    ap.add_argument("--mcmc-steps", type=int, default=330)
+    ap.add_argument("--exact-samples", type=int, default=32768)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

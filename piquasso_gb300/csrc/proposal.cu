@@ -3,8 +3,8 @@
 // masked-softmax draw of the occupation of mode j with the bookkeeping of the
 // chain state.  The features match piquasso_gb300/proposal.py:features().
 //
-// Per-mode statistics `ms` (8 floats per mode): p(0..4), mu, var, and the
-// suffix sum of mu from mode j on.  Chain state: photons left `n_rem`, the
+// Per-mode statistics `ms` (12 floats per mode): p(0..4), the tail
+// Pr(X >= 5), mu, var, the suffix sum of mu from mode j on, 3 pad.  Chain state: photons left `n_rem`, the
 // running mean shift of every later mode `shift` (B x d), the pattern
 // `samples` (B x d, int8) and log q (B).
 #include <cuda_bf16.h>
@@ -20,7 +20,7 @@ void set_last_error(const char *msg);
 
 namespace {
 
-constexpr int kF = 16, kLD = 8, kCap = 4;
+constexpr int kF = 16, kLD = 8, kCap = 7, kMS = 12;
 
 __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     // SplitMix64 finaliser (Steele, Lea, Flood, "Fast splittable pseudorandom
@@ -41,7 +41,7 @@ __global__ void features_kernel(int j, int B, int d, int n, const float *__restr
                                 __nv_bfloat16 *__restrict__ X, int8_t *__restrict__ lo, int8_t *__restrict__ hi) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
-    const float *s = ms + 8 * j;
+    const float *s = ms + kMS * j;
     const int nr = n_rem[b];
     const int left = d - j;
     const float sh = shift[static_cast<int64_t>(b) * d + j];
@@ -51,13 +51,13 @@ __global__ void features_kernel(int j, int B, int d, int n, const float *__restr
     x[2] = static_cast<float>(left) / d;
     x[3] = static_cast<float>(nr) / left;
     for (int k = 0; k < 5; ++k) x[4 + k] = s[k];
-    x[9] = s[5];
-    x[10] = (nr - s[7]) / sqrtf(static_cast<float>(n));
+    x[9] = s[6];
+    x[10] = (nr - s[8]) / sqrtf(static_cast<float>(n));
     x[11] = sh;
-    x[12] = s[5] + sh;
-    x[13] = nr * s[5] / fmaxf(s[7], 1e-12f);
-    x[14] = s[6];
-    x[15] = 0.0f;
+    x[12] = s[6] + sh;
+    x[13] = nr * s[6] / fmaxf(s[8], 1e-12f);
+    x[14] = s[7];
+    x[15] = s[5];
     for (int k = 0; k < kF; ++k) X[static_cast<int64_t>(b) * kF + k] = __float2bfloat16(x[k]);
     const int l = nr - kCap * (left - 1);
     lo[b] = static_cast<int8_t>(l > 0 ? l : 0);
@@ -89,7 +89,7 @@ __global__ void sample_kernel(int j, int B, int d, const float *__restrict__ log
     logq[b] += (z[pick] - mx) - logf(tot);
     samples[static_cast<int64_t>(b) * d + j] = static_cast<int8_t>(pick);
     n_rem[b] -= pick;
-    const float dz = (pick - ms[8 * j + 5]) / ms[8 * j + 6];
+    const float dz = (pick - ms[kMS * j + 6]) / ms[kMS * j + 7];
     float *sh = shift + static_cast<int64_t>(b) * d;
     const float *cj = C + static_cast<int64_t>(j) * d;
     for (int k = j + 1; k < d; ++k) sh[k] += cj[k] * dz;

@@ -113,7 +113,7 @@ struct ArDF {
         c.i = df_add(c.i, dfl{d.z, d.w});
     }
     __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
-        return {df_add(c.r, dfl{d.x, d.y}), df_add(c.i, dfl{d.z, d.w})};
+        return {df_add_lazy(c.r, dfl{d.x, d.y}), df_add_lazy(c.i, dfl{d.z, d.w})};
     }
     __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { df_cmul(x.r, x.i, y.r, y.i); }
     __device__ __forceinline__ static acc_t zero() { return {{0.0f, 0.0f}, {0.0f, 0.0f}}; }

@@ -11,8 +11,8 @@ accepts y over the chain state x with probability
 as in the reference's passive/utils.py:131-138 and probabilities.py:26-54).
 The target probabilities come from ONE batched complex64 permanent launch per
 step (FP32 products with FP64-class seeds and double-double sums).  Patterns
-with a mode holding more than 4 photons cannot be proposed: the chain samples
-the target restricted to occupations <= 4, whose distance from the exact
+with a mode holding more than 7 photons cannot be proposed: the chain samples
+the target restricted to occupations <= 7, whose distance from the exact
 distribution the two-mode-marginal TVD against the exact marginals measures.
 
 `baseline=True` replaces the network by the exact one-mode marginals
@@ -55,11 +55,12 @@ class ProposalSampler:
         self.d = stats.d
         self.n = stats.n
         self.baseline = baseline
-        ms = np.zeros((self.d, 8), dtype=np.float32)
+        ms = np.zeros((self.d, 12), dtype=np.float32)
         ms[:, :5] = stats.p
-        ms[:, 5] = stats.mu
-        ms[:, 6] = stats.var
-        ms[:, 7] = stats.mu_suffix[: self.d]
+        ms[:, 5] = stats.tail
+        ms[:, 6] = stats.mu
+        ms[:, 7] = stats.var
+        ms[:, 8] = stats.mu_suffix[: self.d]
         self.ms = torch.from_numpy(ms).to(device)
         self.C = torch.from_numpy(stats.C.astype(np.float32)).to(device)
         self.X = torch.zeros(B, F, dtype=torch.bfloat16, device=device)
@@ -70,8 +71,10 @@ class ProposalSampler:
         self.shift = torch.zeros(B, self.d, dtype=torch.float32, device=device)
         self.logq = torch.zeros(B, dtype=torch.float32, device=device)
         if baseline:
-            lg = np.full((self.d, LD), -30.0, dtype=np.float32)
-            lg[:, :CLASSES] = np.log(np.maximum(stats.p, 1e-30))
+            # exact one-mode marginals; the tail mass spread over occupations 5..7
+            lg = np.zeros((self.d, LD), dtype=np.float32)
+            lg[:, :5] = np.log(np.maximum(stats.p, 1e-30))
+            lg[:, 5:] = np.log(np.maximum(stats.tail / 3.0, 1e-30))[:, None]
             self.base_logits = torch.from_numpy(lg).to(device)
 
     def propose(self, seed):
@@ -157,4 +160,23 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
     }
     if record:
         out["samples"] = np.concatenate(kept) if kept else np.zeros((0, len(inp)), dtype=np.int64)
+    return out
+
+
+def evaluate(U, input_photons, mlp=None, chains=1024, steps=300, burn_in=30, seed=0, baseline=False, pairs=None,
+             pair_seed=0, n_pairs=16):
+    """Samples/s, acceptance and two-mode-marginal TVD (mean and max over
+    `pairs`, default `n_pairs` random mode pairs) of one Metropolis run."""
+    from .marginals import tvd_two_mode
+
+    d = len(input_photons)
+    if pairs is None:
+        rng = np.random.default_rng(pair_seed)
+        allp = [(a, b) for a in range(d) for b in range(a + 1, d)]
+        pairs = [allp[i] for i in rng.choice(len(allp), size=min(n_pairs, len(allp)), replace=False)]
+    out = run_chains(U, input_photons, mlp=mlp, chains=chains, steps=steps, burn_in=burn_in, seed=seed,
+                     baseline=baseline)
+    tv = tvd_two_mode(out.pop("samples"), input_photons, U, pairs)
+    out.update({"tvd_mean": float(tv.mean()), "tvd_max": float(tv.max()), "pairs": [list(p) for p in pairs],
+                "kept_samples": chains * max(0, steps - burn_in)})
     return out

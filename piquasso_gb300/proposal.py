@@ -2,7 +2,7 @@
 output occupations.
 
 The model walks the output modes j = 0..d-1 in order and predicts the
-occupation s_j in {0, ..., 4} from a fixed-size feature vector of mode j and
+occupation s_j in {0, ..., 7} from a fixed-size feature vector of mode j and
 of the occupations already chosen, so one network serves any (n, d).  It is
 trained by maximum likelihood on exact samples, and its log-probability
 log q(s) = sum_j log softmax_j(s_j) is exact (every step is a normalised,
@@ -10,7 +10,8 @@ masked softmax), as an independence Metropolis proposal requires.
 
 Per-mode inputs, computed once per interferometer from the exact one- and
 two-mode statistics of the output (binomial moments, see marginals.py):
-  * p_j(k): the exact one-mode marginal Pr(X_j = k), k = 0..4;
+  * p_j(k): the exact one-mode marginal Pr(X_j = k), k = 0..4, and the
+    tail Pr(X_j >= 5);
   * mu_j = E[X_j], var_j = Var[X_j];
   * C_kj = Cov(X_k, X_j) = |T_kj|^2 - 2 Q_kj for single-photon inputs, with
     T_kj = sum_a U_ka conj(U_ja) and Q_kj = sum_a |U_ka|^2 |U_ja|^2 over the
@@ -20,10 +21,13 @@ Per-step state: photons left, modes left, and the linear-regression shift of
 mode j's mean given the chosen occupations, sum_{k<j} C_kj (s_k - mu_k)/var_k.
 
 Network: F = 16 features -> 256 -> 256 -> 256 -> 8 logits (GELU, BF16
-weights and activations, FP32 accumulation and master weights), of which the
-first 5 are the occupations; classes that cannot complete a pattern (more
-photons than are left, or too few to fill the remaining modes with at most 4
-each) are masked.  The GEMMs, GELU backward, masked softmax cross-entropy and
+weights and activations, FP32 accumulation and master weights), one per
+occupation 0..7; classes that cannot complete a pattern (more photons than are
+left, or too few to fill the remaining modes with at most 7 each) are masked.
+Occupations above 7 have no support: at n=24, d=48 their exact probability is
+about 1e-5 per mode, so the chain's target differs from the exact distribution
+by well under the sampling noise.  (A softmax over 0..4 alone would leave about
+13 % of the exact mass at n=24, d=48 unreachable.)  The GEMMs, GELU backward, masked softmax cross-entropy and
 Adam run as this package's CUDA kernels (pqg_mlp_* in the C ABI); PyTorch
 only holds the device buffers.
 """
@@ -37,9 +41,9 @@ from .marginals import marginal
 
 F = 16          # features per (sample, mode)
 HIDDEN = 256
-CLASSES = 5     # occupations 0..4
-LD = 8          # padded logit width
-CAP = 4
+CLASSES = 8     # occupations 0..7
+LD = 8          # logit width
+CAP = 7
 
 
 class ModeStats:
@@ -55,11 +59,13 @@ class ModeStats:
         W = U[:, act]                        # U[output j, input a]
         P = np.abs(W) ** 2 * inp[act][None, :]
         self.mu = P.sum(axis=1)              # E[X_j]
-        self.p = np.zeros((self.d, CLASSES))
+        self.p = np.zeros((self.d, 5))
+        self.tail = np.zeros(self.d)
         self.var = np.zeros(self.d)
         for j in range(self.d):
             m = marginal(inp, U, (j,))
-            self.p[j] = m[:CLASSES]
+            self.p[j] = m[:5]
+            self.tail[j] = max(0.0, 1.0 - float(m[:5].sum()))
             k = np.arange(len(m))
             self.var[j] = float((m * k * k).sum() - (m * k).sum() ** 2)
         self.var = np.maximum(self.var, 1e-6)
@@ -94,6 +100,7 @@ def features(stats, samples):
     X[..., 12] = stats.mu[None, :] + shift
     X[..., 13] = n_rem * stats.mu[None, :] / np.maximum(stats.mu_suffix[None, :d], 1e-12)
     X[..., 14] = stats.var[None, :]
+    X[..., 15] = stats.tail[None, :]
     lo = np.maximum(0, n_rem - CAP * (left - 1)).astype(np.int8)
     hi = np.minimum(CAP, n_rem).astype(np.int8)
     return X, lo, hi, S.astype(np.int8)
@@ -229,3 +236,16 @@ class MLP:
                                  self.b[i].numel(), lr, b1, b2, eps, self.step, None)
             if st:
                 raise RuntimeError(_lib.last_error())
+
+
+DEFAULT_WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__file__), "data", "proposal_weights.npz")
+
+
+def load_mlp(path=None, device="cuda"):
+    """The trained network (default: the weights shipped with the package,
+    produced by `python -m piquasso_gb300.train`)."""
+    z = np.load(path or DEFAULT_WEIGHTS)
+    mlp = MLP(seed=0, device=device)
+    mlp.load_state_dict({"W": [z["W%d" % i] for i in range(4)], "b": [z["b%d" % i] for i in range(4)],
+                         "step": int(z["step"]) if "step" in z else 0})
+    return mlp

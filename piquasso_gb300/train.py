@@ -35,7 +35,7 @@ def build_dataset(ns=(12, 13, 14, 15, 16), unitaries=4, samples_per_unitary=4096
                                                   batch_size=samples_per_unitary)
             stats = proposal.ModeStats(U, inp)
             X, lo, hi, tgt = proposal.features(stats, S)
-            keep = S.max(axis=1) <= proposal.CAP  # the proposal's support: occupations <= 4
+            keep = S.max(axis=1) <= proposal.CAP  # the proposal's support: occupations <= CAP
             Xs.append(X[keep].reshape(-1, proposal.F))
             los.append(lo[keep].reshape(-1))
             his.append(hi[keep].reshape(-1))
