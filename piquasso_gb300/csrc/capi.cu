@@ -1,10 +1,12 @@
 // C ABI of the GB300 permanent engine (declared in include/pqperm_gb300.h).
 //
-// Host side of every call: plan on the host (plan.cpp), one H2D copy of the
-// plan, then on one stream: zero the work-queue head, the persistent walk
-// kernel, the level-1 and level-2 double-double reductions, one D2H copy of
-// the results.  Device and pinned host buffers are cached per process and
-// grow on demand.
+// Host side of every call: plan on the host (plan.cpp: problem descriptors,
+// weight tables and the matrix, no per-problem matrix data), one H2D copy of
+// the plan, then on one stream: the prep kernel that builds every problem's
+// seeds, step rows and prefix tables from the matrix (prep.cuh), zero the
+// work-queue head, the persistent walk kernel, the level-1 and level-2
+// double-double reductions, one D2H copy of the results.  Device and pinned
+// host buffers are cached per process and grow on demand.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -19,7 +21,7 @@
 #include "../../include/pqperm_gb300.h"
 #include "kernel_table.h"
 #include "plan.hpp"
-#include "delta.cuh"
+#include "prep.cuh"
 #include "reduce.cuh"
 
 namespace pqg {
@@ -140,11 +142,13 @@ const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, int *which)
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Byte layout of a packed plan (problems | item_begin | chunks | arena) and of
-// its outputs (values in the output type, then the low words in FP64).
+// Byte layout of a packed plan (problems | item_begin | chunks | arena, the
+// uploaded `total` bytes, then the device-built per-problem data up to
+// `dev_total`) and of its outputs (values in the output type, then the low
+// words in FP64).
 struct PlanLayout {
     int64_t n_probs = 0;
-    size_t o_probs = 0, o_items = 0, o_chunks = 0, o_arena = 0, total = 0;
+    size_t o_probs = 0, o_items = 0, o_chunks = 0, o_arena = 0, total = 0, dev_total = 0;
     size_t out_bytes = 0, lo_bytes = 0;
 };
 
@@ -157,7 +161,8 @@ PlanLayout layout_of(const Planner &pl, size_t out_elem) {
     L.o_items = align256(L.o_probs + sizeof(PqgProblem) * L.n_probs);
     L.o_chunks = align256(L.o_items + sizeof(int64_t) * (L.n_probs + 1));
     L.o_arena = align256(L.o_chunks + sizeof(PqgChunk) * std::max<size_t>(1, pl.chunks.size()));
-    L.total = align256(L.o_arena + pl.arena.size());
+    L.total = align256(L.o_arena + pl.arena.size());  // the arena ends 256-aligned: pdata starts here
+    L.dev_total = L.total + align256(static_cast<size_t>(pl.pdata_bytes));
     L.out_bytes = static_cast<size_t>(pl.total_outputs) * 2 * out_elem;
     L.lo_bytes = static_cast<size_t>(pl.total_outputs) * 2 * sizeof(double);
     return L;
@@ -171,7 +176,7 @@ void pack_plan(const Planner &pl, const PlanLayout &L, unsigned char *h) {
 }
 
 int ensure_buffers(DeviceBuffers &B, const Planner &pl, const PlanLayout &L) {
-    PQG_CUDA(B.plan.ensure(L.total));
+    PQG_CUDA(B.plan.ensure(L.dev_total));
     const size_t n_parts = static_cast<size_t>(std::max<int64_t>(1, pl.total_parts));
     PQG_CUDA(B.partials.ensure(n_parts * 4 * sizeof(double)));
     PQG_CUDA(B.chunk_out.ensure(std::max<size_t>(1, pl.chunks.size()) * PQG_MAX_OUT * 4 * sizeof(double)));
@@ -181,23 +186,31 @@ int ensure_buffers(DeviceBuffers &B, const Planner &pl, const PlanLayout &L) {
     return PQG_OK;
 }
 
-// Builds the prefix tables of an uploaded plan (one launch; none if empty).
-int enqueue_delta(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayout &L, cudaStream_t s) {
-    if (pl.total_delta <= 0) return PQG_OK;
+// Builds every problem's seeds, step rows and prefix tables of an uploaded
+// plan (one launch; none without a walk).
+int enqueue_prep(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayout &L, cudaStream_t s) {
+    if (pl.total_items <= 0) return PQG_OK;
     unsigned char *d = static_cast<unsigned char *>(B.plan.p);
-    const PqgProblem *probs = reinterpret_cast<const PqgProblem *>(d + L.o_probs);
-    const int64_t threads = 256;
-    const int64_t blocks = std::min<int64_t>((pl.total_delta + threads - 1) / threads, int64_t(C.num_sms) * 16);
-    const int np = static_cast<int>(L.n_probs);
+    PrepArgs A;
+    A.probs = reinterpret_cast<PqgProblem *>(d + L.o_probs);
+    A.arena = d + L.o_arena;
+    A.delta = B.delta.p;
+    A.matrix_off = pl.matrix_off;
+    A.mat_cols = pl.mat_cols;
+    A.n_probs = static_cast<int32_t>(L.n_probs);
+    // enough blocks for every SM: several slices per problem for small batches
+    const int64_t want = int64_t(C.num_sms) * 4;
+    A.slices = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(64, want / std::max<int64_t>(1, L.n_probs))));
+    const int64_t blocks = std::min<int64_t>(L.n_probs * A.slices, int64_t(C.num_sms) * 16);
     switch (pl.precision()) {
         case Precision::C128:
-            build_delta<DELTA_F64><<<blocks, threads, 0, s>>>(probs, np, d + L.o_arena, B.delta.p, pl.total_delta);
+            prep_problems<PREP_F64><<<blocks, 256, 0, s>>>(A);
             break;
         case Precision::C64:
-            build_delta<DELTA_F32><<<blocks, threads, 0, s>>>(probs, np, d + L.o_arena, B.delta.p, pl.total_delta);
+            prep_problems<PREP_F32><<<blocks, 256, 0, s>>>(A);
             break;
         default:
-            build_delta<DELTA_DF><<<blocks, threads, 0, s>>>(probs, np, d + L.o_arena, B.delta.p, pl.total_delta);
+            prep_problems<PREP_DF><<<blocks, 256, 0, s>>>(A);
     }
     PQG_CUDA(cudaGetLastError());
     g_launches++;
@@ -295,7 +308,7 @@ int run_plan(Context &C, Planner &pl, T *out, double *out_lo) {
     g_walk_flops = pl.total_flops;
     g_h2d = static_cast<double>(L.total);
     g_d2h = static_cast<double>(align256(L.out_bytes) + L.lo_bytes);
-    st = enqueue_delta(C, C.bufs, pl, L, s);
+    st = enqueue_prep(C, C.bufs, pl, L, s);
     if (st) return st;
     PQG_CUDA(cudaEventRecord(C.evs, s));
     st = enqueue_pipeline<T>(C, C.bufs, pl, L, s, C.ev0, C.ev1, k, blocks);
@@ -344,9 +357,10 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     std::lock_guard<std::mutex> lock(C.mu);
     // inputs are validated before the device is touched
     Planner pl(prec, Form::PLAIN, C.cfg);
+    pl.set_matrix(matrix, nr, nc);
     for (int64_t b = 0; b < batch; ++b) {
         std::string err;
-        int st = pl.add(matrix, nr, nc, rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
+        int st = pl.add(rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
         if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
     }
     int st = C.init();
@@ -372,9 +386,10 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
     PlanConfig cfg = C.cfg;
     cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
     Planner pl(prec, Form::LAPLACE, cfg);
+    pl.set_matrix(matrix, nr, nc);
     for (int64_t b = 0; b < batch; ++b) {
         std::string err;
-        int st = pl.add(matrix, nr, nc, rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
+        int st = pl.add(rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
         if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
     }
     int st = C.init();
@@ -492,7 +507,7 @@ int plan_build(Context &C, PlanHandle *h) {
     std::vector<unsigned char> hp(h->L.total);
     pack_plan(h->pl, h->L, hp.data());
     PQG_CUDA(cudaMemcpyAsync(h->B.plan.p, hp.data(), h->L.total, cudaMemcpyHostToDevice, h->stream));
-    st = enqueue_delta(C, h->B, h->pl, h->L, h->stream);
+    st = enqueue_prep(C, h->B, h->pl, h->L, h->stream);
     if (st) return st;
     PQG_CUDA(cudaStreamSynchronize(h->stream));
     const KernelInfo *k = nullptr;
@@ -643,9 +658,10 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     h->pl = Planner(prec, fm, C.cfg);
     h->single = dtype == 1;
     h->n_cols = n_cols;
+    h->pl.set_matrix(m, n_rows, n_cols);
     for (int64_t b = 0; b < batch; ++b) {
         std::string err;
-        int st = h->pl.add(m, n_rows, n_cols, rows ? rows + b * n_rows : nullptr, cols ? cols + b * n_cols : nullptr, err);
+        int st = h->pl.add(rows ? rows + b * n_rows : nullptr, cols ? cols + b * n_cols : nullptr, err);
         if (st) {
             delete h;
             return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);

@@ -30,19 +30,6 @@ int64_t binom64(int64_t n, int64_t k) {
     return r;
 }
 
-// Error-free sum of doubles (Knuth TwoSum), used to form the FP64 seed rows
-// from a compensated sum.
-struct Kahan2 {
-    double s = 0.0, c = 0.0;
-    void add(double x) {
-        double t = s + x;
-        double bb = t - s;
-        c += (s - (t - bb)) + (x - bb);
-        s = t;
-    }
-    double value() const { return s + c; }
-};
-
 }  // namespace
 
 double algorithmic_flops(const PendingProblem &p, Form form) {
@@ -56,10 +43,16 @@ double algorithmic_flops(const PendingProblem &p, Form form) {
     return p.S * (4.0 * nc + 12.0 * sum_cm + 6.0 * nc + 4.0 * p.n_out);
 }
 
-int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
-                 std::string &err) {
+void Planner::set_matrix(const double *a, int64_t nr, int64_t nc) {
+    a_ = a;
+    int_nr_ = nr;
+    int_nc_ = nc;
+}
+
+int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err) {
+    const int64_t nr = int_nr_, nc = int_nc_;
     PendingProblem p;
-    if (nr < 0 || nc < 0 || (nr > 0 && nc > 0 && a == nullptr) || (nr > 0 && !rows) || (nc > 0 && !cols)) {
+    if (nr < 0 || nc < 0 || (nr > 0 && nc > 0 && a_ == nullptr) || (nr > 0 && !rows) || (nc > 0 && !cols)) {
         err = "invalid matrix or multiplicity buffers";
         return 2;
     }
@@ -103,21 +96,24 @@ int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, c
         err = "too many particles";
         return 3;
     }
+    if (nr > (1 << 30) || nc > (1 << 30)) {
+        err = "matrix dimension above 2^30";
+        return 3;
+    }
     // the double-float kernel keeps typical terms (>= N^(-N/2) after column
     // scaling) far above the FP32 underflow threshold only for N <= 32
     if (sr > 32) df_ok_add_ = false;
 
     // columns with nonzero multiplicity
-    std::vector<int> keep;
     for (int64_t j = 0; j < nc; ++j)
-        if (cols[j] > 0) keep.push_back(static_cast<int>(j));
-    if (keep.empty() || static_cast<int>(keep.size()) > PQG_MAX_COLS) {
-        err = keep.empty() ? "no column with nonzero multiplicity"
-                           : "more than 32 distinct columns with nonzero multiplicity";
-        return keep.empty() ? 2 : 3;
+        if (cols[j] > 0) p.col.push_back(static_cast<int>(j));
+    if (p.col.empty() || static_cast<int>(p.col.size()) > PQG_MAX_COLS) {
+        err = p.col.empty() ? "no column with nonzero multiplicity"
+                            : "more than 32 distinct columns with nonzero multiplicity";
+        return p.col.empty() ? 2 : 3;
     }
-    p.nc = static_cast<int>(keep.size());
-    for (int j : keep) {
+    p.nc = static_cast<int>(p.col.size());
+    for (int j : p.col) {
         if (cols[j] > 255) {
             err = "column multiplicity above 255";
             return 3;
@@ -129,8 +125,8 @@ int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, c
         // outputs: one per kept column; every zero-multiplicity column shares
         // one extra output (its exponent stays 0: permanent_laplace.cpp:180,210)
         p.out_map.assign(static_cast<size_t>(nc), -1);
-        for (int k = 0; k < p.nc; ++k) p.out_map[keep[k]] = k;
-        p.laplace_full = static_cast<int64_t>(keep.size()) < nc;
+        for (int k = 0; k < p.nc; ++k) p.out_map[p.col[k]] = k;
+        p.laplace_full = static_cast<int64_t>(p.col.size()) < nc;
         for (int64_t j = 0; j < nc; ++j)
             if (p.out_map[j] < 0) p.out_map[j] = p.nc;
         p.n_out = p.nc + (p.laplace_full ? 1 : 0);
@@ -145,21 +141,13 @@ int Planner::add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, c
             min_idx = i;
         }
     }
-    auto elem = [&](int64_t i, int k, int part) { return a[2 * (i * nc + keep[k]) + part]; };
-    p.a0.resize(2 * p.nc);
-    for (int k = 0; k < p.nc; ++k) {
-        p.a0[2 * k] = elem(min_idx, k, 0);
-        p.a0[2 * k + 1] = elem(min_idx, k, 1);
-    }
+    p.row0 = static_cast<int>(min_idx);
     double S = 1.0;
     for (int64_t i = 0; i < nr; ++i) {
         int m = rows[i] - (i == min_idx ? 1 : 0);
         if (m <= 0) continue;
         p.m.push_back(m);
-        for (int k = 0; k < p.nc; ++k) {
-            p.rows.push_back(elem(i, k, 0));
-            p.rows.push_back(elem(i, k, 1));
-        }
+        p.row.push_back(static_cast<int>(i));
         S *= (m + 1);
     }
     if (S > std::ldexp(1.0, 50)) {
@@ -245,12 +233,6 @@ std::vector<double> build_weights(const std::vector<int> &mm, int64_t P) {
     return w;
 }
 
-void push_df(std::vector<float> &v, double x) {
-    const float hi = static_cast<float>(x);
-    v.push_back(hi);
-    v.push_back(static_cast<float>(x - static_cast<double>(hi)));
-}
-
 }  // namespace
 
 void Planner::finish() {
@@ -262,6 +244,9 @@ void Planner::finish() {
     table_cache_.clear();
     total_items = total_parts = total_outputs = 0;
     total_delta = 0;
+    pdata_bytes = 0;
+    matrix_off = 0;
+    mat_rows = mat_cols = 0;
     total_steps = total_flops = 0.0;
     max_nc = 1;
     df_ok = df_ok_add_;
@@ -276,23 +261,19 @@ void Planner::finish() {
     // step (zero rows), so each term is multiplied by 1 exactly.  In the
     // Laplace form a neutral column's own output is never read, and the shared
     // output of the zero-multiplicity columns moves behind the padded ones.
+    bool any_walk = false;
     {
         int ncmax = 1;
         for (auto &p : pending)
-            if (p.kind == PQG_KIND_WALK) ncmax = std::max(ncmax, p.nc);
+            if (p.kind == PQG_KIND_WALK) {
+                ncmax = std::max(ncmax, p.nc);
+                any_walk = true;
+            }
         for (auto &p : pending) {
             if (p.kind != PQG_KIND_WALK || p.nc == ncmax) continue;
             const int old = p.nc, add = ncmax - old;
             p.cm.resize(ncmax, 1);
-            p.a0.resize(2 * ncmax, 0.0);
-            for (int k = old; k < ncmax; ++k) p.a0[2 * k] = 1.0;
-            std::vector<double> rows;
-            rows.reserve(p.m.size() * 2 * ncmax);
-            for (size_t i = 0; i < p.m.size(); ++i) {
-                rows.insert(rows.end(), p.rows.begin() + i * 2 * old, p.rows.begin() + (i + 1) * 2 * old);
-                rows.insert(rows.end(), static_cast<size_t>(2 * add), 0.0);
-            }
-            p.rows.swap(rows);
+            p.col.resize(ncmax, -1);
             p.nc = ncmax;
             p.padded_cols = add;
             if (laplace) {
@@ -301,6 +282,12 @@ void Planner::finish() {
                 p.n_out = ncmax + (p.laplace_full ? 1 : 0);
             }
         }
+    }
+    // the matrix every problem indexes, once
+    if (any_walk) {
+        mat_rows = int_nr_;
+        mat_cols = int_nc_;
+        matrix_off = push_bytes_(a_, static_cast<size_t>(2 * int_nr_ * int_nc_) * sizeof(double));
     }
 
     // Steps per lane: about items_per_smsp warps of work per SM sub-partition
@@ -321,6 +308,14 @@ void Planner::finish() {
     if (cfg_.p_max_user) p_cap = cfg_.p_max;
     const int64_t p_max = laplace ? std::min<int64_t>(std::min<int64_t>(cfg_.p_max, p_cap), 512)
                                   : std::min<int64_t>(cfg_.p_max, p_cap);
+    // per-problem device data (built by the prep kernel), by offset from the
+    // start of that region; the region follows the uploaded arena
+    auto pdata = [&](int64_t bytes) {
+        const int64_t off = pdata_bytes;
+        pdata_bytes += (bytes + 15) / 16 * 16;
+        return off;
+    };
+    const int64_t d_elem = prec_ == Precision::C64 ? 8 : 16;  // one D element: float2, else double2 / float4
 
     for (size_t ip = 0; ip < np; ++ip) {
         PendingProblem &p = pending[ip];
@@ -334,6 +329,7 @@ void Planner::finish() {
         q.part_begin = total_parts;
         q.chunk_begin = static_cast<int64_t>(chunks.size());
         q.delta_begin = total_delta;  // kept monotone for the device's binary search
+        q.off_base64 = q.off_outer64 = q.off_base_df = q.off_outer_df = q.off_D = -1;
         if (p.kind == PQG_KIND_CONSTANT) {
             q.cval_re = p.cre;
             q.cval_im = p.cim;
@@ -373,92 +369,36 @@ void Planner::finish() {
             }
         }
         const size_t K = inner.size();
+        const int no = static_cast<int>(outer.size());
         q.P = static_cast<int32_t>(P);
         q.K = static_cast<int32_t>(K);
-        q.n_outer = static_cast<int32_t>(outer.size());
+        q.n_outer = no;
         q.Q = static_cast<int64_t>(std::llround(p.S / P));
         // laplace kernels walk one outer position per lane
         q.R = laplace ? 1 : std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
         q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / 32));
-        for (size_t o = 0; o < outer.size(); ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
+        for (int o = 0; o < no; ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
         for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
 
-        // Double-float plans scale column j by 2^-e_j so that no column sum
-        // can exceed 1 in magnitude: |c_j| <= |a0_j| + sum_i m_i |a_ij| <= 1.
-        // Powers of two are exact; the result is multiplied back through the
-        // final 2^-scale_exp factor.
-        std::vector<double> cscale(p.nc, 1.0);
-        if (df) {
-            int shift = 0;
-            for (int k = 0; k < p.nc; ++k) {
-                double B = std::hypot(p.a0[2 * k], p.a0[2 * k + 1]);
-                for (int i = 0; i < nd; ++i) {
-                    const double *r = &p.rows[static_cast<size_t>(i) * 2 * p.nc + 2 * k];
-                    B += p.m[i] * std::hypot(r[0], r[1]);
-                }
-                int e = 0;
-                if (B > 0.0) std::frexp(B, &e);  // B in [2^(e-1), 2^e)
-                cscale[k] = std::ldexp(1.0, -e);
-                shift += e * p.cm[k];
-            }
-            q.scale_exp = p.scale_exp - shift;
-        }
-        auto row = [&](int i, int c) { return p.rows[static_cast<size_t>(i) * 2 * p.nc + c] * cscale[c / 2]; };
-
-        // seeds: column sums with every digit at 0, a0 + sum_i m_i a_i (compensated)
-        std::vector<double> base(2 * p.nc);
-        for (int c = 0; c < 2 * p.nc; ++c) {
-            Kahan2 s;
-            s.add(p.a0[c] * cscale[c / 2]);
-            for (int i = 0; i < nd; ++i) s.add(static_cast<double>(p.m[i]) * row(i, c));
-            base[c] = s.value();
-        }
-        std::vector<double> orow, irow;
-        for (int i : outer)
-            for (int c = 0; c < 2 * p.nc; ++c) orow.push_back(row(i, c));
-        for (int i : inner)
-            for (int c = 0; c < 2 * p.nc; ++c) irow.push_back(row(i, c));
-        q.off_inner64 = irow.empty() ? 0 : push_bytes_(irow.data(), irow.size() * sizeof(double));
-        q.off_base64 = push_bytes_(base.data(), base.size() * sizeof(double));
-        q.off_outer64 = orow.empty() ? q.off_base64 : push_bytes_(orow.data(), orow.size() * sizeof(double));
+        // matrix rows and columns for the device prep
         {
-            std::vector<float> bdf, odf;
-            for (double v : base) push_df(bdf, v);
-            for (double v : orow) push_df(odf, v);
-            q.off_base_df = push_bytes_(bdf.data(), bdf.size() * sizeof(float));
-            q.off_outer_df = odf.empty() ? q.off_base_df : push_bytes_(odf.data(), odf.size() * sizeof(float));
+            std::vector<int32_t> idx;
+            idx.reserve(1 + nd + p.nc);
+            idx.push_back(p.row0);
+            for (int i : outer) idx.push_back(p.row[i]);
+            for (int i : inner) idx.push_back(p.row[i]);
+            for (int k = 0; k < p.nc; ++k) idx.push_back(p.col[k]);
+            q.off_idx = push_bytes_(idx.data(), idx.size() * sizeof(int32_t));
         }
-
-        // D rows of the outer digits, in kernel precision
-        const std::vector<int> &digits = outer;
-        const size_t nrows = std::max<size_t>(1, 2 * digits.size());
+        // device-built seeds and step rows in the walk's precision
         if (c128) {
-            std::vector<double> D(nrows * 2 * p.nc, 0.0);
-            for (size_t k = 0; k < digits.size(); ++k)
-                for (int c = 0; c < 2 * p.nc; ++c) {
-                    const double v = 2.0 * row(digits[k], c);
-                    D[(2 * k) * 2 * p.nc + c] = -v;
-                    D[(2 * k + 1) * 2 * p.nc + c] = v;
-                }
-            q.off_D = push_bytes_(D.data(), D.size() * sizeof(double));
-        } else if (df) {
-            std::vector<float> D;
-            D.reserve(nrows * 4 * p.nc);
-            for (size_t k = 0; k < digits.size(); ++k)
-                for (int sgn = 0; sgn < 2; ++sgn)
-                    for (int c = 0; c < 2 * p.nc; ++c) push_df(D, (sgn ? 2.0 : -2.0) * row(digits[k], c));
-            if (D.empty()) D.assign(4 * p.nc, 0.0f);
-            q.off_D = push_bytes_(D.data(), D.size() * sizeof(float));
+            q.off_base64 = pdata(16 * p.nc);
+            if (no) q.off_outer64 = pdata(16 * int64_t(no) * p.nc);
         } else {
-            std::vector<float> D(nrows * 2 * p.nc, 0.0f);
-            for (size_t k = 0; k < digits.size(); ++k)
-                for (int c = 0; c < 2 * p.nc; ++c) {
-                    const double v = 2.0 * row(digits[k], c);
-                    D[(2 * k) * 2 * p.nc + c] = static_cast<float>(-v);
-                    D[(2 * k + 1) * 2 * p.nc + c] = static_cast<float>(v);
-                }
-            q.off_D = push_bytes_(D.data(), D.size() * sizeof(float));
+            q.off_base_df = pdata(16 * p.nc);
+            if (no) q.off_outer_df = pdata(16 * int64_t(no) * p.nc);
         }
+        if (no) q.off_D = pdata(d_elem * 2 * int64_t(no) * p.nc);
         q.delta_begin = total_delta;
         total_delta += static_cast<int64_t>(q.P) * p.nc;
 
@@ -500,7 +440,21 @@ void Planner::finish() {
         total_flops += algorithmic_flops(p, form_);
     }
     item_begin[np] = total_items;
-    align_(16);
+    // the device data follows the uploaded arena: rebase its offsets (an
+    // unused one points at the region's start and is never read)
+    const int64_t pbase = align_(256);
+    for (auto &q : probs) {
+        if (q.kind != PQG_KIND_WALK) {
+            q.off_base64 = q.off_outer64 = q.off_base_df = q.off_outer_df = q.off_D = pbase;
+            continue;
+        }
+        for (int64_t *o : {&q.off_base64, &q.off_outer64, &q.off_base_df, &q.off_outer_df, &q.off_D})
+            *o = *o < 0 ? pbase : pbase + *o;
+        if (q.n_outer == 0) {  // never read: the seed is the base
+            q.off_outer64 = q.off_base64;
+            q.off_outer_df = q.off_base_df;
+        }
+    }
 }
 
 }  // namespace pqg

@@ -1,5 +1,11 @@
 // Host-side planner: turns (matrix, row multiplicities, column multiplicities)
 // problems into the device work plan described in pqg_plan.h.
+//
+// The planner only decides: the row reduction, which matrix rows and columns
+// take part, the inner/outer split of the Gray-code digits, the per-problem
+// data layout and the work items.  It copies no matrix data per problem: the
+// plan carries the matrix once, and a device kernel (prep.cuh) builds every
+// problem's seeds, step rows and prefix tables in device memory.
 #pragma once
 #include <map>
 #include <string>
@@ -28,9 +34,10 @@ struct PendingProblem {
     double cre = 1.0, cim = 0.0;
     int nc = 0;
     std::vector<int> cm;          // multiplicities of the kept columns
-    std::vector<double> a0;       // 2*nc: the prepended row (multiplicity 1)
+    std::vector<int> col;         // matrix column of each kept column (-1: neutral padding)
+    int row0 = 0;                 // matrix row of the prepended copy (multiplicity 1)
     std::vector<int> m;           // digit multiplicities (>= 1)
-    std::vector<double> rows;     // digits x 2*nc
+    std::vector<int> row;         // matrix row of each digit
     int scale_exp = 0;
     int n_out = 1;
     bool laplace_full = false;    // Laplace form with a zero-multiplicity column
@@ -43,13 +50,16 @@ class Planner {
   public:
     Planner(Precision prec, Form form, const PlanConfig &cfg) : prec_(prec), form_(form), cfg_(cfg) {}
 
-    // Adds one problem; `a` is interleaved complex128 (the complex64 entry
-    // points widen their input first: the seeds are formed in FP64).
-    // Returns PQG_OK or an error status with `err` set.
-    int add(const double *a, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
-            std::string &err);
+    // The matrix every problem of this plan indexes: interleaved complex128,
+    // row-major n_rows x n_cols (the complex64 entry points widen first).
+    void set_matrix(const double *a, int64_t nr, int64_t nc);
 
-    // Fixes every problem's split and lays out the arena.
+    // Adds one problem over the plan's matrix.  Returns PQG_OK or an error
+    // status with `err` set.
+    int add(const int32_t *rows, const int32_t *cols, std::string &err);
+
+    // Fixes every problem's split and lays out the arena and the per-problem
+    // device data.
     void finish();
 
     void set_config(const PlanConfig &cfg) { cfg_ = cfg; }
@@ -58,22 +68,25 @@ class Planner {
     std::vector<PqgProblem> probs;
     std::vector<int64_t> item_begin;   // n_probs + 1
     std::vector<PqgChunk> chunks;
-    std::vector<unsigned char> arena;  // data referenced by byte offsets
+    std::vector<unsigned char> arena;  // weight tables and the matrix, by byte offset
     int64_t total_items = 0;
     int64_t total_parts = 0;           // dd-complex partial slots
     int64_t total_outputs = 0;
-    int64_t total_delta = 0;           // prefix-table elements (sum of P x nc)
+    int64_t total_delta = 0;           // prefix-table entries (delta buffer elements)
+    int64_t pdata_bytes = 0;           // per-problem device data built by the prep kernel
+    int64_t matrix_off = 0;            // byte offset of the matrix in the arena
+    int64_t mat_rows = 0, mat_cols = 0;
     int max_nc = 0;
     double total_steps = 0.0;          // sum over problems of the Gray-code space
     double total_flops = 0.0;          // algorithmic flop count, see algorithmic_flops()
 
     Precision precision() const { return prec_; }
     void set_precision(Precision p) { prec_ = p; }
+    Form form() const { return form_; }
     // C128DF plans only: false when some problem falls outside the double-float
     // kernel's validity domain (more than 32 particles, or an inner weight that
     // is not exact in FP32); the caller then plans in C128 instead.
     bool df_ok = true;
-    Form form() const { return form_; }
 
   private:
     Precision prec_;
@@ -81,6 +94,8 @@ class Planner {
     PlanConfig cfg_;
     std::map<std::vector<int>, int64_t> table_cache_;
     bool df_ok_add_ = true;
+    const double *a_ = nullptr;
+    int64_t int_nr_ = 0, int_nc_ = 0;
     int64_t align_(size_t a);
     int64_t push_bytes_(const void *p, size_t n);
 };

@@ -35,21 +35,27 @@ struct PqgProblem {
     int32_t n_outer;    // outer digits
     int32_t P;          // inner codes = table entries (>= 1)
     int32_t K;          // inner digits
-    int32_t scale_exp;  // result = sum / 2^scale_exp (sum of multiplicities - 1, less column scales)
+    int32_t scale_exp;  // result = sum / 2^(scale_exp - col_shift); scale_exp = sum of multiplicities - 1
     int32_t cm_max;     // largest column multiplicity
     int32_t n_out;      // outputs of this problem (1, or the Laplace count)
+    int32_t col_shift;  // sum_j e_j cm_j of the double-float column scales 2^-e_j (device-written)
+    int32_t pad0;
     int64_t Q;          // outer positions
     int64_t R;          // outer positions per lane
     int64_t item_begin; // first work item
     int64_t n_items;    // ceil(Q / (32 R))
-    int64_t off_base64;   // byte offsets into the arena:  nc x double2, column sums with every digit 0
+    // Byte offsets into the arena.  Uploaded by the host:
+    int64_t off_idx;      //   int32 [row0, matrix row of each outer digit, of each inner
+                          //   digit, matrix column of each column (-1: neutral padding)]
+    int64_t off_tab;      //   P x PqgStep
+    // Built on the device from the matrix (prep.cuh); FP64 walks read the
+    // *64 seeds, FP32-pipe walks the *_df ones:
+    int64_t off_base64;   //   nc x double2, column sums with every digit 0
     int64_t off_outer64;  //   n_outer x nc x double2, rows a_o of the outer digits
     int64_t off_base_df;  //   nc x float4 {re_hi, re_lo, im_hi, im_lo}, the same column sums
     int64_t off_outer_df; //   n_outer x nc x float4, the same rows
-    int64_t off_inner64;  //   K x nc x double2, rows a_k of the inner digits
     int64_t off_D;        //   2 n_outer x nc elements in kernel precision: row 2o = -2 a_o
                           //   (outer digit o steps up), row 2o+1 = +2 a_o (steps down)
-    int64_t off_tab;      //   P x PqgStep
     int64_t delta_begin;  // first element of this problem's P x nc prefix table (delta buffer)
     int64_t out_index;  // first output slot of this problem
     int64_t part_begin; // first partial slot (n_out dd-complex slots per item)

@@ -1,0 +1,184 @@
+// Device construction of every problem's walk data from the plan's matrix.
+//
+// The host uploads one matrix (FP64, interleaved complex, row-major) and, per
+// problem, the matrix rows of its digits and the matrix columns it keeps
+// (PqgProblem::off_idx).  This kernel builds, in the walk's precision:
+//   * the DF column scales 2^-e_j with B_j = |a0_j| + sum_i m_i |a_ij| in
+//     [2^(e_j-1), 2^e_j), so no double-float column sum exceeds 1 in magnitude
+//     (powers of two are exact; sum_j e_j cm_j goes to col_shift and is
+//     multiplied back in the final scaling);
+//   * the seeds, the column sums with every digit at 0: a0 + sum_i m_i a_i,
+//     TwoSum-compensated in FP64;
+//   * the outer digits' rows a_o, and the one-digit update rows -2 a_o / +2 a_o;
+//   * the prefix table Delta(t)_j = sum_k -2 g_k(t) a_kj over the inner codes.
+// A neutral padding column (index -1) has a0 = 1 and zero rows.
+//
+// Work split: `slices` blocks per problem; every block of a problem computes
+// the (cheap) column scales, slice 0 writes the seeds and rows, all slices
+// share the prefix-table entries.  The grid loops over (problem, slice).
+#pragma once
+#include "walk_common.cuh"
+
+namespace pqg {
+
+enum PrepFormat : int { PREP_F64 = 0, PREP_F32 = 1, PREP_DF = 2 };
+
+struct PrepArgs {
+    PqgProblem *probs;
+    unsigned char *arena;
+    void *delta;
+    int64_t matrix_off;  // byte offset of the matrix in the arena
+    int64_t mat_cols;
+    int32_t n_probs;
+    int32_t slices;
+};
+
+__device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - static_cast<double>(hi));
+}
+
+template <int FMT>
+__global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
+    __shared__ int rowix[1 + PQG_MAX_OUTER + PQG_MAX_INNER];
+    __shared__ int colix[PQG_MAX_COLS];
+    __shared__ double cscale[PQG_MAX_COLS];
+    __shared__ int eshift[PQG_MAX_COLS];
+    const double *mat = reinterpret_cast<const double *>(A.arena + A.matrix_off);
+    const int64_t total = static_cast<int64_t>(A.n_probs) * A.slices;
+    for (int64_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
+        const int ip = static_cast<int>(vb / A.slices);
+        const int slice = static_cast<int>(vb - static_cast<int64_t>(ip) * A.slices);
+        PqgProblem *pr = A.probs + ip;
+        if (pr->kind != PQG_KIND_WALK) continue;  // uniform over the block
+        const int nc = pr->nc, no = pr->n_outer, K = pr->K;
+        const int nd = no + K;
+        const int32_t *idx = reinterpret_cast<const int32_t *>(A.arena + pr->off_idx);
+        for (int i = threadIdx.x; i < 1 + nd; i += blockDim.x) rowix[i] = idx[i];
+        for (int j = threadIdx.x; j < nc; j += blockDim.x) colix[j] = idx[1 + nd + j];
+        __syncthreads();
+        // a0 (the prepended row) and the row of digit d (outer first, then inner)
+        auto a0 = [&](int j) -> double2 {
+            const int c = colix[j];
+            if (c < 0) return make_double2(1.0, 0.0);
+            const double *e = mat + 2 * (static_cast<int64_t>(rowix[0]) * A.mat_cols + c);
+            return make_double2(e[0], e[1]);
+        };
+        auto ad = [&](int d, int j) -> double2 {
+            const int c = colix[j];
+            if (c < 0) return make_double2(0.0, 0.0);
+            const double *e = mat + 2 * (static_cast<int64_t>(rowix[1 + d]) * A.mat_cols + c);
+            return make_double2(e[0], e[1]);
+        };
+        auto mult = [&](int d) -> int { return d < no ? pr->outer_m[d] : pr->inner_m[d - no]; };
+
+        for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+            double s = 1.0;
+            int e = 0;
+            if constexpr (FMT == PREP_DF) {
+                const double2 v = a0(j);
+                double B = hypot(v.x, v.y);
+                for (int d = 0; d < nd; ++d) {
+                    const double2 w = ad(d, j);
+                    B += mult(d) * hypot(w.x, w.y);
+                }
+                if (B > 0.0) frexp(B, &e);
+                s = ldexp(1.0, -e);
+            }
+            cscale[j] = s;
+            eshift[j] = e * pr->cm[j];
+        }
+        __syncthreads();
+
+        if (slice == 0) {
+            if (threadIdx.x == 0) {
+                int sh = 0;
+                for (int j = 0; j < nc; ++j) sh += eshift[j];
+                pr->col_shift = sh;
+            }
+            // seeds
+            for (int c = threadIdx.x; c < 2 * nc; c += blockDim.x) {
+                const int j = c >> 1, part = c & 1;
+                const double sc = cscale[j];
+                const double2 v0 = a0(j);
+                double sum = (part ? v0.y : v0.x) * sc, comp = 0.0;
+                for (int d = 0; d < nd; ++d) {
+                    const double2 w = ad(d, j);
+                    const double x = static_cast<double>(mult(d)) * ((part ? w.y : w.x) * sc);
+                    const double t = sum + x;
+                    const double bb = t - sum;
+                    comp += (sum - (t - bb)) + (x - bb);
+                    sum = t;
+                }
+                const double base = sum + comp;
+                if constexpr (FMT == PREP_F64) {
+                    reinterpret_cast<double *>(A.arena + pr->off_base64)[c] = base;
+                } else {
+                    float *b = reinterpret_cast<float *>(A.arena + pr->off_base_df);
+                    split_df(base, b[2 * c], b[2 * c + 1]);
+                }
+            }
+            // outer rows and update rows
+            for (int e = threadIdx.x; e < no * 2 * nc; e += blockDim.x) {
+                const int o = e / (2 * nc);
+                const int c = e - o * 2 * nc;
+                const int j = c >> 1, part = c & 1;
+                const double2 w = ad(o, j);
+                const double v = (part ? w.y : w.x) * cscale[j];
+                const int64_t up = static_cast<int64_t>(2 * o) * 2 * nc + c;  // row 2o: -2 a_o
+                const int64_t dn = up + 2 * nc;                                 // row 2o+1: +2 a_o
+                if constexpr (FMT == PREP_F64) {
+                    reinterpret_cast<double *>(A.arena + pr->off_outer64)[e] = v;
+                    double *D = reinterpret_cast<double *>(A.arena + pr->off_D);
+                    D[up] = -2.0 * v;
+                    D[dn] = 2.0 * v;
+                } else {
+                    float *orow = reinterpret_cast<float *>(A.arena + pr->off_outer_df);
+                    split_df(v, orow[2 * e], orow[2 * e + 1]);
+                    float *D = reinterpret_cast<float *>(A.arena + pr->off_D);
+                    if constexpr (FMT == PREP_DF) {
+                        split_df(-2.0 * v, D[2 * up], D[2 * up + 1]);
+                        split_df(2.0 * v, D[2 * dn], D[2 * dn + 1]);
+                    } else {
+                        D[up] = __double2float_rn(-2.0 * v);
+                        D[dn] = __double2float_rn(2.0 * v);
+                    }
+                }
+            }
+        }
+
+        // prefix table: entries (t, j) of this problem, spread over its slices
+        const int64_t n_ent = static_cast<int64_t>(pr->P) * nc;
+        for (int64_t e = static_cast<int64_t>(slice) * blockDim.x + threadIdx.x; e < n_ent;
+             e += static_cast<int64_t>(A.slices) * blockDim.x) {
+            const int64_t t = e / nc;
+            const int j = static_cast<int>(e - t * nc);
+            uint8_t g[PQG_MAX_INNER];
+            gray_decode(pr->inner_m, K, t, g);
+            double re = 0.0, im = 0.0;
+            for (int k = 0; k < K; ++k) {
+                if (!g[k]) continue;
+                const double f = -2.0 * g[k];
+                const double2 a = ad(no + k, j);
+                re = __fma_rn(f, a.x, re);
+                im = __fma_rn(f, a.y, im);
+            }
+            re *= cscale[j];
+            im *= cscale[j];
+            const int64_t at = pr->delta_begin + e;
+            if constexpr (FMT == PREP_F64) {
+                reinterpret_cast<double2 *>(A.delta)[at] = make_double2(re, im);
+            } else if constexpr (FMT == PREP_F32) {
+                reinterpret_cast<float2 *>(A.delta)[at] = make_float2(__double2float_rn(re), __double2float_rn(im));
+            } else {
+                float4 v;
+                split_df(re, v.x, v.y);
+                split_df(im, v.z, v.w);
+                reinterpret_cast<float4 *>(A.delta)[at] = v;
+            }
+        }
+        __syncthreads();  // the shared index and scale arrays are reused
+    }
+}
+
+}  // namespace pqg

@@ -88,7 +88,7 @@ __global__ void finish_problems(const PqgProblem *__restrict__ probs, int n_prob
         if (lane == 0) {
             // scaling by a power of two is exact in both words; ldexp avoids an
             // intermediate 2^-scale_exp that would itself overflow
-            const int e = -pr->scale_exp;
+            const int e = pr->col_shift - pr->scale_exp;
             const double rh = ldexp(r.hi, e), rl = ldexp(r.lo, e), ih = ldexp(i.hi, e), il = ldexp(i.lo, e);
             if constexpr (sizeof(T) == 8) {
                 out[2 * (oi + o)] = rh;
