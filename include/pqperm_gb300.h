@@ -95,6 +95,25 @@ int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64
 int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                                     const int32_t *cols, int64_t batch, float *out, int64_t *n_out);
 
+/* Gradient of the permanent with respect to every matrix entry.
+ * Replaces grad_perm (src/permanent.cpp:271-300 of the reference), reached
+ * through the JAX FFI backward target PermBwd (src/jax_perm/jax_perm_core.cpp:
+ * 139-208), whose batch loop over leading matrix dimensions this mirrors.
+ * `matrices` holds `batch` row-major n_rows x n_cols interleaved complex
+ * matrices; rows (batch x n_rows) and cols (batch x n_cols) their
+ * multiplicities.  out[b][i][j] (interleaved complex, batch x n_rows x n_cols)
+ * = rows_i cols_j perm(A_b; rows - e_i, cols - e_j), 0 where rows_i or cols_j
+ * is 0.  PQG_ERR_SUM_MISMATCH when sum(rows) != sum(cols) and some entry has
+ * rows_i > 0 and cols_j > 0 (where the reference's first minor throws).  The
+ * reference returns an n_rows x n_rows array; this returns n_rows x n_cols,
+ * the same for the square matrices it supports.  Computed as one batched
+ * Laplace walk per row of nonzero multiplicity (FP64 walk for complex128,
+ * FP32 for complex64). */
+int pqg_permanent_grad_c128(const double *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                            const int32_t *cols, int64_t batch, double *out);
+int pqg_permanent_grad_c64(const float *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                           const int32_t *cols, int64_t batch, float *out);
+
 /* Plan handles: plan and upload a batch once, then execute it many times as
  * one CUDA graph (queue reset, persistent walk, reductions) on the handle's
  * own stream — the form used for repeated batches (exact probabilities of a

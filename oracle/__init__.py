@@ -13,6 +13,8 @@ Contents:
     arithmetic and threading (the CPU baseline where the reference module is absent).
   * ``reference_module()``: the reference's own pybind module when it was built
     here by oracle/build_ref.sh (None elsewhere).
+  * ``grad_perm``: restatement of the reference's permanent gradient
+    (src/permanent.cpp:271-300), minor by minor, over any permanent function.
   * ``sampler``: numpy restatement of the Clifford & Clifford B sampler.
 """
 
@@ -162,3 +164,26 @@ def reference_module():
         return importlib.import_module("piquasso._math.permanent")
     except ImportError:
         return None
+
+
+def grad_perm(matrix, rows, cols, perm=None):
+    """G[i, j] = rows[i] * cols[j] * perm(A; rows - e_i, cols - e_j), zero where
+    rows[i] or cols[j] is zero (src/permanent.cpp:271-300: the same loop over
+    (i, j), one permanent per minor).  ``perm`` defaults to the double-double
+    ``permanent``; pass the reference module's ``permanent`` to follow it
+    bit for bit.  Returns an (n_rows, n_cols) complex128 array."""
+    A = np.asarray(matrix)
+    rows = np.asarray(rows).astype(np.int64)
+    cols = np.asarray(cols).astype(np.int64)
+    perm = perm or permanent
+    G = np.zeros(A.shape, dtype=np.complex128)
+    for i in range(A.shape[0]):
+        for j in range(A.shape[1]):
+            if rows[i] == 0 or cols[j] == 0:
+                continue
+            r2 = rows.copy()
+            r2[i] -= 1
+            c2 = cols.copy()
+            c2[j] -= 1
+            G[i, j] = float(rows[i]) * float(cols[j]) * complex(perm(A, r2, c2))
+    return G

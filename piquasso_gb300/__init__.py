@@ -3,7 +3,7 @@
 Public API (drop-in for ``piquasso._math.permanent``):
     permanent(matrix, rows, cols)
     permanent_laplace(matrix, rows, cols)
-plus the additive ``permanent_batch`` and the connector in
+plus the additive ``permanent_batch``, ``permanent_grad`` and the connector in
 ``piquasso_gb300.connector``.
 """
 
@@ -14,6 +14,7 @@ from .permanent import (  # noqa: F401
     permanent,
     permanent_batch,
     permanent_dd,
+    permanent_grad,
     permanent_laplace,
     permanent_laplace_batch,
 )

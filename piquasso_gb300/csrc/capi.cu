@@ -422,6 +422,93 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
     return PQG_OK;
 }
 
+// Gradient of the permanent with respect to every matrix entry, for `batch`
+// matrices stacked as (batch, nr, nc), each with its own multiplicities:
+//     G_ij = rows_i cols_j perm(A; rows - e_i, cols - e_j)
+// (the reference's grad_perm, src/permanent.cpp:271-300, which evaluates the
+// n^2 minors one by one).  Here one Laplace plan serves every matrix: problem
+// (b, i) walks rows - e_i once and its output j is perm(A_b; rows - e_i,
+// cols - e_j) (Lemma 1 of arXiv:2005.04214), so a matrix costs one walk per
+// row with nonzero multiplicity.  Entries with rows_i = 0 or cols_j = 0 are 0;
+// unequal sums fail as the reference's first minor would (only when some
+// entry has rows_i > 0 and cols_j > 0).  out: batch x nr x nc complex.
+template <typename T>
+int grad_batch(const double *mats, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols, int64_t batch,
+               Precision prec, T *out) {
+    if (nr < 0 || nc < 0 || batch < 0 || !out || (batch * nr * nc > 0 && !mats) || (batch * nr > 0 && !rows) ||
+        (batch * nc > 0 && !cols))
+        return fail(PQG_ERR_INVALID, "invalid arguments");
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    const size_t per = static_cast<size_t>(nr * nc) * 2;
+    std::fill(out, out + per * static_cast<size_t>(batch), T(0));
+    PlanConfig cfg = C.cfg;
+    cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
+    Planner pl(prec, Form::LAPLACE, cfg);
+    pl.set_matrix(mats, batch * nr, nc);
+    struct Minor {
+        int64_t b, i;
+    };
+    std::vector<Minor> minors;
+    std::vector<int32_t> r2(static_cast<size_t>(nr));
+    for (int64_t b = 0; b < batch; ++b) {
+        const int32_t *rb = rows + b * nr, *cb = cols + b * nc;
+        int64_t sr = 0, sc = 0, i_any = -1, j_any = -1;
+        for (int64_t i = 0; i < nr; ++i) {
+            if (rb[i] < 0) return fail(PQG_ERR_INVALID, "row multiplicities must be nonnegative");
+            sr += rb[i];
+            if (rb[i] > 0) i_any = i;
+        }
+        for (int64_t j = 0; j < nc; ++j) {
+            if (cb[j] < 0) return fail(PQG_ERR_INVALID, "column multiplicities must be nonnegative");
+            sc += cb[j];
+            if (cb[j] > 0) j_any = j;
+        }
+        if (i_any < 0 || j_any < 0) continue;  // every entry is 0
+        if (sr != sc) {
+            std::string msg = "Number of input and output states should be equal";
+            return fail(PQG_ERR_SUM_MISMATCH, batch > 1 ? "matrix " + std::to_string(b) + ": " + msg : msg);
+        }
+        if (sr == 1) {  // the single minor is the empty matrix: perm = 1
+            out[static_cast<size_t>(b) * per + 2 * (i_any * nc + j_any)] = T(1);
+            continue;
+        }
+        for (int64_t i = 0; i < nr; ++i) {
+            if (rb[i] == 0) continue;
+            std::copy(rb, rb + nr, r2.begin());
+            r2[i] -= 1;
+            std::string err;
+            int st = pl.add(r2.data(), cb, err, b * nr, nr);
+            if (st) return fail(st, batch > 1 ? "matrix " + std::to_string(b) + ": " + err : err);
+            minors.push_back({b, i});
+        }
+    }
+    if (minors.empty()) return PQG_OK;
+    int st = C.init();
+    if (st) return st;
+    cfg.num_sms = C.cfg.num_sms;
+    pl.set_config(cfg);
+    pl.finish();
+    std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
+    st = run_plan<T>(C, pl, res.data(), nullptr);
+    if (st) return st;
+    for (size_t q = 0; q < minors.size(); ++q) {
+        const Minor &mi = minors[q];
+        const PendingProblem &pp = pl.pending[q];
+        const int64_t oi = pl.probs[q].out_index;
+        const int32_t *rb = rows + mi.b * nr, *cb = cols + mi.b * nc;
+        T *o = out + static_cast<size_t>(mi.b) * per + 2 * mi.i * nc;
+        for (int64_t j = 0; j < nc; ++j) {
+            if (cb[j] == 0) continue;
+            const double f = static_cast<double>(rb[mi.i]) * static_cast<double>(cb[j]);
+            const int slot = pp.out_map[static_cast<size_t>(j)];
+            o[2 * j] = static_cast<T>(f * static_cast<double>(res[2 * (oi + slot)]));
+            o[2 * j + 1] = static_cast<T>(f * static_cast<double>(res[2 * (oi + slot) + 1]));
+        }
+    }
+    return PQG_OK;
+}
+
 template <typename T>
 int laplace_one(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
                 Precision prec, T *out, int64_t *n_out) {
@@ -592,6 +679,19 @@ int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return laplace_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out, n_out);
+}
+
+int pqg_permanent_grad_c128(const double *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                            const int32_t *cols, int64_t batch, double *out) {
+    return grad_batch<double>(matrices, n_rows, n_cols, rows, cols, batch, Precision::C128, out);
+}
+
+int pqg_permanent_grad_c64(const float *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                           const int32_t *cols, int64_t batch, float *out) {
+    if (n_rows < 0 || n_cols < 0 || batch < 0 || (batch * n_rows * n_cols > 0 && !matrices))
+        return fail(PQG_ERR_INVALID, "invalid arguments");
+    std::vector<double> m = widen(matrices, 2 * batch * n_rows * n_cols);
+    return grad_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out);
 }
 
 int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) {

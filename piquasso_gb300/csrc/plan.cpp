@@ -49,10 +49,12 @@ void Planner::set_matrix(const double *a, int64_t nr, int64_t nc) {
     int_nc_ = nc;
 }
 
-int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err) {
-    const int64_t nr = int_nr_, nc = int_nc_;
+int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int64_t row_base,
+                 int64_t n_rows_local) {
+    const int64_t nr = n_rows_local >= 0 ? n_rows_local : int_nr_, nc = int_nc_;
     PendingProblem p;
-    if (nr < 0 || nc < 0 || (nr > 0 && nc > 0 && a_ == nullptr) || (nr > 0 && !rows) || (nc > 0 && !cols)) {
+    if (nr < 0 || nc < 0 || (nr > 0 && nc > 0 && a_ == nullptr) || (nr > 0 && !rows) || (nc > 0 && !cols) ||
+        row_base < 0 || row_base + nr > int_nr_) {
         err = "invalid matrix or multiplicity buffers";
         return 2;
     }
@@ -96,7 +98,7 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err) {
         err = "too many particles";
         return 3;
     }
-    if (nr > (1 << 30) || nc > (1 << 30)) {
+    if (int_nr_ > (1 << 30) || nc > (1 << 30)) {
         err = "matrix dimension above 2^30";
         return 3;
     }
@@ -141,13 +143,13 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err) {
             min_idx = i;
         }
     }
-    p.row0 = static_cast<int>(min_idx);
+    p.row0 = static_cast<int>(row_base + min_idx);
     double S = 1.0;
     for (int64_t i = 0; i < nr; ++i) {
         int m = rows[i] - (i == min_idx ? 1 : 0);
         if (m <= 0) continue;
         p.m.push_back(m);
-        p.row.push_back(static_cast<int>(i));
+        p.row.push_back(static_cast<int>(row_base + i));
         S *= (m + 1);
     }
     if (S > std::ldexp(1.0, 50)) {

@@ -55,8 +55,11 @@ class Planner {
     void set_matrix(const double *a, int64_t nr, int64_t nc);
 
     // Adds one problem over the plan's matrix.  Returns PQG_OK or an error
-    // status with `err` set.
-    int add(const int32_t *rows, const int32_t *cols, std::string &err);
+    // status with `err` set.  `rows` has one multiplicity per matrix row; or,
+    // with n_rows_local >= 0, one per row of the n_rows_local-row block that
+    // starts at matrix row row_base (problems over a stack of matrices).
+    int add(const int32_t *rows, const int32_t *cols, std::string &err, int64_t row_base = 0,
+            int64_t n_rows_local = -1);
 
     // Fixes every problem's split and lays out the arena and the per-problem
     // device data.

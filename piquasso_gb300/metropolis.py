@@ -9,8 +9,9 @@ accepts y over the chain state x with probability
 
 (the output probability of ideal boson sampling with single-photon inputs,
 as in the reference's passive/utils.py:131-138 and probabilities.py:26-54).
-The target probabilities come from ONE batched complex64 permanent launch per
-step (FP32 products with FP64-class seeds and double-double sums).  Patterns
+The target probabilities come from one batched complex64 permanent launch per
+block of steps (FP32 products with FP64-class seeds and double-double sums),
+overlapped with the drawing of the next block (see run_chains).  Patterns
 with a mode holding more than 7 photons cannot be proposed: the chain samples
 the target restricted to occupations <= 7, whose distance from the exact
 distribution the two-mode-marginal TVD against the exact marginals measures.
@@ -109,45 +110,81 @@ def log_target(U64, patterns, inp):
 
 
 def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, seed=0, baseline=False,
-               record=True):
+               record=True, block=8):
     """Runs `chains` independent chains for `steps` steps; returns a dict with
-    the recorded states (after burn-in), acceptance rate and timings."""
+    the recorded states (after burn-in), acceptance rate and timings.
+
+    An independence proposal does not depend on the chain state, so the
+    proposals of `block` consecutive steps are drawn as one batch of
+    chains * block patterns and their target probabilities are one batched
+    permanent launch.  That launch runs on a worker thread (the engine call
+    releases the GIL) while the next block is drawn on the device; the
+    accept/reject pass then walks the block's steps in order, exactly as a
+    step-by-step chain would.  Proposal 0 of every chain is its initial state."""
     import torch
+    from concurrent.futures import ThreadPoolExecutor
 
     inp = np.asarray(input_photons, dtype=int)
     U = np.asarray(U, dtype=np.complex128)
     U64 = U.astype(np.complex64)
+    d = len(inp)
+    block = max(1, int(block))
     stats = ModeStats(U, inp)
-    sampler = ProposalSampler(mlp, stats, chains, baseline=baseline)
+    sampler = ProposalSampler(mlp, stats, chains * block, baseline=baseline)
     rng = np.random.default_rng(seed)
+    n_blocks = (steps + 1 + block - 1) // block
+    t_prop = 0.0
+    t_perm = [0.0]
+
+    def draw(k):
+        y_d, lq_d = sampler.propose(seed * 1000003 + 1 + k)
+        y = y_d.cpu().numpy().astype(np.int64).reshape(block, chains, d)
+        return y, lq_d.cpu().numpy().astype(np.float64).reshape(block, chains)
+
+    def target(Y):
+        t = time.perf_counter()
+        lp = log_target(U64, Y.reshape(-1, d), inp).reshape(block, chains)
+        t_perm[0] += time.perf_counter() - t
+        return lp
+
     t0 = time.perf_counter()
-    y, lq = sampler.propose(seed * 1000003 + 1)
-    x = y.cpu().numpy().astype(np.int64)
-    logq_x = lq.cpu().numpy().astype(np.float64)
-    logp_x = log_target(U64, x, inp)
     accepted = 0
     proposals = 0
     kept = []
-    t_prop = t_perm = 0.0
-    for step in range(steps):
+    x = logp_x = logq_x = None
+    with ThreadPoolExecutor(max_workers=1) as ex:
         ta = time.perf_counter()
-        y_d, lq_d = sampler.propose(seed * 1000003 + 2 + step)
-        y = y_d.cpu().numpy().astype(np.int64)
-        logq_y = lq_d.cpu().numpy().astype(np.float64)
-        tb = time.perf_counter()
-        logp_y = log_target(U64, y, inp)
-        tc = time.perf_counter()
-        t_prop += tb - ta
-        t_perm += tc - tb
-        log_alpha = (logp_y - logp_x) - (logq_y - logq_x)
-        acc = np.log(rng.random(chains)) < log_alpha
-        x[acc] = y[acc]
-        logp_x[acc] = logp_y[acc]
-        logq_x[acc] = logq_y[acc]
-        accepted += int(acc.sum())
-        proposals += chains
-        if record and step >= burn_in:
-            kept.append(x.copy())
+        Y, LQ = draw(0)
+        t_prop += time.perf_counter() - ta
+        fut = ex.submit(target, Y)
+        for k in range(n_blocks):
+            nxt = None
+            if k + 1 < n_blocks:
+                ta = time.perf_counter()
+                nxt = draw(k + 1)  # overlaps the worker's permanents of block k
+                t_prop += time.perf_counter() - ta
+            LP = fut.result()
+            if nxt is not None:
+                fut = ex.submit(target, nxt[0])
+            for s in range(block):
+                g = k * block + s  # proposal index; 0 is the initial state
+                if g > steps:
+                    break
+                if g == 0:
+                    x, logp_x, logq_x = Y[0].copy(), LP[0].copy(), LQ[0].copy()
+                    continue
+                y, logp_y, logq_y = Y[s], LP[s], LQ[s]
+                log_alpha = (logp_y - logp_x) - (logq_y - logq_x)
+                acc = np.log(rng.random(chains)) < log_alpha
+                x[acc] = y[acc]
+                logp_x[acc] = logp_y[acc]
+                logq_x[acc] = logq_y[acc]
+                accepted += int(acc.sum())
+                proposals += chains
+                if record and g - 1 >= burn_in:
+                    kept.append(x.copy())
+            if nxt is not None:
+                Y, LQ = nxt
     torch.cuda.synchronize()
     total = time.perf_counter() - t0
     out = {
@@ -156,7 +193,8 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
         "seconds": total,
         "samples_per_s": proposals / total,
         "propose_s": t_prop,
-        "target_s": t_perm,
+        "target_s": t_perm[0],
+        "block": block,
     }
     if record:
         out["samples"] = np.concatenate(kept) if kept else np.zeros((0, len(inp)), dtype=np.int64)
@@ -164,7 +202,7 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
 
 
 def evaluate(U, input_photons, mlp=None, chains=1024, steps=300, burn_in=30, seed=0, baseline=False, pairs=None,
-             pair_seed=0, n_pairs=16):
+             pair_seed=0, n_pairs=16, block=8):
     """Samples/s, acceptance and two-mode-marginal TVD (mean and max over
     `pairs`, default `n_pairs` random mode pairs) of one Metropolis run."""
     from .marginals import tvd_two_mode
@@ -175,7 +213,7 @@ def evaluate(U, input_photons, mlp=None, chains=1024, steps=300, burn_in=30, see
         allp = [(a, b) for a in range(d) for b in range(a + 1, d)]
         pairs = [allp[i] for i in rng.choice(len(allp), size=min(n_pairs, len(allp)), replace=False)]
     out = run_chains(U, input_photons, mlp=mlp, chains=chains, steps=steps, burn_in=burn_in, seed=seed,
-                     baseline=baseline)
+                     baseline=baseline, block=block)
     tv = tvd_two_mode(out.pop("samples"), input_photons, U, pairs)
     out.update({"tvd_mean": float(tv.mean()), "tvd_max": float(tv.max()), "pairs": [list(p) for p in pairs],
                 "kept_samples": chains * max(0, steps - burn_in)})

@@ -230,3 +230,43 @@ def permanent_laplace_batch(matrix, rows, cols):
         _raise_for(st)
     o = out.reshape(batch, nc, 2)
     return (o[..., 0] + 1j * o[..., 1]).astype(np.complex64 if single else np.complex128)
+
+
+def permanent_grad(matrix, rows, cols):
+    """Gradient of ``permanent(matrix, rows, cols)`` with respect to every
+    matrix entry: G[i, j] = rows[i] * cols[j] * permanent(matrix, rows - e_i,
+    cols - e_j), zero where rows[i] or cols[j] is zero — the reference's
+    grad_perm (src/permanent.cpp:271-300), i.e. the holomorphic derivative that
+    its JAX ``perm`` returns from ``jax.grad(perm, holomorphic=True)``.
+
+    ``matrix`` may carry leading batch dimensions (..., n_rows, n_cols), with
+    ``rows`` (..., n_rows) and ``cols`` (..., n_cols) broadcast against them,
+    as the reference's PermBwd FFI target (src/jax_perm/jax_perm_core.cpp:
+    159-208).  One batched Laplace walk computes every matrix's rows at once.
+    Returns an array of the matrix's shape and complex dtype.
+    """
+    a = np.asarray(matrix)
+    if a.ndim < 2:
+        raise PermanentInputError("matrix must be at least two-dimensional, got shape %s" % (a.shape,))
+    nr, nc = a.shape[-2], a.shape[-1]
+    lead = a.shape[:-2]
+    batch = int(np.prod(lead)) if lead else 1
+    m = _as_matrix(a.reshape(batch * nr, nc)).reshape(batch, nr, nc)
+    R = np.ascontiguousarray(np.broadcast_to(np.asarray(rows).astype(np.int32, casting="unsafe"),
+                                             lead + (nr,)).reshape(batch, nr))
+    C = np.ascontiguousarray(np.broadcast_to(np.asarray(cols).astype(np.int32, casting="unsafe"),
+                                             lead + (nc,)).reshape(batch, nc))
+    m = np.ascontiguousarray(m)
+    L = _lib.load()
+    single = m.dtype == np.complex64
+    out = np.zeros(2 * batch * nr * nc, dtype=np.float32 if single else np.float64)
+    if single:
+        st = L.pqg_permanent_grad_c64(_ptr(m, ctypes.c_float), nr, nc, _ptr(R, ctypes.c_int32),
+                                      _ptr(C, ctypes.c_int32), batch, _ptr(out, ctypes.c_float))
+    else:
+        st = L.pqg_permanent_grad_c128(_ptr(m, ctypes.c_double), nr, nc, _ptr(R, ctypes.c_int32),
+                                       _ptr(C, ctypes.c_int32), batch, _ptr(out, ctypes.c_double))
+    if st:
+        _raise_for(st)
+    g = (out[0::2] + 1j * out[1::2]).astype(np.complex64 if single else np.complex128)
+    return g.reshape(lead + (nr, nc))

@@ -20,6 +20,12 @@ been compiled by oracle/build_ref.sh.  Outputs (JSON, complex numbers as
   (complex128 and complex64) with the reference module's outputs.
 * ``config_14.json`` — the 14x14 parity cases: leading 14x14 block of a seeded
   28x28 Haar unitary, all-ones multiplicities and a repeated-row case.
+* ``grad_cases.json`` — every gradient the reference's own
+  tests/jax_extensions/test_permanent_grad.py asks for through
+  ``jax.grad(perm, holomorphic=True)``, answered by oracle.grad_perm over the
+  reference module's permanent and checked by those tests' own golden
+  assertions (the parts that need jax.jacobian are not run: jax is not
+  installed), plus seeded random cases (repeated rows and columns, non-square).
 
 Usage: python tests/golden/make_golden.py
 """
@@ -241,6 +247,55 @@ def gen_config14(ref):
     return {"haar_seed": 0, "haar_dim": 28, "cases": cases}
 
 
+class _JacobianSkipped(Exception):
+    pass
+
+
+def gen_grad_cases(ref):
+    calls = []
+
+    def grad(fn, holomorphic=False):
+        assert holomorphic
+
+        def g(A, rows, cols):
+            A = np.asarray(A, dtype=np.complex128)
+            rows = np.asarray(rows).astype(np.int64)
+            cols = np.asarray(cols).astype(np.int64)
+            G = oracle.grad_perm(A, rows, cols, perm=lambda M, r, c: ref.permanent(M, rows=r, cols=c))
+            calls.append({"test": sys._getframe(1).f_code.co_name, "matrix": mat(A), "rows": rows.tolist(),
+                          "cols": cols.tolist(), "grad": mat(G)})
+            return G
+        return g
+
+    def jacobian(*a, **k):
+        raise _JacobianSkipped()
+
+    jax_stub = types.SimpleNamespace(grad=grad, jacobian=jacobian,
+                                     numpy=types.SimpleNamespace(array=np.array, uint64=np.uint64,
+                                                                 complex128=np.complex128))
+    ran, skipped = run_test_module(os.path.join(REF, "tests/jax_extensions/test_permanent_grad.py"), "perm",
+                                   None, {"pytest": _PytestStub, "jax": jax_stub})
+    # a test that reached jax.jacobian passed every golden assertion before it
+    # (only tests that asked for a gradient count: the others check nothing here)
+    asked = {c["test"] for c in calls}
+    golden = [t for t in ran + [t.split(" ")[0] for t in skipped if "_JacobianSkipped" in t] if t in asked]
+    skipped = [t for t in skipped if "_JacobianSkipped" not in t] + sorted(
+        set(ran + [t.split(" ")[0] for t in skipped]) - asked)
+    rng = np.random.default_rng(77)
+    rand = []
+    for t in range(24):
+        nr = int(rng.integers(1, 6))
+        nc = int(rng.integers(1, 6))
+        n = int(rng.integers(1, 8))
+        rows = np.bincount(rng.integers(0, nr, n), minlength=nr)
+        cols = np.bincount(rng.integers(0, nc, n), minlength=nc)
+        A = rng.normal(size=(nr, nc)) + 1j * rng.normal(size=(nr, nc))
+        G = oracle.grad_perm(A, rows, cols, perm=lambda M, r, c: ref.permanent(M, rows=r, cols=c))
+        rand.append({"matrix": mat(A), "rows": rows.tolist(), "cols": cols.tolist(), "grad": mat(G)})
+    return {"source": "tests/jax_extensions/test_permanent_grad.py", "tests_golden_checked": golden,
+            "tests_skipped": skipped, "calls": calls, "random": rand}
+
+
 def main():
     oracle.build.build()
     ref = oracle.reference_module()
@@ -252,6 +307,7 @@ def main():
         "sampler_seeded.json": gen_sampler(ref),
         "random_cases.json": gen_random(ref),
         "config_14.json": gen_config14(ref),
+        "grad_cases.json": gen_grad_cases(ref),
     }
     for name, obj in outputs.items():
         with open(os.path.join(HERE, name), "w") as f:
@@ -259,6 +315,8 @@ def main():
         extra = ""
         if "tests_run" in obj:
             extra = " ran=%d skipped=%s" % (len(obj["tests_run"]), obj["tests_skipped"])
+        if "tests_golden_checked" in obj:
+            extra = " golden=%s skipped=%s" % (obj["tests_golden_checked"], obj["tests_skipped"])
         print("wrote", name, extra)
 
 
