@@ -36,6 +36,7 @@ struct ArF64 {
     static constexpr bool kDfSeed = false;
     static constexpr bool kTwoChains = false;  // FP64-pipe bound: one chain
     static constexpr bool kPairSteps = false;
+    static constexpr bool kTwoSeeds = false;
     __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {r, i}; }
     __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r.hi, i.hi}; }
     __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
@@ -67,7 +68,12 @@ struct ArF32 {
     };
     static constexpr bool kDfSeed = true;
     static constexpr bool kTwoChains = true;
-    static constexpr bool kPairSteps = true;  // latency bound: two codes per iteration
+    // latency bound on the prefix-table loads: each lane walks two outer
+    // positions against every loaded table row (half the loads per product,
+    // four independent multiply chains); a lane's odd last position walks
+    // alone, two codes per iteration
+    static constexpr bool kPairSteps = true;
+    static constexpr bool kTwoSeeds = true;
     __device__ __forceinline__ static cs_t from_seed64(double r, double i) {
         return {__double2float_rn(r), __double2float_rn(i)};
     }
@@ -106,6 +112,7 @@ struct ArDF {
     static constexpr bool kDfSeed = true;
     static constexpr bool kTwoChains = true;
     static constexpr bool kPairSteps = false;  // enough independent work per code already
+    static constexpr bool kTwoSeeds = false;   // FMA-pipe bound; its seeds need the registers
     __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {df_split(r), df_split(i)}; }
     __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r, i}; }
     __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
@@ -287,6 +294,74 @@ __device__ __forceinline__ typename Ar::cs_t row_product(const typename Ar::cs_t
     return x;
 }
 
+// The products of two seeds (two outer positions) against one prefix-table
+// row: every table value is loaded once and feeds both column sums.  Each
+// seed's product runs as two chains (even and odd columns), so four
+// independent multiply chains hide the FP32 latency.
+template <class Ar, int NC>
+__device__ __forceinline__ void row_product2(const typename Ar::cs_t (&sa)[NC], const typename Ar::cs_t (&sb)[NC],
+                                             const typename Ar::d_t *__restrict__ d,
+                                             const uint8_t *__restrict__ cm, bool ones, typename Ar::cs_t &xa,
+                                             typename Ar::cs_t &xb) {
+    using cs_t = typename Ar::cs_t;
+    using d_t = typename Ar::d_t;
+    constexpr bool two = NC >= 4;
+    const d_t d0 = d[0];
+    const cs_t a0 = Ar::sum(sa[0], d0), b0 = Ar::sum(sb[0], d0);
+    cs_t ax = a0, bx = b0, ay, by;
+    if constexpr (two) {
+        const d_t d1 = d[1];
+        ay = Ar::sum(sa[1], d1);
+        by = Ar::sum(sb[1], d1);
+    }
+    if (ones) {
+#pragma unroll
+        for (int j = two ? 2 : 1; j < NC; ++j) {
+            const d_t dj = d[j];
+            const cs_t ca = Ar::sum(sa[j], dj), cb = Ar::sum(sb[j], dj);
+            if (two && (j & 1)) {
+                Ar::mul(ay, ca);
+                Ar::mul(by, cb);
+            } else {
+                Ar::mul(ax, ca);
+                Ar::mul(bx, cb);
+            }
+        }
+    } else {
+        for (int r = 1; r < cm[0]; ++r) {
+            Ar::mul(ax, a0);
+            Ar::mul(bx, b0);
+        }
+        if constexpr (two) {
+            const cs_t a1 = ay, b1 = by;
+            for (int r = 1; r < cm[1]; ++r) {
+                Ar::mul(ay, a1);
+                Ar::mul(by, b1);
+            }
+        }
+#pragma unroll
+        for (int j = two ? 2 : 1; j < NC; ++j) {
+            const d_t dj = d[j];
+            const cs_t ca = Ar::sum(sa[j], dj), cb = Ar::sum(sb[j], dj);
+            for (int r = 0; r < cm[j]; ++r) {
+                if (two && (j & 1)) {
+                    Ar::mul(ay, ca);
+                    Ar::mul(by, cb);
+                } else {
+                    Ar::mul(ax, ca);
+                    Ar::mul(bx, cb);
+                }
+            }
+        }
+    }
+    if constexpr (two) {
+        Ar::mul(ax, ay);
+        Ar::mul(bx, by);
+    }
+    xa = ax;
+    xb = bx;
+}
+
 // Blocks per SM the register allocation must allow: the column sums of the
 // wider kernels need up to 255 registers per thread, and a spill inside the
 // step loop costs more than the occupancy it buys.
@@ -327,7 +402,47 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
             // lanes of a problem's last item may own fewer positions and stop
             // early; inner walks never synchronise across lanes
             const int64_t my_R = (Q - r0 < R) ? (Q - r0) : R;
-            for (int64_t seg = 0; seg < my_R; ++seg) {
+            int64_t seg = 0;
+            if constexpr (Ar::kTwoSeeds) {
+                // positions in pairs (seg, seg+1): seed_b is seed one outer
+                // step on, and both walk the inner codes forward (the column
+                // sums are seed + Delta(t), so the walk order is free)
+                for (; seg + 1 < my_R; seg += 2) {
+                    cs_t sb[NC];
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) sb[j] = seed[j];
+                    {
+                        bool up = false;
+                        const int k = outer_next(pr, st, &up);
+                        const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                        for (int j = 0; j < NC; ++j) Ar::update(sb[j], d[j]);
+                    }
+                    const double wb = outer_weight(pr, st);
+                    typename Ar::acc_t acc_a = Ar::zero(), acc_b = Ar::zero();
+                    for (int t = 0; t < P; ++t) {
+                        cs_t xa, xb;
+                        row_product2<Ar, NC>(seed, sb, delta + static_cast<int64_t>(t) * NC, cm, ones, xa, xb);
+                        const PqgStep w = tab[t];
+                        Ar::accumulate(acc_a, xa, w);
+                        Ar::accumulate(acc_b, xb, w);
+                    }
+                    Ar::fold(sr, si, acc_a, wout);
+                    Ar::fold(sr, si, acc_b, wb);
+                    if (seg + 2 < my_R) {  // seed moves on to position seg + 2
+                        bool up = false;
+                        const int k = outer_next(pr, st, &up);
+                        const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                        for (int j = 0; j < NC; ++j) {
+                            seed[j] = sb[j];
+                            Ar::update(seed[j], d[j]);
+                        }
+                        wout = outer_weight(pr, st);
+                    }
+                }
+            }
+            for (; seg < my_R; ++seg) {
                 typename Ar::acc_t acc = Ar::zero();
                 // inner codes in walk order: t = s (forward) or P-1-s (backward);
                 // FP32-pipe walks take two codes per iteration (independent
