@@ -163,25 +163,33 @@ int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *f
  * `stream` is a cudaStream_t (NULL: legacy default stream); the calls enqueue
  * and return.
  *
- * pqg_mlp_gemm: C[M x N] = sum_k A(m,k) B(k,n) in BF16 tensor-core MMAs with
- * FP32 accumulation; A(m,k) = a[m*a_s_row + k*a_s_col] (BF16 if a_bf16, else
- * FP32, rounded to BF16 on load), likewise B.  epilogue 0: C = acc (FP32);
- * 1: C = acc + bias (pre-activation), act_bf16 = GELU(C); 2: split-K over
- * `splits` ranges of K through `splitk_scratch` (splits*M*N floats), then a
- * fixed-order sum into C (weight gradients); 3: C = acc + bias.
- * pqg_mlp_gelu_backward: d *= GELU'(pre).  pqg_mlp_bias_grad: db = column
- * sums of d (M x N).  pqg_mlp_softmax_xent: per row m, softmax over classes
- * lo[m]..hi[m] of logits (row stride ld), loss = -log p(target), dlogits =
- * (p - onehot) * scale.  pqg_mlp_adam: one Adam step on FP32 weights (and
- * their BF16 copy, nullable), bias-corrected with `step`. */
-int pqg_mlp_gemm(const void *a, int32_t a_bf16, int64_t a_s_row, int64_t a_s_col, const void *b, int32_t b_bf16,
-                 int64_t b_s_row, int64_t b_s_col, int64_t M, int64_t N, int64_t K, int32_t epilogue, float *c,
-                 void *act_bf16, const float *bias, float *splitk_scratch, int32_t splits, void *stream);
-int pqg_mlp_gelu_backward(float *d, const float *pre, int64_t n, void *stream);
+ * pqg_mlp_gemm_tc: C[M x N] = A[M x K] . B[N x K]^T with BF16 operands, both
+ * row-major with K contiguous (row strides lda, ldb >= K, multiples of 8;
+ * 16-byte aligned base pointers), FP32 accumulation on the tcgen05 tensor
+ * cores (TMA-staged operands, TMEM accumulator).  epilogue 0: C = acc; 1: C =
+ * acc + bias (pre-activation), c_bf16 = GELU(C); 2: split-K over `splits`
+ * ranges of K through `splitk_scratch` (splits*M*N floats), then a fixed-order
+ * sum into C (weight gradients); 3: C = acc + bias; 4: C = acc * GELU'(pre)
+ * (pre: M x N FP32), c_bf16 = BF16(C) (backward through the activation).
+ * pqg_mlp_transpose_bf16: dst[c*ld_dst + r] = src[r*ld_src + c] (rows x cols
+ * BF16), the K-major copies of backward operands.  pqg_mlp_tc_status: reads
+ * (and clears) the GEMM's device error code: 0, or the bounded wait that ran
+ * out (1: operand copy, 2: stage release, 3: accumulator); synchronising.
+ * pqg_mlp_bias_grad: db = column sums of d (M x N).  pqg_mlp_softmax_xent:
+ * per row m, softmax over classes lo[m]..hi[m] of logits (row stride ld),
+ * loss = -log p(target), dlogits = (p - onehot) * scale (FP32, and BF16 when
+ * dlogits_bf16 is not NULL).  pqg_mlp_adam: one Adam step on FP32 weights
+ * (and their BF16 copy, nullable), bias-corrected with `step`. */
+int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                    int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
+                    float *splitk_scratch, int32_t splits, void *stream);
+int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
+                           void *stream);
+int pqg_mlp_tc_status(int32_t *code);
 int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, void *stream);
 int pqg_mlp_softmax_xent(const float *logits, int64_t M, int32_t ld, int32_t classes, const int8_t *lo,
                          const int8_t *hi, const int8_t *target, float scale, float *loss, float *dlogits,
-                         void *stream);
+                         void *dlogits_bf16, void *stream);
 int pqg_mlp_adam(float *w, void *w_bf16, const float *g, float *m1, float *m2, int64_t n, float lr, float b1,
                  float b2, float eps, int64_t step, void *stream);
 

@@ -55,12 +55,14 @@ SIGNATURES = {
     "pqg_plan_info": ([ctypes.c_void_p, _d, _d, _i64, _i64], ctypes.c_int),
     "pqg_plan_destroy": ([ctypes.c_void_p], ctypes.c_int),
     "pqg_permanent_unit_c128_noalloc": ([ctypes.c_void_p, _I64, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
-    "pqg_mlp_gemm": ([ctypes.c_void_p, _I32, _I64, _I64, ctypes.c_void_p, _I32, _I64, _I64, _I64, _I64, _I64,
-                      _I32, _f, ctypes.c_void_p, _f, _f, _I32, ctypes.c_void_p], ctypes.c_int),
-    "pqg_mlp_gelu_backward": ([_f, _f, _I64, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_gemm_tc": ([ctypes.c_void_p, _I64, ctypes.c_void_p, _I64, _I64, _I64, _I64, _I32, _f,
+                         ctypes.c_void_p, _f, _f, _f, _I32, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_transpose_bf16": ([ctypes.c_void_p, _I64, _I64, _I64, ctypes.c_void_p, _I64, ctypes.c_void_p],
+                               ctypes.c_int),
+    "pqg_mlp_tc_status": ([_i32], ctypes.c_int),
     "pqg_mlp_bias_grad": ([_f, _I64, _I64, _f, ctypes.c_void_p], ctypes.c_int),
-    "pqg_mlp_softmax_xent": ([_f, _I64, _I32, _I32, _i8, _i8, _i8, ctypes.c_float, _f, _f, ctypes.c_void_p],
-                             ctypes.c_int),
+    "pqg_mlp_softmax_xent": ([_f, _I64, _I32, _I32, _i8, _i8, _i8, ctypes.c_float, _f, _f, ctypes.c_void_p,
+                              ctypes.c_void_p], ctypes.c_int),
     "pqg_mlp_adam": ([_f, ctypes.c_void_p, _f, _f, _f, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                       ctypes.c_float, _I64, ctypes.c_void_p], ctypes.c_int),
     "pqg_proposal_features": ([_I32, _I32, _I32, _I32, _f, _i32, _f, ctypes.c_void_p, _i8, _i8, ctypes.c_void_p],

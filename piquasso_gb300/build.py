@@ -25,6 +25,7 @@ CU_SOURCES = [
     "capi.cu",
     "noalloc.cu",
     "mlp.cu",
+    "mlp_tc.cu",
     "proposal.cu",
     "k_plain_c128_0.cu",
     "k_plain_c128_1.cu",

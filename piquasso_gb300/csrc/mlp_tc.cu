@@ -1,0 +1,465 @@
+// Blackwell (sm_103a) tensor-core GEMM of the learned proposal's MLP:
+//
+//     C[M x N] = A[M x K] . B[N x K]^T        (BF16 operands, FP32 accumulation)
+//
+// with A and B row-major and K contiguous ("K-major"), the one layout every
+// forward and backward GEMM of the network is brought into (backward
+// operands by the transpose kernel below).  One CTA of 128 threads computes a
+// 128 x BN tile (BN = N rounded up to 16, at most 256):
+//   * TMA (cp.async.bulk.tensor.2d) stages 64-wide K chunks of A (128 x 64)
+//     and B (BN x 64) into shared memory with the 128-byte swizzle, two stages
+//     deep, each stage completing on an mbarrier (expect-tx bytes);
+//   * one thread issues tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = BN,
+//     K = 16 per instruction) from shared-memory descriptors, accumulating in
+//     tensor memory (TMEM, BN FP32 columns), and tcgen05.commit releases each
+//     stage back to the TMA producer once its MMAs have read it;
+//   * after a final commit, each warp reads its 32 accumulator rows with
+//     tcgen05.ld (32x32b) and applies the fused epilogue: plain FP32, bias,
+//     bias + GELU (FP32 pre-activation and BF16 activation), GELU backward
+//     (dpre = acc * GELU'(pre), FP32 and BF16), or split-K partial sums.
+// Rows and columns past M, N, K are zero-filled by TMA (out-of-range box
+// elements) and never stored.  Every mbarrier wait is bounded: a wait that
+// runs out records an error code in device memory (pqg_mlp_tc_status) and the
+// CTA still waits for its issued MMAs and frees its TMEM before returning.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/pqperm_gb300.h"
+
+namespace pqg {
+void set_last_error(const char *msg);
+}
+
+namespace {
+
+constexpr int TC_BM = 128;      // UMMA M (cta_group::1)
+constexpr int TC_BK = 64;       // K chunk: one 128-byte swizzle row of BF16
+constexpr int TC_STAGES = 2;
+constexpr int TC_THREADS = 128;
+constexpr uint32_t TC_A_BYTES = TC_BM * TC_BK * 2;  // 16 KB per stage
+constexpr long long TC_WAIT_LIMIT = 1ll << 22;       // try_wait rounds before giving up
+
+enum TcEpilogue : int {
+    TC_EPI_F32 = 0,        // C = acc
+    TC_EPI_BIAS_GELU = 1,  // C = acc + bias (FP32), Cb = GELU(C) (BF16)
+    TC_EPI_SPLITK = 2,     // C[split][m][n] = acc over the split's K range
+    TC_EPI_BIAS_F32 = 3,   // C = acc + bias
+    TC_EPI_DGELU = 4,      // C = acc * GELU'(pre) (FP32), Cb = BF16(C)
+};
+
+__device__ int g_tc_error;  // first failure code (0: none)
+
+struct TcArgs {
+    int64_t M, N, K;
+    int64_t k_per_split;  // multiple of TC_BK
+    float *C;
+    __nv_bfloat16 *Cb;
+    const float *bias;
+    const float *pre;
+    int BN;         // tile columns (UMMA N)
+    int tmem_cols;  // power of two >= max(32, BN)
+    int epi;
+    int pad;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false when it ran out.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (long long i = 0; i < TC_WAIT_LIMIT; ++i) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int32_t x, int32_t y,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile in the 128-byte
+// swizzle layout: rows of 128 bytes, 8-row groups 1024 bytes apart (stride
+// byte offset), the leading byte offset unused (one swizzle atom spans the
+// chunk's K), descriptor version 1, swizzle mode 2 (128 B).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t addr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);
+    d |= static_cast<uint64_t>(1) << 16;
+    d |= static_cast<uint64_t>(1024 >> 4) << 32;
+    d |= static_cast<uint64_t>(1) << 46;
+    d |= static_cast<uint64_t>(2) << 61;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = bn, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16(int bn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(bn >> 3) << 17) |
+           (static_cast<uint32_t>(TC_BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void record_error(int code) { atomicCAS(&g_tc_error, 0, code); }
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+    return cdf + x * pdf;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, TcArgs g) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    // stages at a 1024-byte boundary (the swizzle atom), then the barriers
+    const uint32_t raw = smem_u32(tc_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    const uint32_t b_bytes = static_cast<uint32_t>(g.BN) * TC_BK * 2;
+    const uint32_t stage_bytes = TC_A_BYTES + b_bytes;
+    const uint32_t bar0 = base + TC_STAGES * stage_bytes;  // full[s] at bar0 + 8s, empty[s] at +16+8s, done at +32
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem_raw + (bar0 + 40 - raw));
+    const uint32_t full0 = bar0, empty0 = bar0 + 8 * TC_STAGES, done = bar0 + 16 * TC_STAGES;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t m0 = static_cast<int64_t>(blockIdx.y) * TC_BM, n0 = static_cast<int64_t>(blockIdx.x) * g.BN;
+    const int64_t k_lo = static_cast<int64_t>(blockIdx.z) * g.k_per_split;
+    const int64_t k_hi = k_lo + g.k_per_split < g.K ? k_lo + g.k_per_split : g.K;
+    const int nchunks = static_cast<int>((k_hi - k_lo + TC_BK - 1) / TC_BK);
+
+    if (tid == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0) {
+        const uint32_t idesc = idesc_bf16(g.BN);
+        auto issue = [&](int c) {
+            const int s = c % TC_STAGES;
+            const uint32_t sa = base + s * stage_bytes, sb = sa + TC_A_BYTES;
+            const int32_t kx = static_cast<int32_t>(k_lo + static_cast<int64_t>(c) * TC_BK);  // multiple of 64
+            mbar_expect_tx(full0 + 8 * s, stage_bytes);
+            tma_load_2d(sa, &map_a, kx, static_cast<int32_t>(m0), full0 + 8 * s);
+            tma_load_2d(sb, &map_b, kx, static_cast<int32_t>(n0), full0 + 8 * s);
+        };
+        for (int c = 0; c < TC_STAGES && c < nchunks; ++c) issue(c);
+        bool ok = true;
+        for (int c = 0; c < nchunks && ok; ++c) {
+            const int s = c % TC_STAGES;
+            const uint32_t parity = static_cast<uint32_t>((c / TC_STAGES) & 1);
+            if (!mbar_wait(full0 + 8 * s, parity)) {
+                record_error(1);
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = base + s * stage_bytes, sb = sa + TC_A_BYTES;
+            const int64_t kc = k_hi - (k_lo + static_cast<int64_t>(c) * TC_BK);
+            const int nk = kc >= TC_BK ? TC_BK / 16 : static_cast<int>((kc + 15) / 16);
+            for (int kk = 0; kk < nk; ++kk)
+                umma_bf16(tmem, sdesc_sw128(sa + 32u * kk), sdesc_sw128(sb + 32u * kk), idesc, (c > 0 || kk > 0) ? 1 : 0);
+            umma_commit(empty0 + 8 * s);
+            if (c + TC_STAGES < nchunks) {
+                // the stage is refilled once its MMAs have read it
+                if (!mbar_wait(empty0 + 8 * s, parity)) {
+                    record_error(2);
+                    ok = false;
+                    break;
+                }
+                issue(c + TC_STAGES);
+            }
+        }
+        umma_commit(done);  // arrives when every MMA issued above has completed
+    }
+    __syncwarp();
+    // warp-uniform: the TMEM loads below are .sync.aligned
+    const bool have = __all_sync(0xffffffffu, mbar_wait(done, 0));
+    if (!have && lane == 0) record_error(3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (have) {
+        const int64_t row = m0 + warp * 32 + lane;
+        const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+        float *crow = g.C + (g.epi == TC_EPI_SPLITK ? static_cast<int64_t>(blockIdx.z) * g.M * g.N : 0) + row * g.N;
+        for (int j0 = 0; j0 < g.BN; j0 += 16) {
+            float v[16];
+            tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
+            if (row >= g.M) continue;
+            const int64_t c0 = n0 + j0;
+            const int nq = g.N - c0 < 16 ? static_cast<int>(g.N - c0) : 16;
+            if (nq <= 0) continue;
+            // epilogue values of this thread's 16 columns
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                if (q >= nq) break;
+                float x = v[q];
+                if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) x += g.bias[c0 + q];
+                if (g.epi == TC_EPI_DGELU) x *= gelu_grad(g.pre[row * g.N + c0 + q]);
+                v[q] = x;
+            }
+            const bool vec = nq == 16 && (g.N % 8) == 0;  // 16-byte aligned stores
+            if (vec) {
+                float4 *o = reinterpret_cast<float4 *>(crow + c0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+                for (int q = 0; q < nq; ++q) crow[c0 + q] = v[q];
+            }
+            if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_DGELU) {
+                __nv_bfloat16 *brow = g.Cb + row * g.N + c0;
+                if (vec) {
+                    uint4 w[2];
+                    uint32_t *wp = reinterpret_cast<uint32_t *>(w);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float a = g.epi == TC_EPI_BIAS_GELU ? gelu(v[2 * q]) : v[2 * q];
+                        const float b = g.epi == TC_EPI_BIAS_GELU ? gelu(v[2 * q + 1]) : v[2 * q + 1];
+                        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+                        wp[q] = *reinterpret_cast<uint32_t *>(&h);
+                    }
+                    reinterpret_cast<uint4 *>(brow)[0] = w[0];
+                    reinterpret_cast<uint4 *>(brow)[1] = w[1];
+                } else {
+                    for (int q = 0; q < nq; ++q)
+                        brow[q] = __float2bfloat16(g.epi == TC_EPI_BIAS_GELU ? gelu(v[q]) : v[q]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
+}
+
+// dst[c][r] = src[r][c] for BF16 matrices (32 x 32 tiles through shared memory).
+__global__ void transpose_bf16(const __nv_bfloat16 *__restrict__ src, int64_t rows, int64_t cols, int64_t ld_src,
+                               __nv_bfloat16 *__restrict__ dst, int64_t ld_dst) {
+    __shared__ __nv_bfloat16 t[32][33];
+    const int64_t r0 = static_cast<int64_t>(blockIdx.y) * 32, c0 = static_cast<int64_t>(blockIdx.x) * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t r = r0 + i, c = c0 + threadIdx.x;
+        if (r < rows && c < cols) t[i][threadIdx.x] = src[r * ld_src + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int64_t c = c0 + i, r = r0 + threadIdx.x;
+        if (r < rows && c < cols) dst[c * ld_dst + r] = t[threadIdx.x][i];
+    }
+}
+
+// out[m][n] = sum over splits of part[s][m][n]  (fixed order: deterministic)
+__global__ void tc_splitk_reduce(const float *__restrict__ part, int splits, int64_t MN, float *__restrict__ out) {
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < MN;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float s = 0.0f;
+        for (int k = 0; k < splits; ++k) s += part[k * MN + e];
+        out[e] = s;
+    }
+}
+
+int fail(int code, const char *msg) {
+    pqg::set_last_error(msg);
+    return code;
+}
+
+int fail_cuda(cudaError_t e, const char *what) {
+    char buf[200];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    pqg::set_last_error(buf);
+    return PQG_ERR_CUDA;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// Tensor map of a row-major BF16 matrix [rows x k] with row stride ld
+// (elements), boxes of 64 (K) x box_rows, 128-byte swizzle, zero fill.
+int make_map(CUtensorMap *map, const void *p, int64_t rows, int64_t k, int64_t ld, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return fail(PQG_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(k), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(TC_BK), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(p), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld operand", static_cast<int>(r),
+                 static_cast<long long>(rows), static_cast<long long>(k));
+        return fail(PQG_ERR_INVALID, buf);
+    }
+    return PQG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                    int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
+                    float *splitk_scratch, int32_t splits, void *stream) {
+    if (M <= 0 || N <= 0 || K <= 0 || !a || !b || !c || lda < K || ldb < K || epilogue < 0 || epilogue > 4)
+        return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: invalid arguments");
+    if ((lda % 8) || (ldb % 8) || (reinterpret_cast<uintptr_t>(a) % 16) || (reinterpret_cast<uintptr_t>(b) % 16))
+        return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: operands need 16-byte aligned rows (ld % 8 == 0)");
+    if ((epilogue == TC_EPI_BIAS_GELU || epilogue == TC_EPI_BIAS_F32) && !bias)
+        return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: epilogue needs a bias");
+    if ((epilogue == TC_EPI_BIAS_GELU || epilogue == TC_EPI_DGELU) && !c_bf16)
+        return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: epilogue needs a BF16 output");
+    if (epilogue == TC_EPI_DGELU && !pre) return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: epilogue needs pre");
+    if (M >= (1ll << 31) || N >= (1ll << 31) || K >= (1ll << 31) || (M + TC_BM - 1) / TC_BM > 65535)
+        return fail(PQG_ERR_TOO_LARGE, "pqg_mlp_gemm_tc: dimension too large");
+    TcArgs g{};
+    g.M = M;
+    g.N = N;
+    g.K = K;
+    g.C = c;
+    g.Cb = static_cast<__nv_bfloat16 *>(c_bf16);
+    g.bias = bias;
+    g.pre = pre;
+    g.epi = epilogue;
+    g.BN = static_cast<int>(((N < 256 ? N : 256) + 15) / 16 * 16);
+    g.tmem_cols = 32;
+    while (g.tmem_cols < g.BN) g.tmem_cols *= 2;
+    int nsplit = 1;
+    g.k_per_split = (K + TC_BK - 1) / TC_BK * TC_BK;
+    if (epilogue == TC_EPI_SPLITK) {
+        if (splits < 1 || !splitk_scratch)
+            return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: split-K needs splits >= 1 and a scratch buffer");
+        int64_t kps = (K + splits - 1) / splits;
+        kps = (kps + TC_BK - 1) / TC_BK * TC_BK;
+        g.k_per_split = kps;
+        nsplit = static_cast<int>((K + kps - 1) / kps);
+        g.C = splitk_scratch;
+    }
+    CUtensorMap ma, mb;
+    int st = make_map(&ma, a, M, K, lda, TC_BM);
+    if (st) return st;
+    st = make_map(&mb, b, N, K, ldb, g.BN);
+    if (st) return st;
+    // shared memory: two stages, the barriers, and the slack that aligns the
+    // stages to 1024 bytes; a CTA holding 256 TMEM columns asks for enough
+    // shared memory that at most two share an SM (512 columns)
+    size_t smem = 1024 + TC_STAGES * (static_cast<size_t>(TC_A_BYTES) + static_cast<size_t>(g.BN) * TC_BK * 2) + 64;
+    if (g.tmem_cols > 128 && smem < 80 * 1024) smem = 80 * 1024;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        attr_err = cudaFuncSetAttribute(gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    if (attr_err != cudaSuccess) return fail_cuda(attr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    dim3 grid(static_cast<unsigned>((N + g.BN - 1) / g.BN), static_cast<unsigned>((M + TC_BM - 1) / TC_BM),
+              static_cast<unsigned>(nsplit));
+    gemm_tc<<<grid, TC_THREADS, smem, s>>>(ma, mb, g);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc");
+    if (epilogue == TC_EPI_SPLITK) {
+        tc_splitk_reduce<<<256, 256, 0, s>>>(splitk_scratch, nsplit, M * N, c);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc (split-K reduction)");
+    }
+    return PQG_OK;
+}
+
+int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
+                           void *stream) {
+    if (rows <= 0 || cols <= 0 || !src || !dst || ld_src < cols || ld_dst < rows)
+        return fail(PQG_ERR_INVALID, "pqg_mlp_transpose_bf16: invalid arguments");
+    dim3 grid(static_cast<unsigned>((cols + 31) / 32), static_cast<unsigned>((rows + 31) / 32));
+    transpose_bf16<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(src), rows, cols, ld_src, static_cast<__nv_bfloat16 *>(dst), ld_dst);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_transpose_bf16");
+}
+
+int pqg_mlp_tc_status(int32_t *code) {
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(int));
+    if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_tc_status");
+    if (code) *code = v;
+    if (v) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(int));
+        if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_tc_status");
+    }
+    return PQG_OK;
+}
+
+}  // extern "C"

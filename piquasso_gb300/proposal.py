@@ -111,7 +111,13 @@ def _ptr(t):
 
 
 class MLP:
-    """Weights and the forward/backward passes on the engine's BF16 kernels."""
+    """Weights and the forward/backward passes on the engine's kernels.
+
+    Every GEMM is C = A . B^T with both operands BF16 and K-major, on the
+    tcgen05 kernel (pqg_mlp_gemm_tc): the forward pass reads the BF16 weights
+    transposed (WbT[i], fan_out x fan_in), the data gradient reads them as
+    stored (Wb[i]), and the weight gradient reads transposed copies of the
+    activations and of the output gradient (pqg_mlp_transpose_bf16)."""
 
     def __init__(self, seed=0, device="cuda"):
         import torch
@@ -119,7 +125,7 @@ class MLP:
         self.torch = torch
         g = torch.Generator().manual_seed(seed)
         dims = [(F, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, HIDDEN), (HIDDEN, LD)]
-        self.W, self.Wb, self.b, self.mW, self.vW, self.mb, self.vb = [], [], [], [], [], [], []
+        self.W, self.Wb, self.WbT, self.b, self.mW, self.vW, self.mb, self.vb = [], [], [], [], [], [], [], []
         for (fi, fo) in dims:
             w = torch.randn(fi, fo, generator=g) * (2.0 / fi) ** 0.5
             if fo == LD:
@@ -127,6 +133,7 @@ class MLP:
             w = w.to(device)
             self.W.append(w)
             self.Wb.append(w.to(torch.bfloat16))
+            self.WbT.append(w.t().contiguous().to(torch.bfloat16))
             self.b.append(torch.zeros(fo, device=device))
             self.mW.append(torch.zeros_like(w))
             self.vW.append(torch.zeros_like(w))
@@ -142,22 +149,43 @@ class MLP:
         torch = self.torch
         for i in range(4):
             self.W[i] = torch.from_numpy(np.asarray(sd["W"][i], dtype=np.float32)).to(self.device)
-            self.Wb[i] = self.W[i].to(torch.bfloat16)
             self.b[i] = torch.from_numpy(np.asarray(sd["b"][i], dtype=np.float32)).to(self.device)
+            self._refresh_bf16(i)
         self.step = int(sd.get("step", 0))
 
+    def _refresh_bf16(self, i):
+        """BF16 copies of W[i]: as stored (Wb) and transposed (WbT)."""
+        torch = self.torch
+        self.Wb[i] = self.W[i].to(torch.bfloat16)
+        fi, fo = self.W[i].shape
+        self.WbT[i] = torch.empty(fo, fi, device=self.device, dtype=torch.bfloat16)
+        self._transpose(self.Wb[i], self.WbT[i])
+
     # ---------------------------------------------------------------- kernels
-    def _gemm(self, A, A_bf16, a_rows, a_cols, B, B_bf16, b_rows, b_cols, M, N, K, epi, C,
-              act=None, bias=None, scratch=None, splits=0, stream=None):
+    def _gemm(self, A, lda, B, ldb, M, N, K, epi, C, Cb=None, bias=None, pre=None, scratch=None, splits=0):
+        """C = A[M x K] . B[N x K]^T (BF16, K-major) with epilogue `epi`."""
         L = _lib.load()
-        st = L.pqg_mlp_gemm(_ptr(A), int(A_bf16), a_rows, a_cols, _ptr(B), int(B_bf16), b_rows, b_cols,
-                            M, N, K, epi, ctypes.cast(C.data_ptr(), ctypes.POINTER(ctypes.c_float)),
-                            _ptr(act) if act is not None else None,
-                            ctypes.cast(bias.data_ptr(), ctypes.POINTER(ctypes.c_float)) if bias is not None else None,
-                            ctypes.cast(scratch.data_ptr(), ctypes.POINTER(ctypes.c_float)) if scratch is not None else None,
-                            int(splits), stream)
+        fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float)) if t is not None else None  # noqa
+        st = L.pqg_mlp_gemm_tc(_ptr(A), lda, _ptr(B), ldb, M, N, K, epi, fp(C), _ptr(Cb) if Cb is not None else None,
+                               fp(bias), fp(pre), fp(scratch), int(splits), None)
         if st:
-            raise RuntimeError("pqg_mlp_gemm failed: " + _lib.last_error())
+            raise RuntimeError("pqg_mlp_gemm_tc failed: " + _lib.last_error())
+
+    def _transpose(self, src, dst):
+        """dst (cols x ld) = src (rows x cols)^T, BF16."""
+        rows, cols = src.shape
+        st = _lib.load().pqg_mlp_transpose_bf16(_ptr(src), rows, cols, src.stride(0), _ptr(dst), dst.stride(0), None)
+        if st:
+            raise RuntimeError("pqg_mlp_transpose_bf16 failed: " + _lib.last_error())
+
+    def _transposed(self, src):
+        """K-major copy of a (M x C) BF16 matrix for a GEMM over M: (C x Mp),
+        rows padded to a multiple of 8 elements (16 bytes)."""
+        M, C = src.shape
+        Mp = (M + 7) // 8 * 8
+        dst = self.torch.empty(C, Mp, device=self.device, dtype=self.torch.bfloat16)
+        self._transpose(src, dst)
+        return dst
 
     def forward(self, Xb, keep=False):
         """Xb: (M, F) bf16 -> logits (M, LD) fp32 (+ activations if keep)."""
@@ -170,12 +198,12 @@ class MLP:
             pre = torch.empty(M, HIDDEN, device=self.device, dtype=torch.float32)
             act = torch.empty(M, HIDDEN, device=self.device, dtype=torch.bfloat16)
             fi = h.shape[1]
-            self._gemm(h, 1, fi, 1, self.Wb[i], 1, HIDDEN, 1, M, HIDDEN, fi, 1, pre, act=act, bias=self.b[i])
+            self._gemm(h, fi, self.WbT[i], fi, M, HIDDEN, fi, 1, pre, Cb=act, bias=self.b[i])
             pres.append(pre)
             acts.append(act)
             h = act
         logits = torch.empty(M, LD, device=self.device, dtype=torch.float32)
-        self._gemm(h, 1, HIDDEN, 1, self.Wb[3], 1, LD, 1, M, LD, HIDDEN, 3, logits, bias=self.b[3])
+        self._gemm(h, HIDDEN, self.WbT[3], HIDDEN, M, LD, HIDDEN, 3, logits, bias=self.b[3])
         if keep:
             return logits, acts, pres
         return logits
@@ -188,24 +216,26 @@ class MLP:
         logits, acts, pres = self.forward(Xb, keep=True)
         loss = torch.empty(M, device=self.device, dtype=torch.float32)
         dz = torch.empty(M, LD, device=self.device, dtype=torch.float32)
+        dzb = torch.empty(M, LD, device=self.device, dtype=torch.bfloat16)
         st = L.pqg_mlp_softmax_xent(ctypes.cast(logits.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, LD, CLASSES,
                                     ctypes.cast(lo.data_ptr(), ctypes.POINTER(ctypes.c_int8)),
                                     ctypes.cast(hi.data_ptr(), ctypes.POINTER(ctypes.c_int8)),
                                     ctypes.cast(target.data_ptr(), ctypes.POINTER(ctypes.c_int8)), 1.0 / M,
                                     ctypes.cast(loss.data_ptr(), ctypes.POINTER(ctypes.c_float)),
-                                    ctypes.cast(dz.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
+                                    ctypes.cast(dz.data_ptr(), ctypes.POINTER(ctypes.c_float)), _ptr(dzb), None)
         if st:
             raise RuntimeError(_lib.last_error())
         grads_W, grads_b = [None] * 4, [None] * 4
-        splits = max(1, min(64, M // 4096))
-        d_out = dz
+        splits = max(1, min(64, M // 1024))
+        d_out, d_out_b = dz, dzb
         for i in (3, 2, 1, 0):
             fi, fo = self.W[i].shape
-            h_in = acts[i]
-            # dW = h_in^T d_out  (K = M, split over the batch)
+            # dW = h_in^T d_out: K = M (split over the batch), both operands transposed to K-major
+            hT = self._transposed(acts[i])
+            dT = self._transposed(d_out_b)
             gW = torch.empty(fi, fo, device=self.device, dtype=torch.float32)
             scratch = torch.empty(splits * fi * fo, device=self.device, dtype=torch.float32)
-            self._gemm(h_in, 1, 1, fi, d_out, 0, fo, 1, fi, fo, M, 2, gW, scratch=scratch, splits=splits)
+            self._gemm(hT, hT.shape[1], dT, dT.shape[1], fi, fo, M, 2, gW, scratch=scratch, splits=splits)
             gb = torch.empty(fo, device=self.device, dtype=torch.float32)
             st = L.pqg_mlp_bias_grad(ctypes.cast(d_out.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, fo,
                                      ctypes.cast(gb.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
@@ -214,15 +244,11 @@ class MLP:
             grads_W[i], grads_b[i] = gW, gb
             if i == 0:
                 break
-            # d h_in = d_out W^T, then through GELU'(pre)
+            # d h_in = d_out W^T, through GELU'(pre) in the epilogue (FP32 and BF16)
             dh = torch.empty(M, fi, device=self.device, dtype=torch.float32)
-            self._gemm(d_out, 0, fo, 1, self.Wb[i], 1, 1, fo, M, fi, fo, 0, dh)
-            st = L.pqg_mlp_gelu_backward(ctypes.cast(dh.data_ptr(), ctypes.POINTER(ctypes.c_float)),
-                                         ctypes.cast(pres[i - 1].data_ptr(), ctypes.POINTER(ctypes.c_float)),
-                                         dh.numel(), None)
-            if st:
-                raise RuntimeError(_lib.last_error())
-            d_out = dh
+            dhb = torch.empty(M, fi, device=self.device, dtype=torch.bfloat16)
+            self._gemm(d_out_b, fo, self.Wb[i], fo, M, fi, fo, 4, dh, Cb=dhb, pre=pres[i - 1])
+            d_out, d_out_b = dh, dhb
         return loss, grads_W, grads_b
 
     def adam(self, grads_W, grads_b, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
@@ -236,6 +262,7 @@ class MLP:
                                  self.b[i].numel(), lr, b1, b2, eps, self.step, None)
             if st:
                 raise RuntimeError(_lib.last_error())
+            self._transpose(self.Wb[i], self.WbT[i])
 
 
 DEFAULT_WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__file__), "data", "proposal_weights.npz")

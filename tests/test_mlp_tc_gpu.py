@@ -1,0 +1,132 @@
+"""GPU: the tcgen05 GEMM of the MLP (pqg_mlp_gemm_tc) against a plain PyTorch
+FP32 matmul of the same BF16 operands, over ragged shapes (M, N, K not
+multiples of the 128 x BN x 64 tiles, N below 16, K below 16), every
+epilogue, split-K, and the transpose kernel.  After each call the kernel's
+device error code (a bounded wait that ran out) must be 0.
+
+Tolerance: |C - ref| <= 1e-5 * (|A| |B|^T) + 1e-6 per entry (FP32 sums of the
+same exact BF16 products in a different order); GELU epilogues are checked
+against torch's exact (erf) GELU at 1e-5 relative plus the BF16 rounding of
+the stored activation.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(300, 256, 256), (128, 256, 16), (1000, 8, 256), (77, 200, 104), (20, 16, 8), (513, 24, 136),
+          (4096, 256, 256), (256, 256, 4096)]
+
+
+def _f(t):
+    return ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float)) if t is not None else None
+
+
+def _v(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _status(L):
+    code = np.zeros(1, dtype=np.int32)
+    assert L.pqg_mlp_tc_status(code.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) == 0
+    return int(code[0])
+
+
+def _operands(torch, M, N, K, seed):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    ref = A.float() @ B.float().t()
+    scale = A.float().abs() @ B.float().abs().t()
+    return A, B, ref, scale
+
+
+@pytest.fixture(scope="module")
+def L(engine):
+    import torch
+
+    torch.backends.cuda.matmul.allow_tf32 = False
+    from piquasso_gb300 import _lib
+
+    return _lib.load()
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES)
+def test_plain_and_bias(L, M, N, K):
+    import torch
+
+    A, B, ref, scale = _operands(torch, M, N, K, M + N + K)
+    C = torch.empty(M, N, device="cuda")
+    assert L.pqg_mlp_gemm_tc(_v(A), K, _v(B), K, M, N, K, 0, _f(C), None, None, None, None, 0, None) == 0
+    torch.cuda.synchronize()
+    assert _status(L) == 0
+    assert torch.all((C - ref).abs() <= 1e-5 * scale + 1e-6)
+    bias = torch.randn(N, device="cuda")
+    assert L.pqg_mlp_gemm_tc(_v(A), K, _v(B), K, M, N, K, 3, _f(C), None, _f(bias), None, None, 0, None) == 0
+    torch.cuda.synchronize()
+    assert _status(L) == 0
+    assert torch.all((C - ref - bias).abs() <= 1e-5 * scale + 1e-6)
+
+
+@pytest.mark.parametrize("M,N,K", SHAPES[:5])
+def test_gelu_epilogues(L, M, N, K):
+    import torch
+
+    A, B, ref, scale = _operands(torch, M, N, K, 7 * M + K)
+    bias = torch.randn(N, device="cuda")
+    pre = torch.empty(M, N, device="cuda")
+    act = torch.empty(M, N, device="cuda", dtype=torch.bfloat16)
+    assert L.pqg_mlp_gemm_tc(_v(A), K, _v(B), K, M, N, K, 1, _f(pre), _v(act), _f(bias), None, None, 0, None) == 0
+    torch.cuda.synchronize()
+    assert _status(L) == 0
+    want = ref + bias
+    assert torch.all((pre - want).abs() <= 1e-5 * scale + 1e-6)
+    g = torch.nn.functional.gelu(pre)
+    assert torch.all((act.float() - g).abs() <= 2.0 ** -8 * g.abs() + 1e-5)
+    # backward through the activation: C = acc * GELU'(p)
+    p = torch.randn(M, N, device="cuda")
+    d = torch.empty(M, N, device="cuda")
+    db = torch.empty(M, N, device="cuda", dtype=torch.bfloat16)
+    assert L.pqg_mlp_gemm_tc(_v(A), K, _v(B), K, M, N, K, 4, _f(d), _v(db), None, _f(p), None, 0, None) == 0
+    torch.cuda.synchronize()
+    assert _status(L) == 0
+    pr = p.clone().requires_grad_(True)
+    torch.nn.functional.gelu(pr).sum().backward()
+    gg = pr.grad
+    assert torch.all((d - ref * gg).abs() <= 1e-5 * scale * gg.abs() + 1e-5 * (ref * gg).abs() + 1e-6)
+    assert torch.all((db.float() - d).abs() <= 2.0 ** -8 * d.abs() + 1e-30)
+
+
+@pytest.mark.parametrize("splits", [1, 3, 16])
+def test_split_k(L, splits):
+    import torch
+
+    M, N, K = 256, 136, 3000  # K not a multiple of the 64-wide chunk
+    A, B, ref, scale = _operands(torch, M, N, K, splits)
+    A2 = torch.zeros(M, 3008, device="cuda", dtype=torch.bfloat16)  # row stride 3008 (16-byte rows)
+    A2[:, :K] = A
+    B2 = torch.zeros(N, 3008, device="cuda", dtype=torch.bfloat16)
+    B2[:, :K] = B
+    C = torch.empty(M, N, device="cuda")
+    scratch = torch.empty(splits * M * N, device="cuda")
+    assert L.pqg_mlp_gemm_tc(_v(A2), 3008, _v(B2), 3008, M, N, K, 2, _f(C), None, None, None, _f(scratch), splits,
+                             None) == 0
+    torch.cuda.synchronize()
+    assert _status(L) == 0
+    assert torch.all((C - ref).abs() <= 1e-5 * scale + 1e-6)
+
+
+def test_transpose_and_rejects(L):
+    import torch
+
+    X = torch.randn(77, 40, device="cuda").to(torch.bfloat16)
+    Y = torch.zeros(40, 80, device="cuda", dtype=torch.bfloat16)
+    assert L.pqg_mlp_transpose_bf16(_v(X), 77, 40, 40, _v(Y), 80, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(Y[:, :77], X.t())
+    C = torch.empty(4, 4, device="cuda")
+    # row strides that are not multiples of 8 elements are refused on the host
+    assert L.pqg_mlp_gemm_tc(_v(X), 12, _v(X), 12, 4, 4, 12, 0, _f(C), None, None, None, None, 0, None) != 0
