@@ -297,6 +297,63 @@ def bench_sampling(args):
     return out
 
 
+def bench_training(args):
+    """Training throughput of the learned proposal on the engine's kernels
+    (tcgen05 GEMMs, softmax cross-entropy, bias gradients, Adam): Adam steps
+    on batches of 65536 feature rows (synthetic features and targets of the
+    training shapes: 16 features, occupations 0..7), plus the forward GEMM of
+    a hidden layer (65536 x 256 x 256, bias + GELU epilogue) timed alone."""
+    import ctypes
+
+    import torch
+
+    from piquasso_gb300 import _lib, proposal
+
+    rows = 65536
+    g = torch.Generator(device="cuda").manual_seed(0)
+    X = torch.randn(rows, proposal.F, device="cuda", generator=g).to(torch.bfloat16)
+    hi = torch.full((rows,), proposal.CAP, dtype=torch.int8, device="cuda")
+    lo = torch.zeros(rows, dtype=torch.int8, device="cuda")
+    tgt = torch.randint(0, proposal.CLASSES, (rows,), device="cuda", generator=g).to(torch.int8)
+    mlp = proposal.MLP(seed=0)
+    for _ in range(3):
+        loss, gW, gb = mlp.loss_and_grads(X, lo, hi, tgt)
+        mlp.adam(gW, gb)
+    steps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        loss, gW, gb = mlp.loss_and_grads(X, lo, hi, tgt)
+        mlp.adam(gW, gb)
+    e1.record()
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1) / steps
+    L = _lib.load()
+    A = torch.randn(rows, 256, device="cuda", generator=g).to(torch.bfloat16)
+    C = torch.empty(rows, 256, device="cuda")
+    Cb = torch.empty(rows, 256, device="cuda", dtype=torch.bfloat16)
+    fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))  # noqa: E731
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    times = []
+    for _ in range(6):
+        e0.record()
+        st = L.pqg_mlp_gemm_tc(vp(A), 256, vp(mlp.WbT[1]), 256, rows, 256, 256, 1, fp(C), vp(Cb), fp(mlp.b[1]),
+                               None, None, 0, None)
+        e1.record()
+        torch.cuda.synchronize()
+        assert st == 0
+        times.append(e0.elapsed_time(e1))
+    gms = float(np.median(times[2:]))
+    flops = 2.0 * rows * 256 * 256
+    moved = rows * 256 * 2 + 256 * 256 * 2 + rows * 256 * (4 + 2)
+    return {"workload": "Adam steps on 65536-row batches of the 16->256->256->256->8 MLP (BF16, FP32 accumulation)",
+            "step_ms": step_ms, "rows_per_s": rows / (step_ms * 1e-3),
+            "forward_gemm": {"shape": [rows, 256, 256], "ms": gms, "tflops": flops / (gms * 1e-3) / 1e12,
+                             "gb_per_s": moved / (gms * 1e-3) / 1e9,
+                             "note": "memory-bound at this shape: 64 flop/byte of operands and outputs"}}
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__
 
@@ -399,6 +456,7 @@ def run_ours(args, world, rank, local, pg):
         line["batch_4096_d40_n20"] = bench_batch(pg_engine, torch, flush, args, cpu=(rank == 0 and not args.no_cpu_baseline))
     if not args.no_variants and not args.no_sampling:
         line["sampling_n24_d48"] = bench_sampling(args)
+        line["training_mlp"] = bench_training(args)
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
         line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",
@@ -420,7 +478,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-sampling", action="store_true")
-    ap.add_argument("--mcmc-steps", type=int, default=330)
+    ap.add_argument("--mcmc-steps", type=int, default=600)
     ap.add_argument("--exact-samples", type=int, default=32768)
     args = ap.parse_args()
     if args.warmup < 3:

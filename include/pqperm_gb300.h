@@ -175,7 +175,8 @@ int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *f
  * BF16), the K-major copies of backward operands.  pqg_mlp_tc_status: reads
  * (and clears) the GEMM's device error code: 0, or the bounded wait that ran
  * out (1: operand copy, 2: stage release, 3: accumulator); synchronising.
- * pqg_mlp_bias_grad: db = column sums of d (M x N).  pqg_mlp_softmax_xent:
+ * pqg_mlp_bias_grad: db = column sums of d (M x N), deterministic, through
+ * `scratch` (ceil(M/256) * N floats).  pqg_mlp_softmax_xent:
  * per row m, softmax over classes lo[m]..hi[m] of logits (row stride ld),
  * loss = -log p(target), dlogits = (p - onehot) * scale (FP32, and BF16 when
  * dlogits_bf16 is not NULL).  pqg_mlp_adam: one Adam step on FP32 weights
@@ -186,7 +187,7 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
 int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
                            void *stream);
 int pqg_mlp_tc_status(int32_t *code);
-int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, void *stream);
+int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, float *scratch, void *stream);
 int pqg_mlp_softmax_xent(const float *logits, int64_t M, int32_t ld, int32_t classes, const int8_t *lo,
                          const int8_t *hi, const int8_t *target, float scale, float *loss, float *dlogits,
                          void *dlogits_bf16, void *stream);

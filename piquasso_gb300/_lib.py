@@ -60,7 +60,7 @@ SIGNATURES = {
     "pqg_mlp_transpose_bf16": ([ctypes.c_void_p, _I64, _I64, _I64, ctypes.c_void_p, _I64, ctypes.c_void_p],
                                ctypes.c_int),
     "pqg_mlp_tc_status": ([_i32], ctypes.c_int),
-    "pqg_mlp_bias_grad": ([_f, _I64, _I64, _f, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_bias_grad": ([_f, _I64, _I64, _f, _f, ctypes.c_void_p], ctypes.c_int),
     "pqg_mlp_softmax_xent": ([_f, _I64, _I32, _I32, _i8, _i8, _i8, ctypes.c_float, _f, _f, ctypes.c_void_p,
                               ctypes.c_void_p], ctypes.c_int),
     "pqg_mlp_adam": ([_f, ctypes.c_void_p, _f, _f, _f, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,

@@ -17,12 +17,33 @@ void set_last_error(const char *msg);
 
 namespace {
 
-// bias gradient: db[n] = sum_m d[m][n]  (one thread per column, fixed order)
-__global__ void bias_grad(const float *__restrict__ d, int64_t M, int64_t N, float *__restrict__ db) {
+// Bias gradient db[n] = sum_m d[m][n], deterministic and spread over the GPU:
+// blocks of 32 columns x 256 rows write partial sums (8 row lanes, fixed-order
+// shared-memory sum), then a fixed-order sum over the row chunks.
+constexpr int BIAS_ROWS = 256;
+
+__global__ void bias_partial(const float *__restrict__ d, int64_t M, int64_t N, float *__restrict__ part) {
+    __shared__ float s[8][33];
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * 32 + threadIdx.x;
+    const int64_t m_lo = static_cast<int64_t>(blockIdx.y) * BIAS_ROWS;
+    const int64_t m_hi = m_lo + BIAS_ROWS < M ? m_lo + BIAS_ROWS : M;
+    float acc = 0.0f;
+    if (c < N)
+        for (int64_t m = m_lo + threadIdx.y; m < m_hi; m += 8) acc += d[m * N + c];
+    s[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < N) {
+        float t = 0.0f;
+        for (int k = 0; k < 8; ++k) t += s[k][threadIdx.x];
+        part[static_cast<int64_t>(blockIdx.y) * N + c] = t;
+    }
+}
+
+__global__ void bias_final(const float *__restrict__ part, int64_t chunks, int64_t N, float *__restrict__ db) {
     const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (c >= N) return;
     float s = 0.0f;
-    for (int64_t m = 0; m < M; ++m) s += d[m * N + c];
+    for (int64_t k = 0; k < chunks; ++k) s += part[k * N + c];
     db[c] = s;
 }
 
@@ -82,8 +103,20 @@ int fail_cuda(cudaError_t e, const char *what) {
 
 extern "C" {
 
-int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, void *stream) {
-    bias_grad<<<static_cast<unsigned>((N + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(d, M, N, db);
+int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, float *scratch, void *stream) {
+    if (M <= 0 || N <= 0 || !d || !db || !scratch) {
+        pqg::set_last_error("pqg_mlp_bias_grad: invalid arguments");
+        return PQG_ERR_INVALID;
+    }
+    const int64_t chunks = (M + BIAS_ROWS - 1) / BIAS_ROWS;
+    if (chunks > 65535) {
+        pqg::set_last_error("pqg_mlp_bias_grad: too many rows");
+        return PQG_ERR_TOO_LARGE;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    bias_partial<<<dim3(static_cast<unsigned>((N + 31) / 32), static_cast<unsigned>(chunks)), dim3(32, 8), 0, s>>>(
+        d, M, N, scratch);
+    bias_final<<<static_cast<unsigned>((N + 127) / 128), 128, 0, s>>>(scratch, chunks, N, db);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_bias_grad");
 }

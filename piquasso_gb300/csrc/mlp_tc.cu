@@ -14,7 +14,9 @@
 //     tensor memory (TMEM, BN FP32 columns), and tcgen05.commit releases each
 //     stage back to the TMA producer once its MMAs have read it;
 //   * after a final commit, each warp reads its 32 accumulator rows with
-//     tcgen05.ld (32x32b) and applies the fused epilogue: plain FP32, bias,
+//     tcgen05.ld (32x32b), turns them around in shared memory so that the
+//     global stores write whole row segments, and applies the fused
+//     epilogue: plain FP32, bias,
 //     bias + GELU (FP32 pre-activation and BF16 activation), GELU backward
 //     (dpre = acc * GELU'(pre), FP32 and BF16), or split-K partial sums.
 // Rows and columns past M, N, K are zero-filled by TMA (out-of-range box
@@ -148,6 +150,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+        "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void record_error(int code) { atomicCAS(&g_tc_error, 0, code); }
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
@@ -240,52 +257,69 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
     if (have) {
-        const int64_t row = m0 + warp * 32 + lane;
+        // Each warp owns accumulator rows [32 warp, 32 warp + 32).  Per group of
+        // 32 (or a last 16) columns: tcgen05.ld puts row `lane` in this thread;
+        // the rows go through a padded 32 x 33 tile in the (now idle) stage
+        // memory, and the epilogue then runs with 8 threads per row, so every
+        // store instruction writes whole 128-byte row segments and the bias and
+        // pre-activation loads are coalesced too.
+        float *tile = reinterpret_cast<float *>(tc_smem_raw + (base - raw)) + warp * 32 * 33;
         const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-        float *crow = g.C + (g.epi == TC_EPI_SPLITK ? static_cast<int64_t>(blockIdx.z) * g.M * g.N : 0) + row * g.N;
-        for (int j0 = 0; j0 < g.BN; j0 += 16) {
-            float v[16];
-            tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
-            if (row >= g.M) continue;
-            const int64_t c0 = n0 + j0;
-            const int nq = g.N - c0 < 16 ? static_cast<int>(g.N - c0) : 16;
-            if (nq <= 0) continue;
-            // epilogue values of this thread's 16 columns
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                if (q >= nq) break;
-                float x = v[q];
-                if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) x += g.bias[c0 + q];
-                if (g.epi == TC_EPI_DGELU) x *= gelu_grad(g.pre[row * g.N + c0 + q]);
-                v[q] = x;
-            }
-            const bool vec = nq == 16 && (g.N % 8) == 0;  // 16-byte aligned stores
-            if (vec) {
-                float4 *o = reinterpret_cast<float4 *>(crow + c0);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        float *cbase = g.C + (g.epi == TC_EPI_SPLITK ? static_cast<int64_t>(blockIdx.z) * g.M * g.N : 0);
+        const bool vec_ok = (g.N % 4) == 0;
+        for (int j0 = 0; j0 < g.BN; j0 += 32) {
+            const int ncol = g.BN - j0 >= 32 ? 32 : 16;
+            float v[32];
+            if (ncol == 32) {
+                tmem_ld32(taddr + static_cast<uint32_t>(j0), v);
             } else {
-                for (int q = 0; q < nq; ++q) crow[c0 + q] = v[q];
-            }
-            if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_DGELU) {
-                __nv_bfloat16 *brow = g.Cb + row * g.N + c0;
-                if (vec) {
-                    uint4 w[2];
-                    uint32_t *wp = reinterpret_cast<uint32_t *>(w);
+                float h[16];
+                tmem_ld16(taddr + static_cast<uint32_t>(j0), h);
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const float a = g.epi == TC_EPI_BIAS_GELU ? gelu(v[2 * q]) : v[2 * q];
-                        const float b = g.epi == TC_EPI_BIAS_GELU ? gelu(v[2 * q + 1]) : v[2 * q + 1];
-                        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-                        wp[q] = *reinterpret_cast<uint32_t *>(&h);
+                for (int q = 0; q < 16; ++q) v[q] = h[q];
+            }
+            for (int q = 0; q < ncol; ++q) tile[lane * 33 + q] = v[q];
+            __syncwarp();
+            const int nquad = ncol / 4;
+            for (int idx = lane; idx < 32 * nquad; idx += 32) {
+                const int r = idx / nquad, q = idx - r * nquad;
+                const int64_t row = m0 + warp * 32 + r;
+                const int64_t col = n0 + j0 + 4 * q;
+                if (row >= g.M || col >= g.N) continue;
+                float x[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) x[k] = tile[r * 33 + 4 * q + k];
+                const int64_t at = row * g.N + col;
+                if (vec_ok && col + 3 < g.N) {
+                    if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) {
+                        const float4 bb = *reinterpret_cast<const float4 *>(g.bias + col);
+                        x[0] += bb.x, x[1] += bb.y, x[2] += bb.z, x[3] += bb.w;
+                    } else if (g.epi == TC_EPI_DGELU) {
+                        const float4 p = *reinterpret_cast<const float4 *>(g.pre + at);
+                        x[0] *= gelu_grad(p.x), x[1] *= gelu_grad(p.y), x[2] *= gelu_grad(p.z), x[3] *= gelu_grad(p.w);
                     }
-                    reinterpret_cast<uint4 *>(brow)[0] = w[0];
-                    reinterpret_cast<uint4 *>(brow)[1] = w[1];
+                    *reinterpret_cast<float4 *>(cbase + at) = make_float4(x[0], x[1], x[2], x[3]);
+                    if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_DGELU) {
+                        const bool act = g.epi == TC_EPI_BIAS_GELU;
+                        __nv_bfloat162 lo2 = __floats2bfloat162_rn(act ? gelu(x[0]) : x[0], act ? gelu(x[1]) : x[1]);
+                        __nv_bfloat162 hi2 = __floats2bfloat162_rn(act ? gelu(x[2]) : x[2], act ? gelu(x[3]) : x[3]);
+                        uint2 w;
+                        w.x = *reinterpret_cast<uint32_t *>(&lo2);
+                        w.y = *reinterpret_cast<uint32_t *>(&hi2);
+                        *reinterpret_cast<uint2 *>(g.Cb + at) = w;
+                    }
                 } else {
-                    for (int q = 0; q < nq; ++q)
-                        brow[q] = __float2bfloat16(g.epi == TC_EPI_BIAS_GELU ? gelu(v[q]) : v[q]);
+                    for (int k = 0; k < 4 && col + k < g.N; ++k) {
+                        float y = x[k];
+                        if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) y += g.bias[col + k];
+                        if (g.epi == TC_EPI_DGELU) y *= gelu_grad(g.pre[at + k]);
+                        cbase[at + k] = y;
+                        if (g.epi == TC_EPI_BIAS_GELU) g.Cb[at + k] = __float2bfloat16(gelu(y));
+                        if (g.epi == TC_EPI_DGELU) g.Cb[at + k] = __float2bfloat16(y);
+                    }
                 }
             }
+            __syncwarp();  // the tile is rewritten by the next group
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

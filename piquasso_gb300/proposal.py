@@ -237,8 +237,10 @@ class MLP:
             scratch = torch.empty(splits * fi * fo, device=self.device, dtype=torch.float32)
             self._gemm(hT, hT.shape[1], dT, dT.shape[1], fi, fo, M, 2, gW, scratch=scratch, splits=splits)
             gb = torch.empty(fo, device=self.device, dtype=torch.float32)
+            part = torch.empty(((M + 255) // 256) * fo, device=self.device, dtype=torch.float32)
             st = L.pqg_mlp_bias_grad(ctypes.cast(d_out.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, fo,
-                                     ctypes.cast(gb.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
+                                     ctypes.cast(gb.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                                     ctypes.cast(part.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
             if st:
                 raise RuntimeError(_lib.last_error())
             grads_W[i], grads_b[i] = gW, gb

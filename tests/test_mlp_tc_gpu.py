@@ -130,3 +130,20 @@ def test_transpose_and_rejects(L):
     C = torch.empty(4, 4, device="cuda")
     # row strides that are not multiples of 8 elements are refused on the host
     assert L.pqg_mlp_gemm_tc(_v(X), 12, _v(X), 12, 4, 4, 12, 0, _f(C), None, None, None, None, 0, None) != 0
+
+
+@pytest.mark.parametrize("M,N", [(65536, 256), (300, 8), (1, 40)])
+def test_bias_grad(L, M, N):
+    import torch
+
+    d = torch.randn(M, N, device="cuda")
+    db = torch.empty(N, device="cuda")
+    part = torch.empty(((M + 255) // 256) * N, device="cuda")
+    assert L.pqg_mlp_bias_grad(_f(d), M, N, _f(db), _f(part), None) == 0
+    torch.cuda.synchronize()
+    ref = d.double().sum(dim=0)
+    assert torch.all((db.double() - ref).abs() <= 1e-5 * d.abs().double().sum(dim=0) + 1e-6)
+    db2 = torch.empty(N, device="cuda")
+    assert L.pqg_mlp_bias_grad(_f(d), M, N, _f(db2), _f(part), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(db, db2)  # deterministic
