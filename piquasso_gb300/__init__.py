@@ -4,7 +4,10 @@ Public API (drop-in for ``piquasso._math.permanent``):
     permanent(matrix, rows, cols)
     permanent_laplace(matrix, rows, cols)
 plus the additive ``permanent_batch``, ``permanent_grad`` and the connector in
-``piquasso_gb300.connector``.
+``piquasso_gb300.connector``; the samplers (exact, lossy, partially
+distinguishable) in ``piquasso_gb300.sampling``, batched detection
+probabilities and LXEB scoring in ``piquasso_gb300.probabilities``, and the
+learned-proposal Metropolis sampler in ``piquasso_gb300.metropolis``.
 """
 
 from .permanent import (  # noqa: F401

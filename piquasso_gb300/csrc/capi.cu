@@ -263,7 +263,7 @@ int enqueue_pipeline(Context &C, DeviceBuffers &B, const Planner &pl, const Plan
                                   k->smem_bytes, s));
         if (ev_w1) PQG_CUDA(cudaEventRecord(ev_w1, s));
         if (!pl.chunks.empty()) {
-            reduce_chunks<<<static_cast<unsigned>(pl.chunks.size()), 256, 0, s>>>(
+            reduce_chunks<<<static_cast<unsigned>(pl.chunks.size()), PQG_CHUNK_ITEMS, 0, s>>>(
                 reinterpret_cast<const PqgChunk *>(d + L.o_chunks), A.probs, A.partials,
                 static_cast<double *>(B.chunk_out.p));
             PQG_CUDA(cudaGetLastError());
@@ -308,9 +308,9 @@ int run_plan(Context &C, Planner &pl, T *out, double *out_lo) {
     g_walk_flops = pl.total_flops;
     g_h2d = static_cast<double>(L.total);
     g_d2h = static_cast<double>(align256(L.out_bytes) + L.lo_bytes);
+    PQG_CUDA(cudaEventRecord(C.evs, s));  // device time includes the prep kernel
     st = enqueue_prep(C, C.bufs, pl, L, s);
     if (st) return st;
-    PQG_CUDA(cudaEventRecord(C.evs, s));
     st = enqueue_pipeline<T>(C, C.bufs, pl, L, s, C.ev0, C.ev1, k, blocks);
     if (st) return st;
     g_launches += pipeline_launches(pl);

@@ -428,8 +428,8 @@ void Planner::finish() {
         total_items += q.n_items;
         total_parts += q.n_items * q.n_out;
         item_begin[ip + 1] = total_items;
-        // level-1 reduction chunks of at most 512 items
-        const int64_t per_chunk = 512;
+        // level-1 reduction chunks
+        const int64_t per_chunk = PQG_CHUNK_ITEMS;
         for (int64_t lo = q.item_begin; lo < q.item_begin + q.n_items; lo += per_chunk) {
             PqgChunk c{};
             c.item_lo = lo;

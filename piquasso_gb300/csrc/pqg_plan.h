@@ -23,6 +23,10 @@
 #define PQG_MAX_OUTER 60
 #define PQG_MAX_INNER 16
 #define PQG_ITEM_LANES 32
+// Level-1 reduction chunk: items per chunk = threads of its block.  Small
+// chunks spread the double-double sums over every SM (the FP64 pipe of an SM
+// completes about two lanes per clock).
+#define PQG_CHUNK_ITEMS 64
 
 enum PqgProblemKind : int32_t {
     PQG_KIND_WALK = 0,      // Gray-code walk on the device
@@ -76,7 +80,7 @@ struct PqgStep {
     float pad;
 };
 
-// Level-1 reduction chunk: items [item_lo, item_hi) of one problem.
+// Level-1 reduction chunk: items [item_lo, item_hi) of one problem (at most PQG_CHUNK_ITEMS).
 struct PqgChunk {
     int64_t item_lo, item_hi;  // global item indices
     int32_t problem;

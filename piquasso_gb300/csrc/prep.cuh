@@ -3,8 +3,10 @@
 // The host uploads one matrix (FP64, interleaved complex, row-major) and, per
 // problem, the matrix rows of its digits and the matrix columns it keeps
 // (PqgProblem::off_idx).  This kernel builds, in the walk's precision:
-//   * the DF column scales 2^-e_j with B_j = |a0_j| + sum_i m_i |a_ij| in
-//     [2^(e_j-1), 2^e_j), so no double-float column sum exceeds 1 in magnitude
+//   * the DF column scales 2^-e_j with B_j = |a0_j|_1 + sum_i m_i |a_ij|_1 in
+//     [2^(e_j-1), 2^e_j) (|z|_1 = |re z| + |im z| >= |z|, a bound as good as
+//     the modulus to within one power of two, and cheap), so no double-float
+//     column sum exceeds 1 in magnitude
 //     (powers of two are exact; sum_j e_j cm_j goes to col_shift and is
 //     multiplied back in the final scaling);
 //   * the seeds, the column sums with every digit at 0: a0 + sum_i m_i a_i,
@@ -36,6 +38,25 @@ struct PrepArgs {
 __device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
     hi = __double2float_rn(x);
     lo = __double2float_rn(x - static_cast<double>(hi));
+}
+
+// Reflected mixed-radix Gray code of inner code t (< P <= 2^15): the same
+// code as gray_decode, in 32-bit arithmetic.
+__device__ __forceinline__ void gray_decode_inner(const uint8_t *__restrict__ m, int n, uint32_t t, uint8_t *g) {
+    uint8_t c[PQG_MAX_INNER];
+    for (int k = 0; k < n; ++k) {
+        const uint32_t L = m[k] + 1u;
+        const uint32_t q = t / L;
+        c[k] = static_cast<uint8_t>(t - q * L);
+        t = q;
+    }
+    int parity = 0;
+    for (int k = n - 1; k >= 0; --k) {
+        const int L = m[k] + 1;
+        const int code = parity ? L - 1 - c[k] : c[k];
+        g[k] = static_cast<uint8_t>(code);
+        parity ^= (code & 1);
+    }
 }
 
 template <int FMT>
@@ -77,10 +98,10 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             int e = 0;
             if constexpr (FMT == PREP_DF) {
                 const double2 v = a0(j);
-                double B = hypot(v.x, v.y);
+                double B = fabs(v.x) + fabs(v.y);
                 for (int d = 0; d < nd; ++d) {
                     const double2 w = ad(d, j);
-                    B += mult(d) * hypot(w.x, w.y);
+                    B += mult(d) * (fabs(w.x) + fabs(w.y));
                 }
                 if (B > 0.0) frexp(B, &e);
                 s = ldexp(1.0, -e);
@@ -154,7 +175,7 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             const int64_t t = e / nc;
             const int j = static_cast<int>(e - t * nc);
             uint8_t g[PQG_MAX_INNER];
-            gray_decode(pr->inner_m, K, t, g);
+            gray_decode_inner(pr->inner_m, K, static_cast<uint32_t>(t), g);
             double re = 0.0, im = 0.0;
             for (int k = 0; k < K; ++k) {
                 if (!g[k]) continue;

@@ -1,5 +1,5 @@
 // Deterministic double-double reductions of the walk partials.
-//   level 1: one block per chunk of at most 512 items of one problem;
+//   level 1: one block per chunk of at most PQG_CHUNK_ITEMS items of one problem;
 //   level 2: one warp per problem sums its chunks, applies 2^-(N-1) and writes
 //            the output in the problem's precision (plus the low words).
 #pragma once

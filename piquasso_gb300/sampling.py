@@ -1,8 +1,11 @@
 """Exact boson sampling on the GPU (Clifford & Clifford algorithm B).
 
-A drop-in for the lossless, indistinguishable path of the reference's
-``PassiveSimulator`` sampler (piquasso/_simulators/passive/sampling.py:149-236,
-711-753).  Every shot keeps its own ``np.random.default_rng(seed + idx)`` and
+A drop-in for the reference's ``PassiveSimulator`` sampler
+(piquasso/_simulators/passive/sampling.py:149-236, 711-753): lossless,
+uniformly lossy (a per-photon reject condition), non-uniformly lossy (the
+lossless sampler on an SVD dilation, sampling.py:110-146) and with uniform
+partial distinguishability (sampling.py:328-418); ``sample`` dispatches as
+the reference's passive/simulation_steps.py:315-369 does.  Every shot keeps its own ``np.random.default_rng(seed + idx)`` and
 draws exactly the random numbers the reference draws, in the same order, so a
 given seed reproduces the reference's samples.  What changes is the schedule:
 all shots advance one photon at a time together, and each photon step is ONE
@@ -52,12 +55,83 @@ def _pmf_batch(U, current_input, samples, laplace):
     return pmf
 
 
-def generate_samples(input_state, shots, interferometer, seed, batch_size=4096):
-    """Samples of the lossless boson sampler, as tuples, in generation order.
+def _separate_particles(input_occupation, overlap, rng):
+    """sampling.py:371-400 of the reference: per occupied input mode j, the
+    number K of indistinguishable photons, drawn with weights
+    C(n_j, k) x^k (1 - x)^(n_j - k) k!  (same floating-point formula)."""
+    from scipy.special import comb, factorial
+
+    d = len(input_occupation)
+    indist = np.zeros(d, dtype=int)
+    dist = np.zeros(d, dtype=int)
+    for j, n_j in enumerate(input_occupation):
+        if n_j == 0:
+            continue
+        weights = np.array([comb(n_j, k) * (overlap ** k) * ((1.0 - overlap) ** (n_j - k)) * factorial(k)
+                            for k in range(n_j + 1)], dtype=float)
+        K = rng.choice(n_j + 1, p=weights / weights.sum())
+        indist[j] = K
+        dist[j] = n_j - K
+    return indist, dist
+
+
+def _sample_distinguishable(U128, particles, rng, reject):
+    """sampling.py:403-418: every distinguishable photon lands in an output
+    mode drawn from |U[:, input mode]|^2 (normalised), then may be lost."""
+    d = len(particles)
+    out = np.zeros(d, dtype=int)
+    for mode, count in enumerate(particles):
+        p = np.abs(U128[:, mode]) ** 2
+        p = p / np.sum(p)
+        for _ in range(count):
+            o = rng.choice(d, p=p)
+            if not reject():
+                out[o] += 1
+    return out
+
+
+def _lockstep(U, U128, samples, photons, rngs, rejects):
+    """The indistinguishable phase of every shot of a batch at once.  Shot s
+    walks len(photons[s]) steps; at a step its reject flag (from the reject
+    condition, in the reference's call order) either skips the step or it
+    grows its input by a random remaining photon (its own generator), and all
+    growing shots share ONE batched Laplace launch before each draws its
+    output mode.  ``samples`` (shots x d) is updated in place."""
+    nb, d = samples.shape
+    current = np.zeros((nb, d), dtype=int)
+    to_shrink = [np.copy(p) for p in photons]
+    steps = max((len(p) for p in photons), default=0)
+    for k in range(steps):
+        act = [s for s in range(nb) if k < len(photons[s]) and not rejects[s][k]]
+        if not act:
+            continue
+        for s in act:
+            i = rngs[s].choice(len(to_shrink[s]))
+            current[s, to_shrink[s][i]] += 1
+            to_shrink[s] = np.delete(to_shrink[s], i)
+        idx = np.asarray(act)
+        lap = permanent_laplace_batch(U, samples[idx], current[idx]).astype(np.complex128)
+        pmf = _pmf_batch(U128, current[idx], samples[idx], lap)
+        for r, s in enumerate(act):
+            samples[s, rngs[s].choice(np.arange(d), p=pmf[r])] += 1
+
+
+def generate_samples(input_state, shots, interferometer, seed, batch_size=4096, transmission=None,
+                     particle_overlap=None):
+    """Samples of the reference's sampler, as tuples, in generation order.
 
     ``input_state``: occupation numbers (length d); ``interferometer``: the
     d x d matrix (its dtype picks complex64 or complex128 permanents);
     ``seed``: the reference's ``config.seed_sequence`` (shot idx uses seed + idx).
+    ``transmission``: uniform loss — each photon step first asks the reject
+    condition ``config.rng.uniform() > transmission`` of the configuration
+    generator ``np.random.default_rng(seed)`` (passive/simulation_steps.py:
+    351-362 of the reference), so shot s consumes that generator's draws
+    s*n .. s*n+n-1.  ``particle_overlap``: uniform partial distinguishability
+    (sampling.py:328-368): the photons of each shot are split into
+    indistinguishable and distinguishable ones, the distinguishable ones are
+    sampled one by one, the others by the exact sampler; the reject
+    condition is asked once per photon in the same order.
     """
     U = np.asarray(interferometer)
     if U.dtype not in (np.complex64, np.complex128):
@@ -67,26 +141,83 @@ def generate_samples(input_state, shots, interferometer, seed, batch_size=4096):
     d = len(inp)
     n = int(inp.sum())
     fq = to_first_quantized(inp)
+    draws = None
+    if transmission is not None:
+        draws = np.random.default_rng(seed).uniform(size=shots * n) > transmission
     out = []
     for b0 in range(0, shots, batch_size):
         nb = min(batch_size, shots - b0)
         rngs = [np.random.default_rng(seed=seed + b0 + i) for i in range(nb)]
-        samples = np.zeros((nb, d), dtype=int)
-        current = np.zeros((nb, d), dtype=int)
-        to_shrink = [np.copy(fq) for _ in range(nb)]
-        for _ in range(1, n + 1):
-            for s in range(nb):
-                k = rngs[s].choice(len(to_shrink[s]))
-                current[s, to_shrink[s][k]] += 1
-                to_shrink[s] = np.delete(to_shrink[s], k)
-            # Laplace permanents of every shot: rows = sample, cols = current input
-            lap = permanent_laplace_batch(U, samples, current).astype(np.complex128)
-            pmf = _pmf_batch(U128, current, samples, lap)
-            for s in range(nb):
-                idx = rngs[s].choice(np.arange(d), p=pmf[s])
-                samples[s, idx] += 1
-        out.extend(tuple(int(x) for x in row) for row in samples)
+        samples = np.zeros((nb, d), dtype=int)    # the indistinguishable photons' outputs
+        dist_out = np.zeros((nb, d), dtype=int)   # the distinguishable ones', added at the end
+        photons, rejects = [], []
+        for i in range(nb):
+            flags = draws[(b0 + i) * n:(b0 + i + 1) * n] if draws is not None else np.zeros(n, dtype=bool)
+            if particle_overlap is None:
+                photons.append(fq)
+                rejects.append(flags)
+            else:
+                indist, dist = _separate_particles(inp, particle_overlap, rngs[i])
+                it = iter(flags[:int(dist.sum())])
+                dist_out[i] = _sample_distinguishable(U128, dist, rngs[i], lambda: bool(next(it)))
+                photons.append(to_first_quantized(indist))
+                rejects.append(flags[int(dist.sum()):])
+        _lockstep(U, U128, samples, photons, rngs, rejects)
+        out.extend(tuple(int(x) for x in row) for row in samples + dist_out)
     return out
+
+
+def expanded_interferometer(matrix):
+    """The 2d x 2d dilation of a lossy d x d transmission matrix
+    (sampling.py:756-784 of the reference): with the SVD M = V diag(s) W,
+    blockdiag(V, I) [[diag s, diag c], [diag c, diag s]] blockdiag(W, I),
+    c = sqrt(1 - s^2).  Its first d columns are orthonormal and its upper-left
+    block is M; photons enter only the first d modes, so the lossless sampler
+    on it samples the lossy channel.  numpy's SVD, as the reference's, fixes
+    the phases (and so the samples of a given seed)."""
+    M = np.asarray(matrix, dtype=np.complex128)
+    V, sv, W = np.linalg.svd(M)
+    d = len(sv)
+    Z, I = np.zeros((d, d)), np.eye(d)
+    c = np.diag(np.sqrt(np.maximum(0.0, 1.0 - sv ** 2)))
+    return np.block([[V, Z], [Z, I]]) @ np.block([[np.diag(sv), c], [c, np.diag(sv)]]) @ np.block([[W, Z], [Z, I]])
+
+
+def generate_lossy_samples(input_state, shots, matrix, seed, batch_size=4096, batched=False):
+    """Non-uniform loss (sampling.py:110-146): the lossless sampler on the
+    2d-mode dilation with d empty ancilla modes, samples trimmed to the first
+    d modes.  ``batched``: the throughput sampler instead of the reference's
+    per-seed sequence."""
+    inp = np.asarray(input_state).astype(int)
+    d = len(inp)
+    E = expanded_interferometer(matrix)
+    if np.asarray(matrix).dtype == np.complex64:
+        E = E.astype(np.complex64)
+    state = np.concatenate([inp, np.zeros(d, dtype=int)])
+    if batched:
+        return generate_samples_batched(state, shots, E, seed, batch_size=batch_size)[:, :d]
+    return [s[:d] for s in generate_samples(state, shots, E, seed, batch_size=batch_size)]
+
+
+def sample(input_state, shots, interferometer, seed, particle_overlap=None, batched=False, batch_size=4096):
+    """The reference's dispatch (passive/simulation_steps.py:315-369): from the
+    singular values of the interferometer, lossless (all 1), uniform loss
+    (all equal: transmission s_0^2) or non-uniform loss (SVD dilation), with
+    optional uniform particle overlap.  Non-uniform loss with partially
+    distinguishable photons goes through loop hafnians in the reference and is
+    not on this engine's path."""
+    M = np.asarray(interferometer)
+    sv = np.linalg.svd(M.astype(np.complex128), compute_uv=False)
+    if np.all(np.isclose(sv, sv[0])):
+        T = None if np.isclose(sv[0], 1.0) else float(sv[0] ** 2)
+        if batched:
+            return generate_samples_batched(input_state, shots, M, seed, batch_size=batch_size, transmission=T,
+                                            particle_overlap=particle_overlap)
+        return generate_samples(input_state, shots, M, seed, batch_size=batch_size, transmission=T,
+                                particle_overlap=particle_overlap)
+    if particle_overlap is not None:
+        raise NotImplementedError("non-uniform loss with partially distinguishable photons (loop hafnians)")
+    return generate_lossy_samples(input_state, shots, M, seed, batch_size=batch_size, batched=batched)
 
 
 def get_counts(samples):
@@ -105,7 +236,8 @@ def result_samples(samples, seed):
     return out
 
 
-def generate_samples_batched(input_state, shots, interferometer, seed, batch_size=2048, timings=None):
+def generate_samples_batched(input_state, shots, interferometer, seed, batch_size=2048, timings=None,
+                             transmission=None, particle_overlap=None):
     """Exact samples of the same distribution, at throughput.
 
     Same algorithm (Clifford & Clifford B, sampling.py:208-236 of the
@@ -118,6 +250,14 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
     remaining photon at every step), and the pmf and the draw are vectorised
     over shots.  The samples therefore follow the reference's distribution but
     not its per-seed sequence.  Returns an int array (shots, d).
+
+    ``transmission`` (uniform loss): every photon is kept independently with
+    this probability, so a shot samples a random subset of its photons — the
+    distribution of the reference's per-step reject condition.
+    ``particle_overlap``: each shot splits its photons as the reference's
+    _separate_particles does; the distinguishable ones land independently
+    (multinomial over |U[:, j]|^2), the rest go through the exact sampler.
+    Shots with fewer photons left simply sit out the later steps.
 
     ``timings`` (optional dict) receives the seconds spent in the batched
     Laplace calls ("laplace_s") and in total ("total_s").
@@ -132,34 +272,66 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
     inp = np.asarray(input_state).astype(int)
     d = len(inp)
     n = int(inp.sum())
-    fq = to_first_quantized(inp)
     rng = np.random.default_rng(seed)
     out = np.zeros((shots, d), dtype=np.int64)
     t_lap = 0.0
+    colp = np.abs(U128) ** 2
+    colp = colp / colp.sum(axis=0, keepdims=True)  # column j: landing probabilities of a photon from mode j
     for b0 in range(0, shots, batch_size):
         nb = min(batch_size, shots - b0)
-        order = np.argsort(rng.random((nb, n)), axis=1)
-        photons = fq[order]  # (nb, n): the input mode joining at each step
-        samples = np.zeros((nb, d), dtype=np.int64)
-        current = np.zeros((nb, d), dtype=np.int64)
         rows = np.arange(nb)
-        for k in range(n):
-            current[rows, photons[:, k]] += 1
-            if k == 0:
-                # empty output: the Laplace vector is [1] at the only input column
-                lap = np.zeros((nb, d), dtype=np.complex128)
-                lap[rows, photons[:, 0]] = 1.0
-            else:
+        samples = np.zeros((nb, d), dtype=np.int64)    # the exact sampler's photons
+        dist_out = np.zeros((nb, d), dtype=np.int64)   # distinguishable photons, added at the end
+        # photon p of the input (mode fq[p], rank[p] among its mode's photons)
+        # takes part in the exact sampler when it is indistinguishable and kept
+        fq = to_first_quantized(inp).astype(np.int64)
+        rank = np.arange(n) - np.searchsorted(fq, fq)
+        take = np.ones((nb, n), dtype=bool)
+        if particle_overlap is not None:
+            from scipy.special import comb, factorial
+
+            x = float(particle_overlap)
+            K = np.zeros((nb, d), dtype=np.int64)
+            for j in np.nonzero(inp)[0]:
+                nj = int(inp[j])
+                w = np.array([comb(nj, k) * x ** k * (1.0 - x) ** (nj - k) * factorial(k) for k in range(nj + 1)])
+                K[:, j] = rng.choice(nj + 1, size=nb, p=w / w.sum())
+            take = rank[None, :] < K[:, fq]
+            dist = inp[None, :] - K
+            if transmission is not None:
+                dist = rng.binomial(dist, transmission)
+            for j in np.nonzero(dist.sum(axis=0))[0]:
+                dist_out += rng.multinomial(dist[:, j], colp[:, j])
+        if transmission is not None:
+            take &= rng.random((nb, n)) < transmission
+        counts = take.sum(axis=1)
+        m = int(counts.max()) if nb else 0
+        # the photons of each shot in a uniformly random order (the others last)
+        keys = rng.random((nb, n))
+        keys[~take] = 2.0
+        photons = fq[np.argsort(keys, axis=1)] if n else np.zeros((nb, 0), dtype=np.int64)
+        current = np.zeros((nb, d), dtype=np.int64)
+        for k in range(m):
+            act = rows[counts > k]
+            current[act, photons[act, k]] += 1
+            first = samples[act].sum(axis=1) == 0
+            lap = np.zeros((len(act), d), dtype=np.complex128)
+            if np.any(~first):
                 t0 = time.perf_counter()
-                lap = permanent_laplace_batch(U, samples, current).astype(np.complex128)
+                sel = act[~first]
+                lap[~first] = permanent_laplace_batch(U, samples[sel], current[sel]).astype(np.complex128)
                 t_lap += time.perf_counter() - t0
-            amp = (current * lap) @ U128.T  # amp[s, idx] = sum_j cur_j L_j U[idx, j]
+            if np.any(first):
+                # empty output: the Laplace vector is [1] at the only input column
+                f = act[first]
+                lap[np.nonzero(first)[0], photons[f, k]] = 1.0
+            amp = (current[act] * lap) @ U128.T  # amp[s, idx] = sum_j cur_j L_j U[idx, j]
             pmf = np.abs(amp) ** 2
             cdf = np.cumsum(pmf, axis=1)
-            u = rng.random(nb) * cdf[:, -1]
+            u = rng.random(len(act)) * cdf[:, -1]
             idx = np.minimum((cdf < u[:, None]).sum(axis=1), d - 1)
-            samples[rows, idx] += 1
-        out[b0:b0 + nb] = samples
+            samples[act, idx] += 1
+        out[b0:b0 + nb] = samples + dist_out
     if timings is not None:
         timings["laplace_s"] = t_lap
         timings["total_s"] = time.perf_counter() - t_start

@@ -16,6 +16,13 @@ been compiled by oracle/build_ref.sh.  Outputs (JSON, complex numbers as
   (read from the file's syntax tree), checked against oracle.sampler driven
   by the reference module's permanent_laplace; ``generated_samples`` holds the
   samples in generation order, before Result.samples bins and shuffles them.
+* ``sampler_lossy_seeded.json`` — the two seeded lossy-sampling goldens of the same
+  test file (non-uniform singular values through the SVD dilation; uniform
+  ones through the per-photon reject condition), reproduced by oracle.sampler
+  over the reference module's permanent_laplace.
+* ``lxeb_values.json`` — the reference's Haar-averaged LXEB reference values
+  (piquasso/lxeb.py, loaded from its file) on a grid of photon and mode
+  numbers, and the value its tests/test_lxeb.py asserts.
 * ``random_cases.json`` — seeded random permanent and Laplace cases
   (complex128 and complex64) with the reference module's outputs.
 * ``config_14.json`` — the 14x14 parity cases: leading 14x14 block of a seeded
@@ -190,6 +197,69 @@ def gen_sampler(ref):
             "expected_samples": vals["expected_samples"]}
 
 
+def gen_lossy_sampler(ref):
+    """The two seeded lossy goldens of tests/_simulators/passive/test_measurements.py:
+    non-uniform singular values (SVD dilation) and uniform ones (reject
+    condition on the configuration generator)."""
+    path = os.path.join(REF, "tests/_simulators/passive/test_measurements.py")
+    tree = ast.parse(open(path).read())
+    cases = []
+    for name in ("test_LossyInterferometer_boson_sampling_seeded",
+                 "test_LossyInterferometer_boson_sampling_uniform_losses"):
+        fn = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name == name][0]
+        vals = {}
+        for node in ast.walk(fn):
+            if isinstance(node, ast.Assign) and isinstance(node.targets[0], ast.Name):
+                t = node.targets[0].id
+                if t in ("seed_sequence", "expected_samples"):
+                    vals[t] = ast.literal_eval(node.value)
+                if t in ("U", "singular_values"):  # np.array(<literal list expression>)
+                    vals[t] = np.array(eval(ast.unparse(node.value.args[0]), {"__builtins__": {}}))
+                if t == "lossy_interferometer_matrix":
+                    vals["formula"] = ast.unparse(node.value)
+            if isinstance(node, ast.Call) and getattr(node.func, "attr", None) == "NumberState":
+                vals["input"] = ast.literal_eval(node.args[0])
+            if isinstance(node, ast.keyword) and node.arg == "shots":
+                vals["shots"] = ast.literal_eval(node.value)
+        M = eval(vals["formula"], {"np": np, "U": vals["U"], "singular_values": vals["singular_values"]})
+        sv = np.linalg.svd(M, compute_uv=False)
+        inp = np.array(vals["input"])
+        if np.all(np.isclose(sv, sv[0])):
+            kind = "uniform"
+            samples = osampler.generate_samples(inp, vals["shots"], ref.permanent_laplace, M, vals["seed_sequence"],
+                                                transmission=float(sv[0] ** 2))
+        else:
+            kind = "nonuniform"
+            samples = osampler.generate_lossy_samples(inp, vals["shots"], ref.permanent_laplace, M,
+                                                      vals["seed_sequence"])
+        expected = [tuple(x) for x in vals["expected_samples"]]
+        got = osampler.result_samples(samples, vals["seed_sequence"])
+        assert got == expected, "restated %s lossy sampler does not reproduce %s" % (kind, name)
+        cases.append({"source": "tests/_simulators/passive/test_measurements.py::" + name, "kind": kind,
+                      "matrix": mat(M), "input": vals["input"], "seed": vals["seed_sequence"],
+                      "shots": vals["shots"], "transmission": float(sv[0] ** 2) if kind == "uniform" else None,
+                      "generated_samples": [list(map(int, x)) for x in samples],
+                      "expected_samples": vals["expected_samples"]})
+    return {"cases": cases}
+
+
+def gen_lxeb():
+    """Outputs of the reference's own piquasso/lxeb.py (a dependency-free
+    module, loaded from its file) on a grid of (n, m), plus the values its
+    tests/test_lxeb.py asserts."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("ref_lxeb", os.path.join(REF, "piquasso/lxeb.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    grid = []
+    for n in range(0, 31):
+        for m in (1, 2, 3, 5, 8, 16, 40, 48, 100):
+            grid.append({"n": n, "m": m, "value": mod.lxe_ref_boson_sampling(n, m)})
+    return {"source": "piquasso/lxeb.py", "boson_sampling": grid,
+            "test_values": [{"n": 10, "m": 3, "value": 0.018798373343827918}]}
+
+
 def haar(d, seed):
     rng = np.random.default_rng(seed)
     Z = (rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d))) / np.sqrt(2)
@@ -308,6 +378,8 @@ def main():
         "random_cases.json": gen_random(ref),
         "config_14.json": gen_config14(ref),
         "grad_cases.json": gen_grad_cases(ref),
+        "sampler_lossy_seeded.json": gen_lossy_sampler(ref),
+        "lxeb_values.json": gen_lxeb(),
     }
     for name, obj in outputs.items():
         with open(os.path.join(HERE, name), "w") as f:

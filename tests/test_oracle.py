@@ -78,6 +78,23 @@ def test_restated_sampler_reproduces_reference_golden():
     assert [list(s) for s in osampler.result_samples(samples, g["seed"])] == g["expected_samples"]
 
 
+def test_restated_lossy_samplers_reproduce_reference_goldens():
+    """Non-uniform loss (SVD dilation) and uniform loss (per-photon reject
+    condition) of tests/_simulators/passive/test_measurements.py."""
+    g = load_golden("sampler_lossy_seeded.json")
+    assert {c["kind"] for c in g["cases"]} == {"uniform", "nonuniform"}
+    for c in g["cases"]:
+        M = as_matrix(c["matrix"])
+        inp = np.array(c["input"])
+        if c["kind"] == "uniform":
+            samples = osampler.generate_samples(inp, c["shots"], oracle.permanent_laplace_dd, M, c["seed"],
+                                                transmission=c["transmission"])
+        else:
+            samples = osampler.generate_lossy_samples(inp, c["shots"], oracle.permanent_laplace_dd, M, c["seed"])
+        assert [list(s) for s in samples] == c["generated_samples"], c["kind"]
+        assert [list(s) for s in osampler.result_samples(samples, c["seed"])] == c["expected_samples"]
+
+
 def test_oracle_identities():
     U = haar_unitary(10, 4)[:8, :8].copy()
     ones = np.ones(8, dtype=int)
