@@ -114,6 +114,20 @@ int pqg_permanent_grad_c128(const double *matrices, int64_t n_rows, int64_t n_co
 int pqg_permanent_grad_c64(const float *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                            const int32_t *cols, int64_t batch, float *out);
 
+/* Exact binomial moments of ideal boson sampling on n_sets sets of k output
+ * modes each (modes: n_sets x k indices), the generating-function dynamic
+ * program of the reference's marginal probabilities
+ * (piquasso/_simulators/passive/marginal.py:163-216, get_binomial_moments),
+ * for every set in the same launches.  U: host d x d interleaved complex128
+ * interferometer; input: d photon numbers (n = their sum <= 64).  moments
+ * (host): n_sets x (n+1)^k doubles, b[alpha] = E[prod_j C(X_j, alpha_j)]
+ * row-major over alpha (first mode slowest), 0 where |alpha| > n.  The
+ * marginal probabilities follow by the binomial transform.
+ * max_device_bytes > 0 refuses (PQG_ERR_TOO_LARGE) a call whose blocks
+ * would need more device memory; the call allocates and frees its own. */
+int pqg_binomial_moments_c128(const double *U, int64_t d, const int32_t *input, const int32_t *modes, int32_t k,
+                              int32_t n_sets, double *moments, int64_t max_device_bytes);
+
 /* Plan handles: plan and upload a batch once, then execute it many times as
  * one CUDA graph (queue reset, persistent walk, reductions) on the handle's
  * own stream — the form used for repeated batches (exact probabilities of a
@@ -149,7 +163,8 @@ int pqg_measure_vector_peaks(double ms, double *out2);
 
 /* Timing of the calling thread's last plain/Laplace/batch call, measured with
  * CUDA events on the launching stream: `walk_ms` is the walk kernel alone,
- * `device_ms` the whole device pipeline (queue reset, walk, both reductions,
+ * `device_ms` the whole device pipeline (the prep kernel that builds the
+ * problems' seeds, rows and prefix tables, queue reset, walk, both reductions;
  * excluding the host<->device copies).  `steps` is the number of Gray-code
  * steps walked, `flops` the algorithmic flop count of the call, and
  * `h2d_bytes` / `d2h_bytes` the bytes the call copied each way.  Any pointer

@@ -47,6 +47,7 @@ SIGNATURES = {
     "pqg_permanent_laplace_batch_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f, _i64], ctypes.c_int),
     "pqg_permanent_grad_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _d], ctypes.c_int),
     "pqg_permanent_grad_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f], ctypes.c_int),
+    "pqg_binomial_moments_c128": ([_d, _I64, _i32, _i32, _I32, _I32, _d, _I64], ctypes.c_int),
     "pqg_plan_create": ([ctypes.c_void_p, _I64, _I64, _i32, _i32, _I64, _I32, _I32, _I32,
                          ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "pqg_plan_launch": ([ctypes.c_void_p], ctypes.c_int),

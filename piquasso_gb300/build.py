@@ -26,6 +26,7 @@ CU_SOURCES = [
     "noalloc.cu",
     "mlp.cu",
     "mlp_tc.cu",
+    "marginal.cu",
     "proposal.cu",
     "k_plain_c128_0.cu",
     "k_plain_c128_1.cu",

@@ -37,7 +37,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from .marginals import marginal
+from .marginals import marginals
 
 F = 16          # features per (sample, mode)
 HIDDEN = 256
@@ -62,8 +62,9 @@ class ModeStats:
         self.p = np.zeros((self.d, 5))
         self.tail = np.zeros(self.d)
         self.var = np.zeros(self.d)
+        one_mode = marginals(inp, U, [(j,) for j in range(self.d)])  # one GPU call for every mode
         for j in range(self.d):
-            m = marginal(inp, U, (j,))
+            m = one_mode[j]
             self.p[j] = m[:5]
             self.tail[j] = max(0.0, 1.0 - float(m[:5].sum()))
             k = np.arange(len(m))

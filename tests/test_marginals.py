@@ -1,5 +1,6 @@
-"""CPU: exact one- and two-mode marginals (binomial-moment method) against
-brute-force sums of exact output probabilities |perm|^2 / (prod y! prod x!)."""
+"""CPU: the oracle's exact one- and two-mode marginals (binomial-moment
+method, oracle/marginals.py) against brute-force sums of exact output
+probabilities |perm|^2 / (prod y! prod x!) — the checker of the GPU marginals."""
 
 import itertools
 from math import factorial
@@ -9,7 +10,7 @@ import pytest
 
 import oracle
 from conftest import haar_unitary
-from piquasso_gb300 import marginals
+from oracle import marginals as omarg
 
 
 def _all_patterns(n, d):
@@ -31,7 +32,7 @@ def _brute(inp, U, modes):
 def test_marginals_match_brute_force(inp):
     U = haar_unitary(len(inp), 11)
     for modes in ((0,), (3,), (0, 1), (2, 4), (4, 1)):
-        ex = marginals.marginal(inp, U, modes)
+        ex = omarg.marginal(inp, U, modes)
         bf = _brute(inp, U, modes)
         assert np.allclose(ex, bf, atol=1e-12), (modes, ex, bf)
         assert abs(ex.sum() - 1) < 1e-12
@@ -46,5 +47,8 @@ def test_tvd_of_exact_distribution_is_small():
     probs /= probs.sum()
     idx = rng.choice(len(pats), size=200000, p=probs)
     samples = np.array(pats)[idx]
-    tv = marginals.tvd_two_mode(samples, inp, U, [(0, 1), (2, 5), (3, 4)])
-    assert np.all(tv < 0.01), tv
+    for pair in [(0, 1), (2, 5), (3, 4)]:
+        ex = omarg.marginal(inp, U, pair)
+        em = np.zeros_like(ex)
+        np.add.at(em, (samples[:, pair[0]], samples[:, pair[1]]), 1.0 / len(samples))
+        assert 0.5 * np.abs(ex - em).sum() < 0.01, pair
