@@ -91,6 +91,53 @@ __device__ __forceinline__ void df_cmul(dfl &xr, dfl &xi, dfl yr, dfl yi) {
     xi = i;
 }
 
+// The same product without the final renormalisation of either part, for
+// products that only feed further products: the result pair (s, low) still
+// sums to the product to about 2^-48 of its terms (TwoSum kept the rounding
+// error of the high words), and the next product takes the low word through
+// its FMA cross terms, so only the dropped low x low term grows — by the
+// cancellation factor |p1| / |p1 - p2| that the sum already carries.  It
+// takes the two dependent renormalisation operations off the product chain.
+// The pair is renormalised before it is accumulated (df_scale, df_add).
+__device__ __forceinline__ dfl df_mul_sub_lazy(dfl a, dfl b, dfl c, dfl d) {
+    const float p1 = __fmul_rn(a.hi, b.hi);
+    const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+    const float p2 = __fmul_rn(c.hi, d.hi);
+    const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+    const float s = __fsub_rn(p1, p2);
+    const float v = __fsub_rn(s, p1);
+    const float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(-p2, v));
+    float low = __fadd_rn(__fsub_rn(e1, e2), t);
+    low = __fmaf_rn(a.hi, b.lo, low);
+    low = __fmaf_rn(a.lo, b.hi, low);
+    low = __fmaf_rn(-c.hi, d.lo, low);
+    low = __fmaf_rn(-c.lo, d.hi, low);
+    return {s, low};
+}
+
+__device__ __forceinline__ dfl df_mul_add_lazy(dfl a, dfl b, dfl c, dfl d) {
+    const float p1 = __fmul_rn(a.hi, b.hi);
+    const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
+    const float p2 = __fmul_rn(c.hi, d.hi);
+    const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
+    const float s = __fadd_rn(p1, p2);
+    const float v = __fsub_rn(s, p1);
+    const float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
+    float low = __fadd_rn(__fadd_rn(e1, e2), t);
+    low = __fmaf_rn(a.hi, b.lo, low);
+    low = __fmaf_rn(a.lo, b.hi, low);
+    low = __fmaf_rn(c.hi, d.lo, low);
+    low = __fmaf_rn(c.lo, d.hi, low);
+    return {s, low};
+}
+
+__device__ __forceinline__ void df_cmul_lazy(dfl &xr, dfl &xi, dfl yr, dfl yi) {
+    const dfl r = df_mul_sub_lazy(xr, yr, xi, yi);
+    const dfl i = df_mul_add_lazy(xr, yi, xi, yr);
+    xr = r;
+    xi = i;
+}
+
 // w * x for a float w that is an exact small integer
 __device__ __forceinline__ dfl df_scale(dfl x, float w) {
     const float p = __fmul_rn(w, x.hi);

@@ -122,7 +122,9 @@ struct ArDF {
     __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
         return {df_add_lazy(c.r, dfl{d.x, d.y}), df_add_lazy(c.i, dfl{d.z, d.w})};
     }
-    __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { df_cmul(x.r, x.i, y.r, y.i); }
+    // products feed products: unnormalised pairs (df_cmul_lazy); the
+    // accumulation renormalises (df_scale, df_add)
+    __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { df_cmul_lazy(x.r, x.i, y.r, y.i); }
     __device__ __forceinline__ static acc_t zero() { return {{0.0f, 0.0f}, {0.0f, 0.0f}}; }
     __device__ __forceinline__ static void accumulate(acc_t &a, const cs_t &x, const PqgStep &s) {
         a.r = df_add(a.r, df_scale(x.r, s.wf));
