@@ -466,6 +466,55 @@ def run_ours(args, world, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def profile_case(name):
+    """Small named cases for ncu captures (no JSON line): each runs its kernel
+    a few times after building the engine.
+      gemm16k    — the tcgen05 forward GEMM, 16384 x 256 x 256, bias + GELU, 6 launches;
+      target1024 — 1024 complex64 permanents of learned-proposal patterns at
+                   n=24, d=48 (one Metropolis block's targets), 3 calls;
+      df24       — one n=24 complex128 permanent (double-float walk), 4 calls."""
+    import ctypes
+
+    import __graft_entry__
+
+    __graft_entry__.build_engine()
+    import torch
+
+    import piquasso_gb300 as pge
+    from piquasso_gb300 import _lib, metropolis, proposal, workloads
+
+    if name == "gemm16k":
+        L = _lib.load()
+        rows = 16384
+        g = torch.Generator(device="cuda").manual_seed(0)
+        A = torch.randn(rows, 256, device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn(256, 256, device="cuda", generator=g).to(torch.bfloat16)
+        bias = torch.zeros(256, device="cuda")
+        C = torch.empty(rows, 256, device="cuda")
+        Cb = torch.empty(rows, 256, device="cuda", dtype=torch.bfloat16)
+        fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))  # noqa: E731
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        for _ in range(6):
+            assert L.pqg_mlp_gemm_tc(vp(A), 256, vp(B), 256, rows, 256, 256, 1, fp(C), vp(Cb), fp(bias), None, None,
+                                     0, None) == 0
+        torch.cuda.synchronize()
+    elif name == "target1024":
+        U = workloads.haar_unitary(48, 3)
+        inp = np.array([1] * 24 + [0] * 24)
+        ps = metropolis.ProposalSampler(proposal.load_mlp(), proposal.ModeStats(U, inp), 1024)
+        y, _ = ps.propose(seed=11)
+        pats = y.cpu().numpy().astype(np.int64)
+        for _ in range(3):
+            pge.permanent_batch(U.astype(np.complex64), pats, inp)
+    elif name == "df24":
+        A = haar_unitary(48, 0)[:24, :24].copy()
+        for _ in range(4):
+            pge.permanent(A, np.ones(24, int), np.ones(24, int))
+    else:
+        raise SystemExit("unknown profile case %r" % name)
+    print(json.dumps({"profile_case": name, "timing": pge.last_timing()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -480,7 +529,11 @@ def main():
     ap.add_argument("--no-sampling", action="store_true")
     ap.add_argument("--mcmc-steps", type=int, default=600)
     ap.add_argument("--exact-samples", type=int, default=32768)
+    ap.add_argument("--profile-case", default=None, help="run one small named case for ncu and exit")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.warmup < 3:
         args.warmup = 3
     world, rank, local, pg = dist_setup()
