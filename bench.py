@@ -354,6 +354,61 @@ def bench_training(args):
                              "note": "memory-bound at this shape: 64 flop/byte of operands and outputs"}}
 
 
+def bench_next_rows(args, cpu=True):
+    """The rows beyond the permanent: the permanent gradient (n=20, one
+    Laplace walk per row, against the reference's n^2 minors through the
+    reference CPU method on a sample of them), exact marginals on four and
+    five modes at n=24 (the five-mode program holds about 89 GB of degree
+    blocks in HBM), and the lossy sampler's throughput."""
+    import piquasso_gb300 as pge
+    from piquasso_gb300 import marginals, sampling, workloads
+
+    out = {}
+    n = 20
+    A = haar_unitary(2 * n, 1)[:n, :n].copy()
+    o = np.ones(n, dtype=int)
+    pge.permanent_grad(A, o, o)
+    ts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        G = pge.permanent_grad(A, o, o)
+        ts.append(time.perf_counter() - t0)
+    g = {"workload": "gradient of the n=20 all-ones permanent (complex128), leading block of Haar(40) seed 1",
+         "ms": 1e3 * statistics.median(ts), "entries": n * n}
+    if cpu:
+        import oracle
+
+        oracle.build.build(with_reference=False)
+        k = 8
+        t0 = time.perf_counter()
+        for j in range(k):  # entries (0, j): rows - e_0, cols - e_j, the reference's per-entry minor
+            r2, c2 = o.copy(), o.copy()
+            r2[0] -= 1
+            c2[j] -= 1
+            v = oracle.port_permanent(A, r2, c2)
+            assert abs(v - G[0, j]) <= 1e-9 * abs(G).max()
+        per = (time.perf_counter() - t0) / k
+        g["cpu_baseline"] = {"ms": 1e3 * per * n * n, "unit": "ms per gradient", "cores": os.cpu_count(),
+                             "kind": "port", "sample": "%d of the %d minors (reference method), scaled" % (k, n * n)}
+        g["speedup_vs_cpu"] = g["cpu_baseline"]["ms"] / g["ms"]
+    out["gradient_n20"] = g
+    U = workloads.haar_unitary(48, 3)
+    inp = np.array([1] * 24 + [0] * 24)
+    for k in (4, 5):
+        modes = tuple(range(k))
+        t0 = time.perf_counter()
+        p = marginals.marginal(inp, U, modes)
+        dt = time.perf_counter() - t0
+        out["marginal_k%d_n24" % k] = {"workload": "exact %d-mode marginal, n=24, d=48, Haar(48) seed 3" % k,
+                                        "s": dt, "outcomes": int(p.size), "sum": float(p.sum())}
+    tm = {}
+    S = sampling.generate_samples_batched(inp, 8192, U.astype(np.complex64), 5, batch_size=8192, timings=tm,
+                                          transmission=0.5)
+    out["lossy_sampler_n24_d48"] = {"workload": "uniform loss T=0.5, n=24 inputs, d=48, batched, complex64",
+                                    "samples_per_s": 8192 / tm["total_s"], "mean_photons": float(S.sum(1).mean())}
+    return out
+
+
 def run_ours(args, world, rank, local, pg):
     import __graft_entry__
 
@@ -457,6 +512,7 @@ def run_ours(args, world, rank, local, pg):
     if not args.no_variants and not args.no_sampling:
         line["sampling_n24_d48"] = bench_sampling(args)
         line["training_mlp"] = bench_training(args)
+        line["next_rows"] = bench_next_rows(args, cpu=(rank == 0 and not args.no_cpu_baseline))
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
         line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",

@@ -191,7 +191,11 @@ int permanent_port(const T *a, int nr, int nc, const int *rows, const int *cols,
             minus_all += ms;
             bc *= binom_int(m, ms);
         }
-        char parity = (minus_all % 2 == 0) ? 1 : -1;
+        // the reference stores this sign in a plain `char` (src/permanent.cpp:202,
+        // src/permanent_laplace.cpp:174): unsigned on aarch64, where -1 becomes
+        // 255 and the reference's result is wrong; a signed type gives the same
+        // values as the reference on x86-64 and the right ones everywhere
+        int parity = (minus_all % 2 == 0) ? 1 : -1;
         C prod(static_cast<T>(parity), 0);
         for (int i = 0; i < ncol; ++i)
             for (int j = 0; j < A.cols[i]; ++j) prod *= colsum[i];
@@ -267,7 +271,11 @@ int laplace_port(const T *a, int nr, int nc, const int *rows, const int *cols, i
             minus_all += ms;
             bc *= binom_int(m, ms);
         }
-        char parity = (minus_all % 2 == 0) ? 1 : -1;
+        // the reference stores this sign in a plain `char` (src/permanent.cpp:202,
+        // src/permanent_laplace.cpp:174): unsigned on aarch64, where -1 becomes
+        // 255 and the reference's result is wrong; a signed type gives the same
+        // values as the reference on x86-64 and the right ones everywhere
+        int parity = (minus_all % 2 == 0) ? 1 : -1;
         std::vector<C> prods(ncol);
         for (int l = 0; l < ncol; ++l) {
             prods[l] = static_cast<T>(parity);

@@ -185,3 +185,23 @@ def test_large_n_properties(engine):
     assert abs(pt - p) <= 2 * t
     assert abs(pc - p.conjugate()) <= 2 * t
     assert abs(ps - 2 * p) <= 4 * t
+
+
+def test_cpu_baseline_port_agrees_with_engine(engine):
+    """The CPU baseline (the reference's method restated, oracle/perm_port.cpp)
+    computes the same permanents as the engine on this host, whatever its
+    architecture (the reference keeps the term's sign in a plain char, which
+    is unsigned on aarch64)."""
+    oracle.build.build(with_reference=False)
+    for n in (8, 14):
+        A = haar_unitary(2 * n, 1)[:n, :n].copy()
+        o = np.ones(n, dtype=int)
+        r2, c2 = o.copy(), o.copy()
+        r2[0] -= 1
+        c2[1] -= 1
+        for r, c in ((o, o), (r2, c2)):
+            want = engine.permanent(A, r, c)
+            got = oracle.port_permanent(A, r, c)
+            assert abs(got - want) <= 1e-10 * abs(want)
+        lap = oracle.port_laplace(A, r2, o)
+        assert np.allclose(lap, engine.permanent_laplace(A, r2, o), rtol=1e-10, atol=0)
