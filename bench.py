@@ -528,6 +528,8 @@ def profile_case(name):
       gemm16k    — the tcgen05 forward GEMM, 16384 x 256 x 256, bias + GELU, 6 launches;
       target1024 — 1024 complex64 permanents of learned-proposal patterns at
                    n=24, d=48 (one Metropolis block's targets), 3 calls;
+      laplace24  — 1024 complex64 Laplace permanents shaped like the exact
+                   sampler's last photon step at n=24, d=48, 3 calls;
       df24       — one n=24 complex128 permanent (double-float walk), 4 calls."""
     import ctypes
 
@@ -562,6 +564,22 @@ def profile_case(name):
         pats = y.cpu().numpy().astype(np.int64)
         for _ in range(3):
             pge.permanent_batch(U.astype(np.complex64), pats, inp)
+    elif name == "laplace24":
+        # the exact sampler's last photon step at n=24, d=48: 1024 shots with 23
+        # photons placed (exact samples less one photon), 24 input columns
+        from piquasso_gb300 import sampling
+
+        U = workloads.haar_unitary(48, 3)
+        inp = np.array([1] * 24 + [0] * 24)
+        S = sampling.generate_samples_batched(inp, 1024, U.astype(np.complex64), 7)
+        rng = np.random.default_rng(1)
+        rows = S.copy()
+        for s_ in range(len(rows)):
+            nz = np.nonzero(rows[s_])[0]
+            rows[s_, nz[rng.integers(len(nz))]] -= 1
+        cols = np.broadcast_to(inp, rows.shape)
+        for _ in range(3):
+            pge.permanent_laplace_batch(U.astype(np.complex64), rows, cols)
     elif name == "df24":
         A = haar_unitary(48, 0)[:24, :24].copy()
         for _ in range(4):

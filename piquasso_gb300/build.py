@@ -38,6 +38,8 @@ CU_SOURCES = [
     "k_laplace_c128_1.cu",
     "k_laplace_c64_0.cu",
     "k_laplace_c64_1.cu",
+    "k_laplace_c64o_0.cu",
+    "k_laplace_c64o_1.cu",
 ]
 CPP_SOURCES = ["plan.cpp"]
 

@@ -91,7 +91,7 @@ struct Context {
     HostBuf h_plan, h_out;
     PlanConfig cfg;
     int blocks_per_sm = 0;  // 0: as many as fit (occupancy)
-    std::vector<int> occ_cache[5];  // blocks per SM, per kernel table, per column count
+    std::vector<int> occ_cache[6];  // blocks per SM, per kernel table, per column count
 
     int init() {
         if (ready) return PQG_OK;
@@ -119,7 +119,7 @@ Context &ctx() {
 
 // walk kernel for (form, precision, exact column count); `which` indexes the
 // occupancy cache
-const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, int *which) {
+const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_ones, int *which) {
     if (form == Form::PLAIN) {
         if (prec == Precision::C128DF) {
             *which = 4;
@@ -133,6 +133,10 @@ const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, int *which)
         return kernel_for(k_plain_c64_0, k_plain_c64_1, nc);
     }
     if (prec == Precision::C64) {
+        if (all_ones) {
+            *which = 5;
+            return kernel_for(k_laplace_c64o_0, k_laplace_c64o_1, nc);
+        }
         *which = 3;
         return kernel_for(k_laplace_c64_0, k_laplace_c64_1, nc);
     }
@@ -220,7 +224,7 @@ int enqueue_prep(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayo
 // Walk kernel of a plan, its dynamic shared memory set up, and its grid size.
 int walk_launch_config(Context &C, const Planner &pl, const KernelInfo **k, int64_t *blocks) {
     int which = 0;
-    const KernelInfo &kk = kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, &which);
+    const KernelInfo &kk = kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, &which);
     int &occ = C.occ_cache[which][pl.max_nc];
     if (occ < 0) {
         if (kk.smem_bytes > 48 * 1024)

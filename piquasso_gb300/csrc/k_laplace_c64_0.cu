@@ -5,22 +5,22 @@
 namespace pqg {
 
 const KernelInfo k_laplace_c64_0[16] = {
-    {reinterpret_cast<const void *>(&walk_laplace_c64<1>), LaplaceC64Cfg<1>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<2>), LaplaceC64Cfg<2>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<3>), LaplaceC64Cfg<3>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<4>), LaplaceC64Cfg<4>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<5>), LaplaceC64Cfg<5>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<6>), LaplaceC64Cfg<6>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<7>), LaplaceC64Cfg<7>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<8>), LaplaceC64Cfg<8>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<9>), LaplaceC64Cfg<9>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<10>), LaplaceC64Cfg<10>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<11>), LaplaceC64Cfg<11>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<12>), LaplaceC64Cfg<12>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<13>), LaplaceC64Cfg<13>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<14>), LaplaceC64Cfg<14>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<15>), LaplaceC64Cfg<15>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<16>), LaplaceC64Cfg<16>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<1, false>), LaplaceC64Cfg<1>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<2, false>), LaplaceC64Cfg<2>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<3, false>), LaplaceC64Cfg<3>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<4, false>), LaplaceC64Cfg<4>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<5, false>), LaplaceC64Cfg<5>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<6, false>), LaplaceC64Cfg<6>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<7, false>), LaplaceC64Cfg<7>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<8, false>), LaplaceC64Cfg<8>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<9, false>), LaplaceC64Cfg<9>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<10, false>), LaplaceC64Cfg<10>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<11, false>), LaplaceC64Cfg<11>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<12, false>), LaplaceC64Cfg<12>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<13, false>), LaplaceC64Cfg<13>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<14, false>), LaplaceC64Cfg<14>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<15, false>), LaplaceC64Cfg<15>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<16, false>), LaplaceC64Cfg<16>::smem_bytes},
 };
 
 }  // namespace pqg

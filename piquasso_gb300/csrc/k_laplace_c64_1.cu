@@ -5,22 +5,22 @@
 namespace pqg {
 
 const KernelInfo k_laplace_c64_1[16] = {
-    {reinterpret_cast<const void *>(&walk_laplace_c64<17>), LaplaceC64Cfg<17>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<18>), LaplaceC64Cfg<18>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<19>), LaplaceC64Cfg<19>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<20>), LaplaceC64Cfg<20>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<21>), LaplaceC64Cfg<21>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<22>), LaplaceC64Cfg<22>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<23>), LaplaceC64Cfg<23>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<24>), LaplaceC64Cfg<24>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<25>), LaplaceC64Cfg<25>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<26>), LaplaceC64Cfg<26>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<27>), LaplaceC64Cfg<27>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<28>), LaplaceC64Cfg<28>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<29>), LaplaceC64Cfg<29>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<30>), LaplaceC64Cfg<30>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<31>), LaplaceC64Cfg<31>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_laplace_c64<32>), LaplaceC64Cfg<32>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<17, false>), LaplaceC64Cfg<17>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<18, false>), LaplaceC64Cfg<18>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<19, false>), LaplaceC64Cfg<19>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<20, false>), LaplaceC64Cfg<20>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<21, false>), LaplaceC64Cfg<21>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<22, false>), LaplaceC64Cfg<22>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<23, false>), LaplaceC64Cfg<23>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<24, false>), LaplaceC64Cfg<24>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<25, false>), LaplaceC64Cfg<25>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<26, false>), LaplaceC64Cfg<26>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<27, false>), LaplaceC64Cfg<27>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<28, false>), LaplaceC64Cfg<28>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<29, false>), LaplaceC64Cfg<29>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<30, false>), LaplaceC64Cfg<30>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<31, false>), LaplaceC64Cfg<31>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_laplace_c64<32, false>), LaplaceC64Cfg<32>::smem_bytes},
 };
 
 }  // namespace pqg

@@ -251,6 +251,7 @@ void Planner::finish() {
     mat_rows = mat_cols = 0;
     total_steps = total_flops = 0.0;
     max_nc = 1;
+    all_ones = true;
     df_ok = df_ok_add_;
 
     const bool c128 = prec_ == Precision::C128;
@@ -349,6 +350,7 @@ void Planner::finish() {
             cm_max = std::max(cm_max, p.cm[k]);
         }
         q.cm_max = cm_max;
+        all_ones = all_ones && cm_max == 1;
 
         // this problem's steps per lane: the plan's, but never so many that
         // the problem fills less than one warp

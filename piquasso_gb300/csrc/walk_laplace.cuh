@@ -194,8 +194,12 @@ struct LaplaceC64Cfg {
 
 // Complex64 Laplace walk: seed in double-float rounded to FP32, column sums
 // seed + Delta(t) and products in FP32, FP32 partial sums over 32 codes folded
-// into per-lane FP64 sums held in shared memory.
-template <int NC>
+// into per-lane FP64 sums held in shared memory, lanes combined in FP64 (the
+// output is complex64).  ONES: every column has multiplicity 1 (the sampler's
+// case), so the repeated-factor code is compiled out; a fully unrolled
+// 24-column step with it did not fit the instruction cache (ncu: 9.7
+// no-instruction stalls per issue, 11 % issue).
+template <int NC, bool ONES>
 __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_laplace_c64(WalkArgs A) {
     using Cfg = LaplaceC64Cfg<NC>;
     extern __shared__ double2 lap_smem64[];
@@ -229,10 +233,12 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                 }
                 wout = outer_weight(pr, st);
             }
-            int cm[NC];
+            int cm[ONES ? 1 : NC];
+            if constexpr (!ONES) {
 #pragma unroll
-            for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
-            const bool ones = pr->cm_max == 1;
+                for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
+            }
+            const bool ones = ONES || pr->cm_max == 1;
             const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
             const float2 *delta = reinterpret_cast<const float2 *>(A.delta) + pr->delta_begin;
             const int P = pr->P;
@@ -258,7 +264,14 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                 for (int j = 0; j + 1 < NC; ++j) {
                     float cr, ci;
                     col(j, cr, ci);
-                    if (j == 0 && (ones || cm[0] == 1)) {
+                    if constexpr (ONES) {
+                        if (j == 0) {
+                            xr = cr;
+                            xi = ci;
+                        } else {
+                            cmulf(xr, xi, cr, ci);
+                        }
+                    } else if (j == 0 && (ones || cm[0] == 1)) {
                         xr = cr;
                         xi = ci;
                     } else {
@@ -285,16 +298,22 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                         ti = p.y;
                         cmulf(tr, ti, sr, si);
                     }
-                    if (!ones)
-                        for (int r = 1; r < cm[l]; ++r) cmulf(tr, ti, cr, ci);
+                    if constexpr (!ONES) {
+                        if (!ones)
+                            for (int r = 1; r < cm[l]; ++r) cmulf(tr, ti, cr, ci);
+                    }
                     ar[l] += tr;
                     ai[l] += ti;
                     if (l > 0 || full) {
                         if (l == NC - 1) {
                             sr = w * cr;
                             si = w * ci;
-                            if (!ones)
-                                for (int r = 1; r < cm[l]; ++r) cmulf(sr, si, cr, ci);
+                            if constexpr (!ONES) {
+                                if (!ones)
+                                    for (int r = 1; r < cm[l]; ++r) cmulf(sr, si, cr, ci);
+                            }
+                        } else if constexpr (ONES) {
+                            cmulf(sr, si, cr, ci);
                         } else {
                             const int ee = ones ? 1 : cm[l];
                             for (int r = 0; r < ee; ++r) cmulf(sr, si, cr, ci);
@@ -320,18 +339,18 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
             }
         }
         for (int l = 0; l < n_out; ++l) {
-            ddv r{0.0, 0.0}, i{0.0, 0.0};
+            double r = 0.0, i = 0.0;
             if (q < pr->Q) {
                 const double2 a = acc64.get(l);
-                r = dd_mul_d(ddv{a.x, 0.0}, wout);
-                i = dd_mul_d(ddv{a.y, 0.0}, wout);
+                r = a.x * wout;
+                i = a.y * wout;
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
-                r = dd_add(r, dd_shfl_down(r, off));
-                i = dd_add(i, dd_shfl_down(i, off));
+                r += __shfl_down_sync(PQG_FULL_MASK, r, off);
+                i += __shfl_down_sync(PQG_FULL_MASK, i, off);
             }
-            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, ddv{r, 0.0}, ddv{i, 0.0});
         }
     }
 }
