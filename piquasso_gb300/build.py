@@ -34,6 +34,12 @@ CU_SOURCES = [
     "k_plain_c64_1.cu",
     "k_plain_df_0.cu",
     "k_plain_df_1.cu",
+    "k_plain_c128o_0.cu",
+    "k_plain_c128o_1.cu",
+    "k_plain_c64o_0.cu",
+    "k_plain_c64o_1.cu",
+    "k_plain_dfo_0.cu",
+    "k_plain_dfo_1.cu",
     "k_laplace_c128_0.cu",
     "k_laplace_c128_1.cu",
     "k_laplace_c64_0.cu",

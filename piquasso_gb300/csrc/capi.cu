@@ -91,7 +91,7 @@ struct Context {
     HostBuf h_plan, h_out;
     PlanConfig cfg;
     int blocks_per_sm = 0;  // 0: as many as fit (occupancy)
-    std::vector<int> occ_cache[6];  // blocks per SM, per kernel table, per column count
+    std::vector<int> occ_cache[9];  // blocks per SM, per kernel table, per column count
 
     int init() {
         if (ready) return PQG_OK;
@@ -122,15 +122,16 @@ Context &ctx() {
 const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_ones, int *which) {
     if (form == Form::PLAIN) {
         if (prec == Precision::C128DF) {
-            *which = 4;
-            return kernel_for(k_plain_df_0, k_plain_df_1, nc);
+            *which = all_ones ? 8 : 4;
+            return all_ones ? kernel_for(k_plain_dfo_0, k_plain_dfo_1, nc) : kernel_for(k_plain_df_0, k_plain_df_1, nc);
         }
         if (prec == Precision::C128) {
-            *which = 0;
-            return kernel_for(k_plain_c128_0, k_plain_c128_1, nc);
+            *which = all_ones ? 6 : 0;
+            return all_ones ? kernel_for(k_plain_c128o_0, k_plain_c128o_1, nc)
+                            : kernel_for(k_plain_c128_0, k_plain_c128_1, nc);
         }
-        *which = 1;
-        return kernel_for(k_plain_c64_0, k_plain_c64_1, nc);
+        *which = all_ones ? 7 : 1;
+        return all_ones ? kernel_for(k_plain_c64o_0, k_plain_c64o_1, nc) : kernel_for(k_plain_c64_0, k_plain_c64_1, nc);
     }
     if (prec == Precision::C64) {
         if (all_ones) {

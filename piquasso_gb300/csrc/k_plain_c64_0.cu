@@ -5,22 +5,22 @@
 namespace pqg {
 
 const KernelInfo k_plain_c64_0[16] = {
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 1>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 2>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 3>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 4>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 5>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 6>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 7>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 8>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 9>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 10>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 11>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 12>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 13>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 14>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 15>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArF32, 16>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 1, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 2, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 3, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 4, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 5, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 6, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 7, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 8, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 9, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 10, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 11, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 12, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 13, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 14, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 15, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArF32, 16, false>), 0},
 };
 
 }  // namespace pqg

@@ -5,22 +5,22 @@
 namespace pqg {
 
 const KernelInfo k_plain_df_0[16] = {
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 1>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 2>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 3>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 4>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 5>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 6>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 7>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 8>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 9>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 10>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 11>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 12>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 13>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 14>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 15>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 16>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 1, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 2, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 3, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 4, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 5, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 6, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 7, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 8, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 9, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 10, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 11, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 12, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 13, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 14, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 15, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 16, false>), 0},
 };
 
 }  // namespace pqg

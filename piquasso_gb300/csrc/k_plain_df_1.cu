@@ -5,22 +5,22 @@
 namespace pqg {
 
 const KernelInfo k_plain_df_1[16] = {
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 17>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 18>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 19>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 20>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 21>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 22>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 23>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 24>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 25>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 26>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 27>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 28>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 29>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 30>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 31>), 0},
-    {reinterpret_cast<const void *>(&walk_plain<ArDF, 32>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 17, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 18, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 19, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 20, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 21, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 22, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 23, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 24, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 25, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 26, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 27, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 28, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 29, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 30, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 31, false>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 32, false>), 0},
 };
 
 }  // namespace pqg

@@ -1,0 +1,26 @@
+// Walk-kernel instantiations (all-ones columns), column counts 17..32 (generated list).
+#include "walk_plain.cuh"
+#include "kernel_table.h"
+
+namespace pqg {
+
+const KernelInfo k_plain_dfo_1[16] = {
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 17, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 18, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 19, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 20, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 21, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 22, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 23, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 24, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 25, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 26, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 27, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 28, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 29, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 30, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 31, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 32, true>), 0},
+};
+
+}  // namespace pqg

@@ -19,6 +19,12 @@ extern const KernelInfo k_plain_c64_0[16];
 extern const KernelInfo k_plain_c64_1[16];
 extern const KernelInfo k_plain_df_0[16];
 extern const KernelInfo k_plain_df_1[16];
+extern const KernelInfo k_plain_c128o_0[16];  // every column of multiplicity 1
+extern const KernelInfo k_plain_c128o_1[16];
+extern const KernelInfo k_plain_c64o_0[16];
+extern const KernelInfo k_plain_c64o_1[16];
+extern const KernelInfo k_plain_dfo_0[16];
+extern const KernelInfo k_plain_dfo_1[16];
 extern const KernelInfo k_laplace_c128_0[16];
 extern const KernelInfo k_laplace_c128_1[16];
 extern const KernelInfo k_laplace_c64_0[16];

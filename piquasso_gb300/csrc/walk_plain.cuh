@@ -372,7 +372,10 @@ constexpr int walk_min_blocks() {
     return NC <= 8 ? 4 : (NC <= 16 ? 3 : 2);
 }
 
-template <class Ar, int NC>
+// ONES: every column of every problem has multiplicity 1 (the usual case:
+// unit input photons), so the repeated-factor code is compiled out — a
+// smaller loop body for the instruction cache and the register allocator.
+template <class Ar, int NC, bool ONES>
 __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_plain(WalkArgs A) {
     using cs_t = typename Ar::cs_t;
     using d_t = typename Ar::d_t;
@@ -396,7 +399,7 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
             // column multiplicities are read from the problem (L1) only when
             // some exceed 1; keeping them out of registers leaves room for the sums
             const uint8_t *cm = pr->cm;
-            const bool ones = pr->cm_max == 1;
+            const bool ones = ONES || pr->cm_max == 1;
             const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
             const d_t *D = reinterpret_cast<const d_t *>(A.arena + pr->off_D);
             const d_t *delta = reinterpret_cast<const d_t *>(A.delta) + pr->delta_begin;
