@@ -406,6 +406,7 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
     st = run_plan<T>(C, pl, res.data(), nullptr);
     if (st) return st;
     const int64_t stride = 2 * std::max<int64_t>(1, nc);
+    std::vector<int> slot(static_cast<size_t>(std::max<int64_t>(1, nc)));
     for (int64_t b = 0; b < batch; ++b) {
         const PendingProblem &pp = pl.pending[static_cast<size_t>(b)];
         const int64_t oi = pl.probs[static_cast<size_t>(b)].out_index;
@@ -417,10 +418,10 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
             if (n_out) n_out[b] = 1;
             continue;
         }
+        laplace_slots(pp, nc, slot.data());
         for (int64_t j = 0; j < nc; ++j) {
-            const int slot = pp.out_map[static_cast<size_t>(j)];
-            o[2 * j] = res[2 * (oi + slot)];
-            o[2 * j + 1] = res[2 * (oi + slot) + 1];
+            o[2 * j] = res[2 * (oi + slot[j])];
+            o[2 * j + 1] = res[2 * (oi + slot[j]) + 1];
         }
         if (n_out) n_out[b] = nc;
     }
@@ -497,18 +498,19 @@ int grad_batch(const double *mats, int64_t nr, int64_t nc, const int32_t *rows, 
     std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
     st = run_plan<T>(C, pl, res.data(), nullptr);
     if (st) return st;
+    std::vector<int> slot(static_cast<size_t>(std::max<int64_t>(1, nc)));
     for (size_t q = 0; q < minors.size(); ++q) {
         const Minor &mi = minors[q];
         const PendingProblem &pp = pl.pending[q];
+        laplace_slots(pp, nc, slot.data());
         const int64_t oi = pl.probs[q].out_index;
         const int32_t *rb = rows + mi.b * nr, *cb = cols + mi.b * nc;
         T *o = out + static_cast<size_t>(mi.b) * per + 2 * mi.i * nc;
         for (int64_t j = 0; j < nc; ++j) {
             if (cb[j] == 0) continue;
             const double f = static_cast<double>(rb[mi.i]) * static_cast<double>(cb[j]);
-            const int slot = pp.out_map[static_cast<size_t>(j)];
-            o[2 * j] = static_cast<T>(f * static_cast<double>(res[2 * (oi + slot)]));
-            o[2 * j + 1] = static_cast<T>(f * static_cast<double>(res[2 * (oi + slot) + 1]));
+            o[2 * j] = static_cast<T>(f * static_cast<double>(res[2 * (oi + slot[j])]));
+            o[2 * j + 1] = static_cast<T>(f * static_cast<double>(res[2 * (oi + slot[j]) + 1]));
         }
     }
     return PQG_OK;
@@ -831,6 +833,7 @@ int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) {
     }
     // Laplace: scatter every problem's outputs to the caller's column layout
     const int64_t stride = std::max<int64_t>(1, h->n_cols);
+    std::vector<int> slot(static_cast<size_t>(stride));
     unsigned char *o = static_cast<unsigned char *>(out);
     for (size_t b = 0; b < h->pl.pending.size(); ++b) {
         const PendingProblem &pp = h->pl.pending[b];
@@ -841,8 +844,9 @@ int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) {
             std::memcpy(ob, tmp.data() + oi * 2 * es, 2 * es);
             continue;
         }
+        laplace_slots(pp, h->n_cols, slot.data());
         for (int64_t j = 0; j < h->n_cols; ++j)
-            std::memcpy(ob + j * 2 * es, tmp.data() + (oi + pp.out_map[j]) * 2 * es, 2 * es);
+            std::memcpy(ob + j * 2 * es, tmp.data() + (oi + slot[j]) * 2 * es, 2 * es);
     }
     if (n_values) *n_values = static_cast<int64_t>(h->pl.pending.size()) * stride;
     return PQG_OK;

@@ -83,14 +83,14 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
         if (nr == 0 || nc == 0 || sr == 0) {  // src/permanent.cpp:106-108
             p.kind = PQG_KIND_CONSTANT;
             p.n_out = 1;
-            pending.push_back(std::move(p));
+            pending.push_back(p);
             return 0;
         }
     } else {
         if (nr == 0 || nc == 0 || sr == 0 || sc == 0) {  // src/permanent_laplace.cpp:52-57
             p.kind = PQG_KIND_CONSTANT;
             p.n_out = 1;
-            pending.push_back(std::move(p));
+            pending.push_back(p);
             return 0;
         }
     }
@@ -107,30 +107,31 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     if (sr > 32) df_ok_add_ = false;
 
     // columns with nonzero multiplicity
-    for (int64_t j = 0; j < nc; ++j)
-        if (cols[j] > 0) p.col.push_back(static_cast<int>(j));
-    if (p.col.empty() || static_cast<int>(p.col.size()) > PQG_MAX_COLS) {
-        err = p.col.empty() ? "no column with nonzero multiplicity"
-                            : "more than 32 distinct columns with nonzero multiplicity";
-        return p.col.empty() ? 2 : 3;
-    }
-    p.nc = static_cast<int>(p.col.size());
-    for (int j : p.col) {
+    int kept = 0;
+    for (int64_t j = 0; j < nc; ++j) {
+        if (cols[j] == 0) continue;
+        if (kept == PQG_MAX_COLS) {
+            err = "more than 32 distinct columns with nonzero multiplicity";
+            return 3;
+        }
         if (cols[j] > 255) {
             err = "column multiplicity above 255";
             return 3;
         }
-        p.cm.push_back(cols[j]);
+        p.col[kept] = static_cast<int32_t>(j);
+        p.cm[kept] = static_cast<uint8_t>(cols[j]);
+        ++kept;
     }
+    if (kept == 0) {
+        err = "no column with nonzero multiplicity";
+        return 2;
+    }
+    p.nc = kept;
 
     if (form_ == Form::LAPLACE) {
         // outputs: one per kept column; every zero-multiplicity column shares
         // one extra output (its exponent stays 0: permanent_laplace.cpp:180,210)
-        p.out_map.assign(static_cast<size_t>(nc), -1);
-        for (int k = 0; k < p.nc; ++k) p.out_map[p.col[k]] = k;
-        p.laplace_full = static_cast<int64_t>(p.col.size()) < nc;
-        for (int64_t j = 0; j < nc; ++j)
-            if (p.out_map[j] < 0) p.out_map[j] = p.nc;
+        p.laplace_full = static_cast<int64_t>(kept) < nc;
         p.n_out = p.nc + (p.laplace_full ? 1 : 0);
     }
 
@@ -148,8 +149,13 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     for (int64_t i = 0; i < nr; ++i) {
         int m = rows[i] - (i == min_idx ? 1 : 0);
         if (m <= 0) continue;
-        p.m.push_back(m);
-        p.row.push_back(static_cast<int>(row_base + i));
+        if (p.nd == PQG_MAX_OUTER) {  // every digit at least doubles S
+            S = std::ldexp(1.0, 60);
+            break;
+        }
+        p.m[p.nd] = static_cast<uint8_t>(m);  // m <= 250
+        p.row[p.nd] = static_cast<int32_t>(row_base + i);
+        ++p.nd;
         S *= (m + 1);
     }
     if (S > std::ldexp(1.0, 50)) {
@@ -160,7 +166,7 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     // and in the kernels' int64 products
     {
         double wmax = 1.0;
-        for (int m : p.m) wmax *= static_cast<double>(binom64(m, m / 2));
+        for (int i = 0; i < p.nd; ++i) wmax *= static_cast<double>(binom64(p.m[i], p.m[i] / 2));
         if (wmax > 9.0e15) {
             err = "binomial weights of the row multiplicities exceed 2^53";
             return 3;
@@ -168,8 +174,13 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     }
     p.S = S;
     p.scale_exp = static_cast<int>(sr - 1);
-    pending.push_back(std::move(p));
+    pending.push_back(p);
     return 0;
+}
+
+void laplace_slots(const PendingProblem &p, int64_t n_cols, int *slot) {
+    for (int64_t j = 0; j < n_cols; ++j) slot[j] = p.nc;  // the shared slot (only read when laplace_full)
+    for (int k = 0; k < p.nc - p.padded_cols; ++k) slot[p.col[k]] = k;
 }
 
 int64_t Planner::align_(size_t al) {
@@ -275,15 +286,13 @@ void Planner::finish() {
         for (auto &p : pending) {
             if (p.kind != PQG_KIND_WALK || p.nc == ncmax) continue;
             const int old = p.nc, add = ncmax - old;
-            p.cm.resize(ncmax, 1);
-            p.col.resize(ncmax, -1);
+            for (int k = old; k < ncmax; ++k) {
+                p.cm[k] = 1;
+                p.col[k] = -1;
+            }
             p.nc = ncmax;
             p.padded_cols = add;
-            if (laplace) {
-                for (int &slot : p.out_map)
-                    if (slot == old) slot = ncmax;
-                p.n_out = ncmax + (p.laplace_full ? 1 : 0);
-            }
+            if (laplace) p.n_out = ncmax + (p.laplace_full ? 1 : 0);
         }
     }
     // the matrix every problem indexes, once
@@ -347,7 +356,7 @@ void Planner::finish() {
         int cm_max = 1;
         for (int k = 0; k < p.nc; ++k) {
             q.cm[k] = static_cast<uint8_t>(p.cm[k]);
-            cm_max = std::max(cm_max, p.cm[k]);
+            cm_max = std::max<int>(cm_max, p.cm[k]);
         }
         q.cm_max = cm_max;
         all_ones = all_ones && cm_max == 1;
@@ -357,42 +366,42 @@ void Planner::finish() {
         const double lane_steps = std::max(1.0, std::min(steps_per_lane, p.S / 32.0));
         // inner digits: ascending multiplicity, greedily while the inner walk
         // fits both the lane's steps and the table limit
-        const int nd = static_cast<int>(p.m.size());
-        std::vector<int> order(nd);
+        const int nd = p.nd;
+        int order[PQG_MAX_OUTER];
         for (int i = 0; i < nd; ++i) order[i] = i;
-        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return p.m[x] < p.m[y]; });
+        std::stable_sort(order, order + nd, [&](int x, int y) { return p.m[x] < p.m[y]; });
         const double p_target = std::min<double>(static_cast<double>(p_max), lane_steps);
-        std::vector<int> inner, outer;
+        int inner[PQG_MAX_INNER], outer[PQG_MAX_OUTER];
+        int K_ = 0, no = 0;
         double P = 1.0;
-        for (int i : order) {
-            if (outer.empty() && inner.size() < PQG_MAX_INNER && P * (p.m[i] + 1) <= p_target) {
-                inner.push_back(i);
+        for (int oi = 0; oi < nd; ++oi) {
+            const int i = order[oi];
+            if (no == 0 && K_ < PQG_MAX_INNER && P * (p.m[i] + 1) <= p_target) {
+                inner[K_++] = i;
                 P *= (p.m[i] + 1);
             } else {
-                outer.push_back(i);
+                outer[no++] = i;
             }
         }
-        const size_t K = inner.size();
-        const int no = static_cast<int>(outer.size());
+        const size_t K = static_cast<size_t>(K_);
         q.P = static_cast<int32_t>(P);
         q.K = static_cast<int32_t>(K);
         q.n_outer = no;
         q.Q = static_cast<int64_t>(std::llround(p.S / P));
-        // laplace kernels walk one outer position per lane
-        q.R = laplace ? 1 : std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
+        q.R = std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
         q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / 32));
         for (int o = 0; o < no; ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
         for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
 
         // matrix rows and columns for the device prep
         {
-            std::vector<int32_t> idx;
-            idx.reserve(1 + nd + p.nc);
-            idx.push_back(p.row0);
-            for (int i : outer) idx.push_back(p.row[i]);
-            for (int i : inner) idx.push_back(p.row[i]);
-            for (int k = 0; k < p.nc; ++k) idx.push_back(p.col[k]);
-            q.off_idx = push_bytes_(idx.data(), idx.size() * sizeof(int32_t));
+            int32_t idx[1 + PQG_MAX_OUTER + PQG_MAX_COLS];
+            int c = 0;
+            idx[c++] = p.row0;
+            for (int o = 0; o < no; ++o) idx[c++] = p.row[outer[o]];
+            for (size_t k = 0; k < K; ++k) idx[c++] = p.row[inner[k]];
+            for (int k = 0; k < p.nc; ++k) idx[c++] = p.col[k];
+            q.off_idx = push_bytes_(idx, static_cast<size_t>(c) * sizeof(int32_t));
         }
         // device-built seeds and step rows in the walk's precision
         if (c128) {
@@ -406,13 +415,22 @@ void Planner::finish() {
         q.delta_begin = total_delta;
         total_delta += static_cast<int64_t>(q.P) * p.nc;
 
-        // the weight table depends only on the inner multiplicities
-        std::vector<int> mm;
-        for (int i : inner) mm.push_back(p.m[i]);
-        auto it = table_cache_.find(mm);
+        // the weight table depends only on the inner multiplicities: K <= 16
+        // of them, each below 256, packed into a 128-bit key
+        std::pair<uint64_t, uint64_t> key{static_cast<uint64_t>(K), 0};
+        for (size_t k = 0; k < K; ++k) {
+            const uint64_t v = p.m[inner[k]];
+            if (k < 7)
+                key.first |= v << (8 * (k + 1));
+            else
+                key.second |= v << (8 * (k - 7));
+        }
+        auto it = table_cache_.find(key);
         if (it != table_cache_.end()) {
             q.off_tab = it->second;
         } else {
+            std::vector<int> mm(K);
+            for (size_t k = 0; k < K; ++k) mm[k] = p.m[inner[k]];
             const std::vector<double> w = build_weights(mm, q.P);
             std::vector<PqgStep> tab(q.P);
             for (int64_t t = 0; t < q.P; ++t) {
@@ -422,7 +440,7 @@ void Planner::finish() {
                 if (df && std::fabs(w[t]) > 16777216.0) df_ok = false;  // not exact in FP32
             }
             q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep));
-            table_cache_[mm] = q.off_tab;
+            table_cache_[key] = q.off_tab;
         }
 
         const int64_t lanes = (q.Q + q.R - 1) / q.R;

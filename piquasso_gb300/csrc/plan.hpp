@@ -8,6 +8,7 @@
 // problem's seeds, step rows and prefix tables in device memory.
 #pragma once
 #include <map>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -28,23 +29,31 @@ struct PlanConfig {
     int64_t seed_steps = 0;       // steps per lane that amortise a seed; 0: per-precision default
 };
 
-// One reduced problem before its inner/outer split is fixed.
+// One reduced problem before its inner/outer split is fixed.  Fixed-size
+// (no heap storage): a batch of thousands of problems is planned without
+// per-problem allocations.
 struct PendingProblem {
     int kind = PQG_KIND_WALK;
     double cre = 1.0, cim = 0.0;
-    int nc = 0;
-    std::vector<int> cm;          // multiplicities of the kept columns
-    std::vector<int> col;         // matrix column of each kept column (-1: neutral padding)
+    int nc = 0;                   // kept columns (padded to the plan's count by finish())
+    int nd = 0;                   // digits (rows of nonzero multiplicity after the reduction)
     int row0 = 0;                 // matrix row of the prepended copy (multiplicity 1)
-    std::vector<int> m;           // digit multiplicities (>= 1)
-    std::vector<int> row;         // matrix row of each digit
     int scale_exp = 0;
     int n_out = 1;
-    bool laplace_full = false;    // Laplace form with a zero-multiplicity column
-    std::vector<int> out_map;     // Laplace: output slot of every original column
-    double S = 1.0;               // Gray-code space size
     int padded_cols = 0;          // neutral columns added to reach the plan's column count
+    bool laplace_full = false;    // Laplace form with a zero-multiplicity column (shared output nc)
+    double S = 1.0;               // Gray-code space size
+    uint8_t cm[PQG_MAX_COLS];     // multiplicities of the kept columns
+    int32_t col[PQG_MAX_COLS];    // matrix column of each kept column, ascending (-1: padding)
+    uint8_t m[PQG_MAX_OUTER];     // digit multiplicities (>= 1)
+    int32_t row[PQG_MAX_OUTER];   // matrix row of each digit
 };
+
+// Laplace outputs of a problem in the caller's column layout: original column
+// j of the matrix (0 <= j < n_cols) reads output slot slot[j]: k for the k-th
+// kept column, the shared zero-multiplicity slot nc otherwise
+// (src/permanent_laplace.cpp:180,210 keeps those columns' exponent at 0).
+void laplace_slots(const PendingProblem &p, int64_t n_cols, int *slot);
 
 class Planner {
   public:
@@ -96,7 +105,7 @@ class Planner {
     Precision prec_;
     Form form_;
     PlanConfig cfg_;
-    std::map<std::vector<int>, int64_t> table_cache_;
+    std::map<std::pair<uint64_t, uint64_t>, int64_t> table_cache_;  // packed inner multiplicities -> table
     bool df_ok_add_ = true;
     const double *a_ = nullptr;
     int64_t int_nr_ = 0, int_nc_ = 0;

@@ -7,8 +7,8 @@
 //     out_l += w * prefix_l * suffix_l * c_l^(m_l - 1),
 // and the final suffix w * prod_l c_l^(m_l) is the value shared by every
 // column of multiplicity zero (their exponent stays 0 in the reference).
-// Work split (with one outer position per lane), seeding, prefix tables and
-// reductions are those of the plain kernels.
+// Work split (R consecutive outer positions per lane), seeding, one-digit
+// outer steps, prefix tables and reductions are those of the plain kernels.
 #pragma once
 #include "walk_plain.cuh"
 
@@ -44,8 +44,9 @@ struct LaplaceC128Cfg {
         (ACC_SMEM ? size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) : 0);
 };
 
-// Complex128 Laplace walk.  One outer position per lane (R = 1), seeded in
-// FP64; the column sums of inner code t are seed + Delta(t).  Per-lane sums are
+// Complex128 Laplace walk.  R consecutive outer positions per lane, seeded in
+// FP64 and moved on by one-digit updates; the column sums of inner code t are
+// seed + Delta(t).  Per-lane sums are
 // plain FP64 over one inner walk (at most 512 codes), combined across lanes,
 // items and chunks in double-double.
 template <int NC>
@@ -64,15 +65,16 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 1) walk_laplace_c128(WalkArg
         const int ip = find_problem(A.item_begin, A.n_probs, item);
         const PqgProblem *pr = A.probs + ip;
         const int64_t local = item - pr->item_begin;
-        const int64_t q = local * PQG_ITEM_LANES + lane;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
         const int n_out = pr->n_out;
         const bool full = n_out > NC;
-        double wout = 0.0;
-        if (q < pr->Q) {
-            double sr0[NC], si0[NC];  // FP64 seed of this lane's outer position
+        const bool active = r0 < pr->Q;
+        if (active) {
+            double sr0[NC], si0[NC];  // FP64 seed of this lane's current outer position
+            OuterState st;
+            outer_decode(pr, r0, st);
             {
-                OuterState st;
-                outer_decode(pr, q, st);
                 ArF64::cs_t s[NC];
                 seed_lane<ArF64, NC>(pr, A.arena, st, s);
 #pragma unroll
@@ -80,8 +82,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 1) walk_laplace_c128(WalkArg
                     sr0[j] = s[j].r;
                     si0[j] = s[j].i;
                 }
-                wout = outer_weight(pr, st);
             }
+            double wout = outer_weight(pr, st);
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const double2 *D = reinterpret_cast<const double2 *>(A.arena + pr->off_D);
             int cm[NC];
 #pragma unroll
             for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
@@ -92,8 +96,11 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 1) walk_laplace_c128(WalkArg
 #pragma unroll
             for (int l = 0; l <= NC; ++l) acc.set(l, make_double2(0.0, 0.0));
 
+            // R consecutive outer positions: the outer weight rides on every
+            // step weight (their product stays an exact integer below 2^53)
+            for (int64_t seg = 0; seg < my_R; ++seg) {
             for (int t = 0; t < P; ++t) {
-                const double w = __ldg(&tab[t].wd);
+                const double w = __ldg(&tab[t].wd) * wout;
                 // column sums of inner code t are seed + prefix-table row t,
                 // formed where they are used (no per-step array of sums)
                 const double2 *d = delta + static_cast<int64_t>(t) * NC;
@@ -162,17 +169,29 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 1) walk_laplace_c128(WalkArg
                     acc.set(NC, a);
                 }
             }
+            if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                bool up = false;
+                const int k = outer_next(pr, st, &up);
+                const double2 *d = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = __dadd_rn(sr0[j], d[j].x);
+                    si0[j] = __dadd_rn(si0[j], d[j].y);
+                }
+                wout = outer_weight(pr, st);
+            }
+            }
         }
-        // one output at a time: scale, reduce over the warp, store
+        // one output at a time: reduce over the warp, store
         // (unrolled so that a register-resident accumulator array keeps static indices)
 #pragma unroll
         for (int l = 0; l <= NC; ++l) {
             if (l >= n_out) break;
             ddv r{0.0, 0.0}, i{0.0, 0.0};
-            if (q < pr->Q) {
+            if (active) {
                 const double2 a = acc.get(l);
-                r = dd_mul_d(ddv{a.x, 0.0}, wout);
-                i = dd_mul_d(ddv{a.y, 0.0}, wout);
+                r = ddv{a.x, 0.0};
+                i = ddv{a.y, 0.0};
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
@@ -215,15 +234,16 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
         const int ip = find_problem(A.item_begin, A.n_probs, item);
         const PqgProblem *pr = A.probs + ip;
         const int64_t local = item - pr->item_begin;
-        const int64_t q = local * PQG_ITEM_LANES + lane;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
         const int n_out = pr->n_out;
         const bool full = n_out > NC;
-        double wout = 0.0;
-        if (q < pr->Q) {
-            float sr0[NC], si0[NC];  // seed of this lane's outer position (double-float, rounded)
+        const bool active = r0 < pr->Q;
+        if (active) {
+            float sr0[NC], si0[NC];  // seed of the current outer position (double-float, rounded)
+            OuterState st;
+            outer_decode(pr, r0, st);
             {
-                OuterState st;
-                outer_decode(pr, q, st);
                 ArF32::cs_t s[NC];
                 seed_lane<ArF32, NC>(pr, A.arena, st, s);
 #pragma unroll
@@ -231,8 +251,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                     sr0[j] = s[j].r;
                     si0[j] = s[j].i;
                 }
-                wout = outer_weight(pr, st);
             }
+            double wout = outer_weight(pr, st);
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
             int cm[ONES ? 1 : NC];
             if constexpr (!ONES) {
 #pragma unroll
@@ -250,6 +272,9 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                 acc64.set(l, make_double2(0.0, 0.0));
             }
 
+            // R consecutive outer positions; the FP32 partial sums fold into
+            // the FP64 accumulators weighted by the current outer weight
+            for (int64_t seg = 0; seg < my_R; ++seg) {
             for (int t = 0; t < P; ++t) {
                 const float w = __ldg(&tab[t].wf);
                 const float2 *d = delta + static_cast<int64_t>(t) * NC;
@@ -329,21 +354,33 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                     for (int l = 0; l <= NC; ++l) {
                         if (l == NC && !full) continue;
                         double2 a = acc64.get(l);
-                        a.x += static_cast<double>(ar[l]);
-                        a.y += static_cast<double>(ai[l]);
+                        a.x = __fma_rn(wout, static_cast<double>(ar[l]), a.x);
+                        a.y = __fma_rn(wout, static_cast<double>(ai[l]), a.y);
                         acc64.set(l, a);
                         ar[l] = 0.0f;
                         ai[l] = 0.0f;
                     }
                 }
             }
+            if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                bool up = false;
+                const int k = outer_next(pr, st, &up);
+                const float2 *d = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = __fadd_rn(sr0[j], d[j].x);
+                    si0[j] = __fadd_rn(si0[j], d[j].y);
+                }
+                wout = outer_weight(pr, st);
+            }
+            }
         }
         for (int l = 0; l < n_out; ++l) {
             double r = 0.0, i = 0.0;
-            if (q < pr->Q) {
+            if (active) {
                 const double2 a = acc64.get(l);
-                r = a.x * wout;
-                i = a.y * wout;
+                r = a.x;
+                i = a.y;
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
