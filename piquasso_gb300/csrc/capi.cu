@@ -359,24 +359,32 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
                 Precision prec, T *out, double *out_lo) {
     if (batch < 0 || nr < 0 || nc < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
     Context &C = ctx();
-    std::lock_guard<std::mutex> lock(C.mu);
-    // inputs are validated before the device is touched
-    Planner pl(prec, Form::PLAIN, C.cfg);
+    // Host planning runs outside the context lock (threads plan concurrently;
+    // only the device part is serialised); inputs are validated before the
+    // device is touched.
+    Planner pl(prec, Form::PLAIN, PlanConfig{});
+    pl.pending.reserve(static_cast<size_t>(batch));
     pl.set_matrix(matrix, nr, nc);
     for (int64_t b = 0; b < batch; ++b) {
         std::string err;
         int st = pl.add(rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
         if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
     }
-    int st = C.init();
-    if (st) return st;
-    pl.set_config(C.cfg);
+    PlanConfig cfg;
+    {
+        std::lock_guard<std::mutex> lock(C.mu);
+        int st = C.init();
+        if (st) return st;
+        cfg = C.cfg;
+    }
+    pl.set_config(cfg);
     pl.finish();
     if (prec == Precision::C128DF && !pl.df_ok) {
         // outside the double-float domain: the FP64 walk
         pl.set_precision(Precision::C128);
         pl.finish();
     }
+    std::lock_guard<std::mutex> lock(C.mu);
     return run_plan<T>(C, pl, out, out_lo);
 }
 
@@ -387,24 +395,31 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
                   int64_t batch, Precision prec, T *out, int64_t *n_out) {
     if (nr < 0 || nc < 0 || batch < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
     Context &C = ctx();
-    std::lock_guard<std::mutex> lock(C.mu);
-    PlanConfig cfg = C.cfg;
-    cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
-    Planner pl(prec, Form::LAPLACE, cfg);
+    // planning and the scatter of the outputs run outside the context lock
+    Planner pl(prec, Form::LAPLACE, PlanConfig{});
+    pl.pending.reserve(static_cast<size_t>(batch));
     pl.set_matrix(matrix, nr, nc);
     for (int64_t b = 0; b < batch; ++b) {
         std::string err;
         int st = pl.add(rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
         if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
     }
-    int st = C.init();
-    if (st) return st;
-    cfg.num_sms = C.cfg.num_sms;
+    PlanConfig cfg;
+    {
+        std::lock_guard<std::mutex> lock(C.mu);
+        int st = C.init();
+        if (st) return st;
+        cfg = C.cfg;
+    }
+    cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
     pl.set_config(cfg);
     pl.finish();
     std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
-    st = run_plan<T>(C, pl, res.data(), nullptr);
-    if (st) return st;
+    {
+        std::lock_guard<std::mutex> lock(C.mu);
+        int st = run_plan<T>(C, pl, res.data(), nullptr);
+        if (st) return st;
+    }
     const int64_t stride = 2 * std::max<int64_t>(1, nc);
     std::vector<int> slot(static_cast<size_t>(std::max<int64_t>(1, nc)));
     for (int64_t b = 0; b < batch; ++b) {

@@ -117,10 +117,12 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
     An independence proposal does not depend on the chain state, so the
     proposals of `block` consecutive steps are drawn as one batch of
     chains * block patterns and their target probabilities are one batched
-    permanent launch.  That launch runs on a worker thread (the engine call
-    releases the GIL) while the next block is drawn on the device; the
-    accept/reject pass then walks the block's steps in order, exactly as a
-    step-by-step chain would.  Proposal 0 of every chain is its initial state."""
+    permanent launch.  Those launches run on two worker threads (the engine
+    call releases the GIL and plans outside its lock), so one block's host
+    planning overlaps the previous block's kernels while later blocks are
+    drawn on the device; the accept/reject pass then walks each block's steps
+    in order, exactly as a step-by-step chain would.  Proposal 0 of every
+    chain is its initial state."""
     import torch
     from concurrent.futures import ThreadPoolExecutor
 
@@ -144,28 +146,36 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
     def target(Y):
         t = time.perf_counter()
         lp = log_target(U64, Y.reshape(-1, d), inp).reshape(block, chains)
-        t_perm[0] += time.perf_counter() - t
+        t_perm[0] += time.perf_counter() - t  # summed over the two workers
         return lp
+
+    from collections import deque
 
     t0 = time.perf_counter()
     accepted = 0
     proposals = 0
     kept = []
     x = logp_x = logq_x = None
-    with ThreadPoolExecutor(max_workers=1) as ex:
-        ta = time.perf_counter()
-        Y, LQ = draw(0)
-        t_prop += time.perf_counter() - ta
-        fut = ex.submit(target, Y)
+    # two blocks' target launches in flight (one block's host planning
+    # overlaps the other's kernels); proposals are drawn ahead on this thread
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        inflight = deque()
+        nxt = 0
+        while nxt < min(2, n_blocks):
+            ta = time.perf_counter()
+            Yn, LQn = draw(nxt)
+            t_prop += time.perf_counter() - ta
+            inflight.append((Yn, LQn, ex.submit(target, Yn)))
+            nxt += 1
         for k in range(n_blocks):
-            nxt = None
-            if k + 1 < n_blocks:
+            Y, LQ, fut = inflight.popleft()
+            if nxt < n_blocks:
                 ta = time.perf_counter()
-                nxt = draw(k + 1)  # overlaps the worker's permanents of block k
+                Yn, LQn = draw(nxt)  # overlaps the workers' permanents
                 t_prop += time.perf_counter() - ta
+                inflight.append((Yn, LQn, ex.submit(target, Yn)))
+                nxt += 1
             LP = fut.result()
-            if nxt is not None:
-                fut = ex.submit(target, nxt[0])
             for s in range(block):
                 g = k * block + s  # proposal index; 0 is the initial state
                 if g > steps:
@@ -183,8 +193,6 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
                 proposals += chains
                 if record and g - 1 >= burn_in:
                     kept.append(x.copy())
-            if nxt is not None:
-                Y, LQ = nxt
     torch.cuda.synchronize()
     total = time.perf_counter() - t0
     out = {

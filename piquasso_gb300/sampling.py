@@ -237,7 +237,7 @@ def result_samples(samples, seed):
 
 
 def generate_samples_batched(input_state, shots, interferometer, seed, batch_size=2048, timings=None,
-                             transmission=None, particle_overlap=None):
+                             transmission=None, particle_overlap=None, workers=2):
     """Exact samples of the same distribution, at throughput.
 
     Same algorithm (Clifford & Clifford B, sampling.py:208-236 of the
@@ -245,11 +245,15 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
     the input, the conditional pmf over the d output modes comes from the
     Laplace permanents of (sample, current input), and one output mode is drawn.
     Differences from :func:`generate_samples`, all in the random-number
-    plumbing: one generator drives all shots, the photon order is a random
+    plumbing: each batch of shots has its own generator
+    ``np.random.default_rng((seed, batch))``, the photon order is a random
     permutation drawn up front (equivalent to picking a uniformly random
     remaining photon at every step), and the pmf and the draw are vectorised
     over shots.  The samples therefore follow the reference's distribution but
-    not its per-seed sequence.  Returns an int array (shots, d).
+    not its per-seed sequence.  Batches run on ``workers`` threads, so one
+    batch's host work (planning, pmf, draws) overlaps another's Laplace
+    launches; the result does not depend on the thread count.  Returns an int
+    array (shots, d).
 
     ``transmission`` (uniform loss): every photon is kept independently with
     this probability, so a shot samples a random subset of its photons — the
@@ -260,9 +264,11 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
     Shots with fewer photons left simply sit out the later steps.
 
     ``timings`` (optional dict) receives the seconds spent in the batched
-    Laplace calls ("laplace_s") and in total ("total_s").
+    Laplace calls summed over the workers ("laplace_s") and the wall time
+    ("total_s").
     """
     import time
+    from concurrent.futures import ThreadPoolExecutor
 
     t_start = time.perf_counter()
     U = np.asarray(interferometer)
@@ -272,20 +278,19 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
     inp = np.asarray(input_state).astype(int)
     d = len(inp)
     n = int(inp.sum())
-    rng = np.random.default_rng(seed)
-    out = np.zeros((shots, d), dtype=np.int64)
-    t_lap = 0.0
     colp = np.abs(U128) ** 2
     colp = colp / colp.sum(axis=0, keepdims=True)  # column j: landing probabilities of a photon from mode j
-    for b0 in range(0, shots, batch_size):
-        nb = min(batch_size, shots - b0)
+    fq = to_first_quantized(inp).astype(np.int64)
+    rank = np.arange(n) - np.searchsorted(fq, fq)  # rank of each input photon among its mode's photons
+
+    def one_batch(bi, nb):
+        rng = np.random.default_rng((seed, bi))
+        t_lap = 0.0
         rows = np.arange(nb)
         samples = np.zeros((nb, d), dtype=np.int64)    # the exact sampler's photons
         dist_out = np.zeros((nb, d), dtype=np.int64)   # distinguishable photons, added at the end
-        # photon p of the input (mode fq[p], rank[p] among its mode's photons)
-        # takes part in the exact sampler when it is indistinguishable and kept
-        fq = to_first_quantized(inp).astype(np.int64)
-        rank = np.arange(n) - np.searchsorted(fq, fq)
+        # photon p of the input takes part in the exact sampler when it is
+        # indistinguishable and kept
         take = np.ones((nb, n), dtype=bool)
         if particle_overlap is not None:
             from scipy.special import comb, factorial
@@ -331,7 +336,15 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
             u = rng.random(len(act)) * cdf[:, -1]
             idx = np.minimum((cdf < u[:, None]).sum(axis=1), d - 1)
             samples[act, idx] += 1
-        out[b0:b0 + nb] = samples + dist_out
+        return samples + dist_out, t_lap
+
+    batches = [(bi, min(batch_size, shots - b0)) for bi, b0 in enumerate(range(0, shots, batch_size))]
+    out = np.zeros((shots, d), dtype=np.int64)
+    t_lap = 0.0
+    with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
+        for (bi, nb), (S, tl) in zip(batches, ex.map(lambda a: one_batch(*a), batches)):
+            out[bi * batch_size:bi * batch_size + nb] = S
+            t_lap += tl
     if timings is not None:
         timings["laplace_s"] = t_lap
         timings["total_s"] = time.perf_counter() - t_start
