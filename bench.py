@@ -460,7 +460,13 @@ def run_ours(args, world, rank, local, pg):
                 "flops_basis": "FP32 flops of the double-float walk, 2^(n-1)(72n+38) (FMA = 2)",
                 "complex128_algorithmic_tflops": F / mean_walk_s / 1e12}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = None
+    # DRAM bytes (read + write) of one headline launch, from one ncu capture
+    # of the same workload (profiles/walk_plain_df_n28_dram.md)
+    if n == 28 and args.dtype == "c128":
+        roof["traffic"] = 528128
+        roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one n=28 launch"
+    else:
+        roof["traffic"] = None
     roof["peak_source"] = "measured: engine FMA-chain microkernel (pqg_measure_vector_peaks)"
     roof["walk_ms"] = 1e3 * mean_walk_s
 
@@ -530,7 +536,8 @@ def profile_case(name):
                    n=24, d=48 (one Metropolis block's targets), 3 calls;
       laplace24  — 1024 complex64 Laplace permanents shaped like the exact
                    sampler's last photon step at n=24, d=48, 3 calls;
-      df24       — one n=24 complex128 permanent (double-float walk), 4 calls."""
+      df24       — one n=24 complex128 permanent (double-float walk), 4 calls;
+      df28       — the n=28 headline permanent (double-float walk), 3 calls."""
     import ctypes
 
     import __graft_entry__
@@ -580,6 +587,10 @@ def profile_case(name):
         cols = np.broadcast_to(inp, rows.shape)
         for _ in range(3):
             pge.permanent_laplace_batch(U.astype(np.complex64), rows, cols)
+    elif name == "df28":
+        A = haar_unitary(56, 0)[:28, :28].copy()
+        for _ in range(3):
+            pge.permanent(A, np.ones(28, int), np.ones(28, int))
     elif name == "df24":
         A = haar_unitary(48, 0)[:24, :24].copy()
         for _ in range(4):
