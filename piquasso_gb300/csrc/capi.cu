@@ -157,7 +157,11 @@ struct PlanLayout {
     size_t out_bytes = 0, lo_bytes = 0;
 };
 
-size_t delta_elem_bytes(const Planner &pl) { return pl.precision() == Precision::C64 ? 8 : 16; }
+// prefix-table entry: double2 (FP64), float4 (double-float), float2 (complex64
+// Laplace) or float4 {re, re, im, im} (complex64 plain: the packed two-seed walk)
+size_t delta_elem_bytes(const Planner &pl) {
+    return (pl.precision() == Precision::C64 && pl.form() == Form::LAPLACE) ? 8 : 16;
+}
 
 PlanLayout layout_of(const Planner &pl, size_t out_elem) {
     PlanLayout L;
@@ -203,6 +207,8 @@ int enqueue_prep(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayo
     A.matrix_off = pl.matrix_off;
     A.mat_cols = pl.mat_cols;
     A.n_probs = static_cast<int32_t>(L.n_probs);
+    A.dup = (pl.precision() == Precision::C64 && pl.form() == Form::PLAIN) ? 1 : 0;
+    A.pad = 0;
     // enough blocks for every SM: several slices per problem for small batches
     const int64_t want = int64_t(C.num_sms) * 4;
     A.slices = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(64, want / std::max<int64_t>(1, L.n_probs))));

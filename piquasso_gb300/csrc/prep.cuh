@@ -33,6 +33,8 @@ struct PrepArgs {
     int64_t mat_cols;
     int32_t n_probs;
     int32_t slices;
+    int32_t dup;   // PREP_F32 only: table entries {re, re, im, im} (the packed two-seed walk)
+    int32_t pad;
 };
 
 __device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
@@ -190,7 +192,11 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             if constexpr (FMT == PREP_F64) {
                 reinterpret_cast<double2 *>(A.delta)[at] = make_double2(re, im);
             } else if constexpr (FMT == PREP_F32) {
-                reinterpret_cast<float2 *>(A.delta)[at] = make_float2(__double2float_rn(re), __double2float_rn(im));
+                const float fr = __double2float_rn(re), fi = __double2float_rn(im);
+                if (A.dup)
+                    reinterpret_cast<float4 *>(A.delta)[at] = make_float4(fr, fr, fi, fi);
+                else
+                    reinterpret_cast<float2 *>(A.delta)[at] = make_float2(fr, fi);
             } else {
                 float4 v;
                 split_df(re, v.x, v.y);

@@ -29,7 +29,8 @@ struct ArF64 {
     struct cs_t {
         double r, i;
     };
-    using d_t = double2;
+    using d_t = double2;  // outer update rows
+    using t_t = double2;  // prefix-table entries
     struct acc_t {
         double r, i;
     };
@@ -62,7 +63,8 @@ struct ArF32 {
     struct cs_t {
         float r, i;
     };
-    using d_t = float2;
+    using d_t = float2;  // outer update rows
+    using t_t = float4;  // prefix-table entries {re, re, im, im}: one load feeds both packed lanes
     struct acc_t {
         float r, cr, i, ci;  // TwoSum-compensated partial sums
     };
@@ -84,8 +86,8 @@ struct ArF32 {
         c.r = __fadd_rn(c.r, d.x);
         c.i = __fadd_rn(c.i, d.y);
     }
-    __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
-        return {__fadd_rn(c.r, d.x), __fadd_rn(c.i, d.y)};
+    __device__ __forceinline__ static cs_t sum(const cs_t &c, const t_t &d) {
+        return {__fadd_rn(c.r, d.x), __fadd_rn(c.i, d.z)};
     }
     __device__ __forceinline__ static void mul(cs_t &x, const cs_t &y) { cmulf(x.r, x.i, y.r, y.i); }
     __device__ __forceinline__ static acc_t zero() { return {0.0f, 0.0f, 0.0f, 0.0f}; }
@@ -106,6 +108,7 @@ struct ArDF {
         dfl r, i;
     };
     using d_t = float4;  // re_hi, re_lo, im_hi, im_lo
+    using t_t = float4;
     struct acc_t {
         dfl r, i;
     };
@@ -258,7 +261,7 @@ __device__ __forceinline__ void seed_lane(const PqgProblem *__restrict__ pr, con
 // join them at the end.
 template <class Ar, int NC>
 __device__ __forceinline__ typename Ar::cs_t row_product(const typename Ar::cs_t (&seed)[NC],
-                                                         const typename Ar::d_t *__restrict__ d,
+                                                         const typename Ar::t_t *__restrict__ d,
                                                          const uint8_t *__restrict__ cm, bool ones) {
     using cs_t = typename Ar::cs_t;
     constexpr bool two = Ar::kTwoChains && NC >= 4;
@@ -296,72 +299,82 @@ __device__ __forceinline__ typename Ar::cs_t row_product(const typename Ar::cs_t
     return x;
 }
 
-// The products of two seeds (two outer positions) against one prefix-table
-// row: every table value is loaded once and feeds both column sums.  Each
-// seed's product runs as two chains (even and odd columns), so four
-// independent multiply chains hide the FP32 latency.
-template <class Ar, int NC>
-__device__ __forceinline__ void row_product2(const typename Ar::cs_t (&sa)[NC], const typename Ar::cs_t (&sb)[NC],
-                                             const typename Ar::d_t *__restrict__ d,
-                                             const uint8_t *__restrict__ cm, bool ones, typename Ar::cs_t &xa,
-                                             typename Ar::cs_t &xb) {
-    using cs_t = typename Ar::cs_t;
-    using d_t = typename Ar::d_t;
+// --------------------------------------------- packed two-seed complex64 walk
+// The two outer positions a complex64 lane walks together ride side by side in
+// Blackwell's packed FP32 instructions (__fadd2_rn, __fmul2_rn, __ffma2_rn:
+// FADD2 / FMUL2 / FFMA2, each lane rounded as the scalar instruction): lane .x
+// is position A, lane .y position B.  A column sum, a complex product and a
+// compensated accumulation are then one packed instruction for both
+// positions — half the FP32 instructions of two scalar walks — and every
+// prefix-table value, stored duplicated {re, re, im, im}, is one 16-byte load
+// that feeds both lanes.
+__device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// (xr + i xi) *= (cr + i ci) per lane, with cmulf's rounding
+__device__ __forceinline__ void cmul2(float2 &xr, float2 &xi, float2 cr, float2 ci) {
+    const float2 r = __ffma2_rn(xr, cr, f2neg(__fmul2_rn(xi, ci)));
+    const float2 i = __ffma2_rn(xr, ci, __fmul2_rn(xi, cr));
+    xr = r;
+    xi = i;
+}
+
+// TwoSum-compensated s += y per lane (f_two_sum_acc)
+__device__ __forceinline__ void two_sum_acc2(float2 &s, float2 &c, float2 y) {
+    const float2 t = __fadd2_rn(s, y);
+    const float2 bb = __fadd2_rn(t, f2neg(s));
+    const float2 e = __fadd2_rn(__fadd2_rn(s, f2neg(__fadd2_rn(t, f2neg(bb)))), __fadd2_rn(y, f2neg(bb)));
+    s = t;
+    c = __fadd2_rn(c, e);
+}
+
+// Product over the columns of (seed + table row t) for both lanes: even and
+// odd columns in two packed chains (four independent chains in all).
+template <int NC>
+__device__ __forceinline__ void row_product_packed(const float2 (&sr)[NC], const float2 (&si)[NC],
+                                                   const float4 *__restrict__ d, const uint8_t *__restrict__ cm,
+                                                   bool ones, float2 &pr, float2 &pi) {
     constexpr bool two = NC >= 4;
-    const d_t d0 = d[0];
-    const cs_t a0 = Ar::sum(sa[0], d0), b0 = Ar::sum(sb[0], d0);
-    cs_t ax = a0, bx = b0, ay, by;
+    const float4 d0 = d[0];
+    const float2 c0r = __fadd2_rn(sr[0], make_float2(d0.x, d0.y)), c0i = __fadd2_rn(si[0], make_float2(d0.z, d0.w));
+    float2 xr = c0r, xi = c0i, yr, yi;
     if constexpr (two) {
-        const d_t d1 = d[1];
-        ay = Ar::sum(sa[1], d1);
-        by = Ar::sum(sb[1], d1);
+        const float4 d1 = d[1];
+        yr = __fadd2_rn(sr[1], make_float2(d1.x, d1.y));
+        yi = __fadd2_rn(si[1], make_float2(d1.z, d1.w));
     }
     if (ones) {
 #pragma unroll
         for (int j = two ? 2 : 1; j < NC; ++j) {
-            const d_t dj = d[j];
-            const cs_t ca = Ar::sum(sa[j], dj), cb = Ar::sum(sb[j], dj);
-            if (two && (j & 1)) {
-                Ar::mul(ay, ca);
-                Ar::mul(by, cb);
-            } else {
-                Ar::mul(ax, ca);
-                Ar::mul(bx, cb);
-            }
+            const float4 dj = d[j];
+            const float2 cr = __fadd2_rn(sr[j], make_float2(dj.x, dj.y));
+            const float2 ci = __fadd2_rn(si[j], make_float2(dj.z, dj.w));
+            if (two && (j & 1))
+                cmul2(yr, yi, cr, ci);
+            else
+                cmul2(xr, xi, cr, ci);
         }
     } else {
-        for (int r = 1; r < cm[0]; ++r) {
-            Ar::mul(ax, a0);
-            Ar::mul(bx, b0);
-        }
+        for (int r = 1; r < cm[0]; ++r) cmul2(xr, xi, c0r, c0i);
         if constexpr (two) {
-            const cs_t a1 = ay, b1 = by;
-            for (int r = 1; r < cm[1]; ++r) {
-                Ar::mul(ay, a1);
-                Ar::mul(by, b1);
-            }
+            const float2 c1r = yr, c1i = yi;
+            for (int r = 1; r < cm[1]; ++r) cmul2(yr, yi, c1r, c1i);
         }
 #pragma unroll
         for (int j = two ? 2 : 1; j < NC; ++j) {
-            const d_t dj = d[j];
-            const cs_t ca = Ar::sum(sa[j], dj), cb = Ar::sum(sb[j], dj);
+            const float4 dj = d[j];
+            const float2 cr = __fadd2_rn(sr[j], make_float2(dj.x, dj.y));
+            const float2 ci = __fadd2_rn(si[j], make_float2(dj.z, dj.w));
             for (int r = 0; r < cm[j]; ++r) {
-                if (two && (j & 1)) {
-                    Ar::mul(ay, ca);
-                    Ar::mul(by, cb);
-                } else {
-                    Ar::mul(ax, ca);
-                    Ar::mul(bx, cb);
-                }
+                if (two && (j & 1))
+                    cmul2(yr, yi, cr, ci);
+                else
+                    cmul2(xr, xi, cr, ci);
             }
         }
     }
-    if constexpr (two) {
-        Ar::mul(ax, ay);
-        Ar::mul(bx, by);
-    }
-    xa = ax;
-    xb = bx;
+    if constexpr (two) cmul2(xr, xi, yr, yi);
+    pr = xr;
+    pi = xi;
 }
 
 // Blocks per SM the register allocation must allow: the column sums of the
@@ -379,6 +392,7 @@ template <class Ar, int NC, bool ONES>
 __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_plain(WalkArgs A) {
     using cs_t = typename Ar::cs_t;
     using d_t = typename Ar::d_t;
+    using t_t = typename Ar::t_t;
     const int lane = threadIdx.x & 31;
     for (;;) {
         const int64_t item = next_item(A.counter, lane);
@@ -402,45 +416,46 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
             const bool ones = ONES || pr->cm_max == 1;
             const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
             const d_t *D = reinterpret_cast<const d_t *>(A.arena + pr->off_D);
-            const d_t *delta = reinterpret_cast<const d_t *>(A.delta) + pr->delta_begin;
+            const t_t *delta = reinterpret_cast<const t_t *>(A.delta) + pr->delta_begin;
             const int P = pr->P;
             // lanes of a problem's last item may own fewer positions and stop
             // early; inner walks never synchronise across lanes
             const int64_t my_R = (Q - r0 < R) ? (Q - r0) : R;
             int64_t seg = 0;
             if constexpr (Ar::kTwoSeeds) {
-                // positions in pairs (seg, seg+1): seed_b is seed one outer
-                // step on, and both walk the inner codes forward (the column
-                // sums are seed + Delta(t), so the walk order is free)
+                // positions in pairs (seg, seg+1) in the two lanes of packed
+                // FP32 instructions: lane .x the current seed, lane .y the
+                // seed one outer step on; both walk the inner codes forward
+                // (the column sums are seed + Delta(t), so the walk order is free)
                 for (; seg + 1 < my_R; seg += 2) {
-                    cs_t sb[NC];
+                    float2 pr2[NC], pi2[NC];
+                    bool up = false;
+                    int k = outer_next(pr, st, &up);
+                    const d_t *db = D + (2 * k + (up ? 0 : 1)) * NC;
 #pragma unroll
-                    for (int j = 0; j < NC; ++j) sb[j] = seed[j];
-                    {
-                        bool up = false;
-                        const int k = outer_next(pr, st, &up);
-                        const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
-#pragma unroll
-                        for (int j = 0; j < NC; ++j) Ar::update(sb[j], d[j]);
+                    for (int j = 0; j < NC; ++j) {
+                        const d_t dj = db[j];
+                        pr2[j] = make_float2(seed[j].r, __fadd_rn(seed[j].r, dj.x));
+                        pi2[j] = make_float2(seed[j].i, __fadd_rn(seed[j].i, dj.y));
                     }
                     const double wb = outer_weight(pr, st);
-                    typename Ar::acc_t acc_a = Ar::zero(), acc_b = Ar::zero();
+                    float2 accr = make_float2(0.0f, 0.0f), accrc = accr, acci = accr, accic = accr;
                     for (int t = 0; t < P; ++t) {
-                        cs_t xa, xb;
-                        row_product2<Ar, NC>(seed, sb, delta + static_cast<int64_t>(t) * NC, cm, ones, xa, xb);
-                        const PqgStep w = tab[t];
-                        Ar::accumulate(acc_a, xa, w);
-                        Ar::accumulate(acc_b, xb, w);
+                        float2 xr, xi;
+                        row_product_packed<NC>(pr2, pi2, delta + static_cast<int64_t>(t) * NC, cm, ones, xr, xi);
+                        const float wf = tab[t].wf;
+                        const float2 w2 = make_float2(wf, wf);
+                        two_sum_acc2(accr, accrc, __fmul2_rn(w2, xr));
+                        two_sum_acc2(acci, accic, __fmul2_rn(w2, xi));
                     }
-                    Ar::fold(sr, si, acc_a, wout);
-                    Ar::fold(sr, si, acc_b, wb);
+                    Ar::fold(sr, si, typename Ar::acc_t{accr.x, accrc.x, acci.x, accic.x}, wout);
+                    Ar::fold(sr, si, typename Ar::acc_t{accr.y, accrc.y, acci.y, accic.y}, wb);
                     if (seg + 2 < my_R) {  // seed moves on to position seg + 2
-                        bool up = false;
-                        const int k = outer_next(pr, st, &up);
+                        k = outer_next(pr, st, &up);
                         const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
 #pragma unroll
                         for (int j = 0; j < NC; ++j) {
-                            seed[j] = sb[j];
+                            seed[j] = cs_t{pr2[j].y, pi2[j].y};
                             Ar::update(seed[j], d[j]);
                         }
                         wout = outer_weight(pr, st);
