@@ -95,6 +95,23 @@ int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64
 int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                                     const int32_t *cols, int64_t batch, float *out, int64_t *n_out);
 
+/* One step of the batched exact boson sampler (Clifford & Clifford algorithm
+ * B), fused on the device: for every shot b, the Laplace permanents L of
+ * (rows[b*n_rows ...] = the output photons drawn so far, cols[b*n_cols ...] =
+ * the input photons placed so far), then the pmf over the n_rows output modes
+ * p_i = |sum_j cols_j L_j U[i, j]|^2 and the inverse-CDF draw
+ * modes[b] = min(#{i : cdf_i < uniforms[b] * cdf_last}, n_rows - 1).
+ * Replaces one iteration of the reference's sampling loop
+ * (piquasso/_simulators/passive/sampling.py:723-749: permanent_laplace, the
+ * pmf and the draw), batched over shots; the Laplace values stay on the device
+ * and only the drawn modes are copied back.  Every shot needs at least one
+ * output and one input photon (PQG_ERR_INVALID otherwise: the first step of a
+ * shot, with no output photon, has pmf |U[i, j]|^2 and needs no permanent). */
+int pqg_sampler_step_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                          const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes);
+int pqg_sampler_step_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                         const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes);
+
 /* Gradient of the permanent with respect to every matrix entry.
  * Replaces grad_perm (src/permanent.cpp:271-300 of the reference), reached
  * through the JAX FFI backward target PermBwd (src/jax_perm/jax_perm_core.cpp:

@@ -20,6 +20,7 @@ from .permanent import (  # noqa: F401
     permanent_grad,
     permanent_laplace,
     permanent_laplace_batch,
+    sampler_step_batch,
 )
 from .plan import PermanentPlan  # noqa: F401
 from ._lib import EngineUnavailable, get_tuning, kernel_launches, last_timing, set_tuning  # noqa: F401

@@ -45,6 +45,8 @@ SIGNATURES = {
     "pqg_permanent_laplace_c64": ([_f, _I64, _I64, _i32, _i32, _f, _i64], ctypes.c_int),
     "pqg_permanent_laplace_batch_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _d, _i64], ctypes.c_int),
     "pqg_permanent_laplace_batch_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f, _i64], ctypes.c_int),
+    "pqg_sampler_step_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _d, _i32], ctypes.c_int),
+    "pqg_sampler_step_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _d, _i32], ctypes.c_int),
     "pqg_permanent_grad_c128": ([_d, _I64, _I64, _i32, _i32, _I64, _d], ctypes.c_int),
     "pqg_permanent_grad_c64": ([_f, _I64, _I64, _i32, _i32, _I64, _f], ctypes.c_int),
     "pqg_binomial_moments_c128": ([_d, _I64, _i32, _i32, _I32, _I32, _d, _I64], ctypes.c_int),

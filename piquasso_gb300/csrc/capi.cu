@@ -23,6 +23,7 @@
 #include "plan.hpp"
 #include "prep.cuh"
 #include "reduce.cuh"
+#include "draw.cuh"
 
 namespace pqg {
 
@@ -77,7 +78,7 @@ struct HostBuf {
 
 // Device buffers of one executable plan.
 struct DeviceBuffers {
-    DevBuf plan, partials, chunk_out, out, counter, delta;
+    DevBuf plan, partials, chunk_out, out, counter, delta, draw;
 };
 
 struct Context {
@@ -274,8 +275,9 @@ int enqueue_pipeline(Context &C, DeviceBuffers &B, const Planner &pl, const Plan
                                   k->smem_bytes, s));
         if (ev_w1) PQG_CUDA(cudaEventRecord(ev_w1, s));
         if (!pl.chunks.empty()) {
-            reduce_chunks<<<static_cast<unsigned>(pl.chunks.size()), PQG_CHUNK_ITEMS, 0, s>>>(
-                reinterpret_cast<const PqgChunk *>(d + L.o_chunks), A.probs, A.partials,
+            const int n_chunks = static_cast<int>(pl.chunks.size());
+            reduce_chunks<<<static_cast<unsigned>((n_chunks + 3) / 4), 128, 0, s>>>(
+                reinterpret_cast<const PqgChunk *>(d + L.o_chunks), n_chunks, A.probs, A.partials,
                 static_cast<double *>(B.chunk_out.p));
             PQG_CUDA(cudaGetLastError());
         }
@@ -294,10 +296,19 @@ int64_t pipeline_launches(const Planner &pl) {
     return 1 + (pl.total_items > 0 ? 1 : 0) + (pl.total_items > 0 && !pl.chunks.empty() ? 1 : 0);
 }
 
+// A sampler step fused behind a Laplace plan: one uniform in, one output mode
+// out per problem (draw.cuh).
+struct DrawRequest {
+    const double *uniforms;
+    int32_t *modes;
+};
+
 // Runs a finished plan; writes n_outputs complex values (2*T each) to host `out`
-// and, if out_lo != nullptr, the low words (2 doubles per output).
+// and, if out_lo != nullptr, the low words (2 doubles per output).  With a
+// draw request the outputs stay on the device and only the drawn modes come
+// back.
 template <typename T>
-int run_plan(Context &C, Planner &pl, T *out, double *out_lo) {
+int run_plan(Context &C, Planner &pl, T *out, double *out_lo, const DrawRequest *draw = nullptr) {
     if (pl.probs.empty()) return PQG_OK;
     const PlanLayout L = layout_of(pl, sizeof(T));
     PQG_CUDA(C.h_plan.ensure(L.total));
@@ -325,6 +336,38 @@ int run_plan(Context &C, Planner &pl, T *out, double *out_lo) {
     st = enqueue_pipeline<T>(C, C.bufs, pl, L, s, C.ev0, C.ev1, k, blocks);
     if (st) return st;
     g_launches += pipeline_launches(pl);
+    if (draw) {
+        const int64_t np = L.n_probs;
+        const size_t ub = align256(sizeof(double) * np);
+        PQG_CUDA(C.bufs.draw.ensure(ub + sizeof(int32_t) * np));
+        PQG_CUDA(C.h_out.ensure(ub + sizeof(int32_t) * np));
+        unsigned char *hd = static_cast<unsigned char *>(C.h_out.p);
+        std::memcpy(hd, draw->uniforms, sizeof(double) * np);
+        unsigned char *dd = static_cast<unsigned char *>(C.bufs.draw.p);
+        PQG_CUDA(cudaMemcpyAsync(dd, hd, sizeof(double) * np, cudaMemcpyHostToDevice, s));
+        unsigned char *dplan = static_cast<unsigned char *>(C.bufs.plan.p);
+        draw_modes<T><<<static_cast<unsigned>((np + 3) / 4), 128, 0, s>>>(
+            reinterpret_cast<const PqgProblem *>(dplan + L.o_probs), static_cast<int>(np), dplan + L.o_arena,
+            pl.matrix_off, pl.mat_rows, pl.mat_cols, static_cast<const T *>(C.bufs.out.p),
+            reinterpret_cast<const double *>(dd), reinterpret_cast<int32_t *>(dd + ub));
+        PQG_CUDA(cudaGetLastError());
+        g_launches++;
+        PQG_CUDA(cudaEventRecord(C.ev2, s));
+        PQG_CUDA(cudaMemcpyAsync(hd + ub, dd + ub, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, s));
+        PQG_CUDA(cudaStreamSynchronize(s));
+        if (pl.total_items > 0) {
+            float ms = 0.0f;
+            PQG_CUDA(cudaEventElapsedTime(&ms, C.ev0, C.ev1));
+            g_walk_ms = ms;
+        }
+        float ms = 0.0f;
+        PQG_CUDA(cudaEventElapsedTime(&ms, C.evs, C.ev2));
+        g_dev_ms = ms;
+        g_h2d += static_cast<double>(sizeof(double) * np);
+        g_d2h = static_cast<double>(sizeof(int32_t) * np);
+        std::memcpy(draw->modes, hd + ub, sizeof(int32_t) * np);
+        return PQG_OK;
+    }
     PQG_CUDA(cudaEventRecord(C.ev2, s));
     unsigned char *hout = static_cast<unsigned char *>(C.h_out.p);
     PQG_CUDA(cudaMemcpyAsync(hout, C.bufs.out.p, align256(L.out_bytes) + L.lo_bytes, cudaMemcpyDeviceToHost, s));
@@ -394,15 +437,10 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     return run_plan<T>(C, pl, out, out_lo);
 }
 
-// Laplace permanents of `batch` problems sharing one matrix; problem b writes
-// 2*nc values at out + 2*nc*b (its count, 1 or nc, to n_out[b]).
-template <typename T>
-int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
-                  int64_t batch, Precision prec, T *out, int64_t *n_out) {
-    if (nr < 0 || nc < 0 || batch < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
-    Context &C = ctx();
-    // planning and the scatter of the outputs run outside the context lock
-    Planner pl(prec, Form::LAPLACE, PlanConfig{});
+// Plans `batch` Laplace problems over one matrix (outside the context lock;
+// the lock is taken only to read the device's configuration).
+int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int64_t nc, const int32_t *rows,
+                 const int32_t *cols, int64_t batch) {
     pl.pending.reserve(static_cast<size_t>(batch));
     pl.set_matrix(matrix, nr, nc);
     for (int64_t b = 0; b < batch; ++b) {
@@ -420,6 +458,43 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
     cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
     pl.set_config(cfg);
     pl.finish();
+    return PQG_OK;
+}
+
+// One step of the batched exact sampler: the Laplace permanents of shot b
+// (rows = its output photons so far, cols = its input photons so far) and the
+// draw of its next output mode with uniforms[b] (draw.cuh).
+template <typename T>
+int sampler_step(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
+                 int64_t batch, Precision prec, const double *uniforms, int32_t *modes) {
+    if (nr <= 0 || nc < 0 || batch < 0 || (batch > 0 && (!uniforms || !modes)))
+        return fail(PQG_ERR_INVALID, "invalid arguments");
+    if (nr > (int64_t(1) << 31) - 1) return fail(PQG_ERR_TOO_LARGE, "more than 2^31 - 1 output modes");
+    if (batch == 0) return PQG_OK;
+    Context &C = ctx();
+    Planner pl(prec, Form::LAPLACE, PlanConfig{});
+    int st = plan_laplace(C, pl, matrix, nr, nc, rows, cols, batch);
+    if (st) return st;
+    for (int64_t b = 0; b < batch; ++b)
+        if (pl.pending[static_cast<size_t>(b)].kind != PQG_KIND_WALK)
+            return fail(PQG_ERR_INVALID, "shot " + std::to_string(b) +
+                                             ": a sampler step needs at least one output and one input photon");
+    DrawRequest dr{uniforms, modes};
+    std::lock_guard<std::mutex> lock(C.mu);
+    return run_plan<T>(C, pl, nullptr, nullptr, &dr);
+}
+
+// Laplace permanents of `batch` problems sharing one matrix; problem b writes
+// 2*nc values at out + 2*nc*b (its count, 1 or nc, to n_out[b]).
+template <typename T>
+int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols,
+                  int64_t batch, Precision prec, T *out, int64_t *n_out) {
+    if (nr < 0 || nc < 0 || batch < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
+    Context &C = ctx();
+    // planning and the scatter of the outputs run outside the context lock
+    Planner pl(prec, Form::LAPLACE, PlanConfig{});
+    int st = plan_laplace(C, pl, matrix, nr, nc, rows, cols, batch);
+    if (st) return st;
     std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
     {
         std::lock_guard<std::mutex> lock(C.mu);
@@ -707,6 +782,18 @@ int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return laplace_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out, n_out);
+}
+
+int pqg_sampler_step_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                          const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) {
+    return sampler_step<double>(matrix, n_rows, n_cols, rows, cols, batch, Precision::C128, uniforms, modes);
+}
+
+int pqg_sampler_step_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
+                         const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) {
+    if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
+    std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
+    return sampler_step<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, uniforms, modes);
 }
 
 int pqg_permanent_grad_c128(const double *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,

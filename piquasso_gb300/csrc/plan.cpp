@@ -22,11 +22,12 @@ namespace pqg {
 
 namespace {
 
-int64_t binom64(int64_t n, int64_t k) {
-    if (k < 0 || k > n) return 0;
+// C(n, k) in FP64 (exact while below 2^53; a bound check beyond that)
+double binom_d(int n, int k) {
+    if (k < 0 || k > n) return 0.0;
     if (k > n - k) k = n - k;
-    int64_t r = 1;
-    for (int64_t i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+    double r = 1.0;
+    for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
     return r;
 }
 
@@ -58,20 +59,33 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
         err = "invalid matrix or multiplicity buffers";
         return 2;
     }
+    // one pass per side: validation, sums and (rows) the first index of the
+    // smallest nonzero multiplicity, the row the reduction copies
     int64_t sr = 0, sc = 0;
+    int32_t neg = 0;
+    int64_t min_idx = 0;
+    int minelem = 0;
     for (int64_t i = 0; i < nr; ++i) {
-        if (rows[i] < 0) {
-            err = "row multiplicities must be nonnegative";
-            return 2;
+        const int32_t r = rows[i];
+        neg |= r;
+        sr += r;
+        if (r != 0 && (minelem == 0 || r < minelem)) {
+            minelem = r;
+            min_idx = i;
         }
-        sr += rows[i];
     }
+    if (neg < 0) {
+        err = "row multiplicities must be nonnegative";
+        return 2;
+    }
+    neg = 0;
     for (int64_t j = 0; j < nc; ++j) {
-        if (cols[j] < 0) {
-            err = "column multiplicities must be nonnegative";
-            return 2;
-        }
+        neg |= cols[j];
         sc += cols[j];
+    }
+    if (neg < 0) {
+        err = "column multiplicities must be nonnegative";
+        return 2;
     }
 
     if (form_ == Form::PLAIN) {
@@ -106,21 +120,30 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     // scaling) far above the FP32 underflow threshold only for N <= 32
     if (sr > 32) df_ok_add_ = false;
 
-    // columns with nonzero multiplicity
+    // columns with nonzero multiplicity (branch-free: a slot is written for
+    // every column and kept only when its multiplicity is nonzero)
     int kept = 0;
-    for (int64_t j = 0; j < nc; ++j) {
-        if (cols[j] == 0) continue;
-        if (kept == PQG_MAX_COLS) {
-            err = "more than 32 distinct columns with nonzero multiplicity";
-            return 3;
+    int32_t cmax = 0;
+    {
+        int32_t col[PQG_MAX_COLS + 1];  // one spare slot for the columns not kept
+        uint8_t cm[PQG_MAX_COLS + 1];
+        for (int64_t j = 0; j < nc; ++j) {
+            const int32_t c = cols[j];
+            col[kept] = static_cast<int32_t>(j);
+            cm[kept] = static_cast<uint8_t>(c);
+            cmax = c > cmax ? c : cmax;
+            kept += c != 0;
+            if (kept > PQG_MAX_COLS) {
+                err = "more than 32 distinct columns with nonzero multiplicity";
+                return 3;
+            }
         }
-        if (cols[j] > 255) {
-            err = "column multiplicity above 255";
-            return 3;
-        }
-        p.col[kept] = static_cast<int32_t>(j);
-        p.cm[kept] = static_cast<uint8_t>(cols[j]);
-        ++kept;
+        std::memcpy(p.col, col, sizeof(int32_t) * kept);
+        std::memcpy(p.cm, cm, kept);
+    }
+    if (cmax > 255) {
+        err = "column multiplicity above 255";
+        return 3;
     }
     if (kept == 0) {
         err = "no column with nonzero multiplicity";
@@ -135,42 +158,42 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
         p.n_out = p.nc + (p.laplace_full ? 1 : 0);
     }
 
-    // row reduction (src/permanent.cpp:54-95)
-    int64_t min_idx = 0;
-    int minelem = 0;
-    for (int64_t i = 0; i < nr; ++i) {
-        if (minelem == 0 || (rows[i] < minelem && rows[i] != 0)) {
-            minelem = rows[i];
-            min_idx = i;
-        }
-    }
+    // row reduction (src/permanent.cpp:54-95): a copy of row min_idx (the
+    // first row with the smallest nonzero multiplicity) becomes the
+    // prepended row with multiplicity 1
     p.row0 = static_cast<int>(row_base + min_idx);
     double S = 1.0;
-    for (int64_t i = 0; i < nr; ++i) {
-        int m = rows[i] - (i == min_idx ? 1 : 0);
-        if (m <= 0) continue;
-        if (p.nd == PQG_MAX_OUTER) {  // every digit at least doubles S
-            S = std::ldexp(1.0, 60);
-            break;
+    // the binomial weights prod C(m_i, g_i) must stay exact integers in FP64
+    // and in the kernels' int64 products (only multiplicities >= 2 add to it)
+    double wmax = 1.0;
+    int nd = 0;
+    {
+        uint8_t mm[PQG_MAX_OUTER + 1];  // branch-free like the columns
+        int32_t rr[PQG_MAX_OUTER + 1];
+        for (int64_t i = 0; i < nr; ++i) {
+            const int m = rows[i] - (i == min_idx ? 1 : 0);
+            mm[nd] = static_cast<uint8_t>(m);  // m <= 250
+            rr[nd] = static_cast<int32_t>(row_base + i);
+            S *= m > 0 ? m + 1 : 1;
+            nd += m > 0;
+            if (nd > PQG_MAX_OUTER) {  // every digit at least doubles S
+                S = std::ldexp(1.0, 60);
+                nd = PQG_MAX_OUTER;
+                break;
+            }
+            if (m > 1) wmax *= binom_d(m, m / 2);
         }
-        p.m[p.nd] = static_cast<uint8_t>(m);  // m <= 250
-        p.row[p.nd] = static_cast<int32_t>(row_base + i);
-        ++p.nd;
-        S *= (m + 1);
+        p.nd = nd;
+        std::memcpy(p.m, mm, nd);
+        std::memcpy(p.row, rr, sizeof(int32_t) * nd);
     }
-    if (S > std::ldexp(1.0, 50)) {
+    if (S > 1125899906842624.0) {  // 2^50
         err = "Gray-code space above 2^50 steps";
         return 3;
     }
-    // the binomial weights prod C(m_i, g_i) must stay exact integers in FP64
-    // and in the kernels' int64 products
-    {
-        double wmax = 1.0;
-        for (int i = 0; i < p.nd; ++i) wmax *= static_cast<double>(binom64(p.m[i], p.m[i] / 2));
-        if (wmax > 9.0e15) {
-            err = "binomial weights of the row multiplicities exceed 2^53";
-            return 3;
-        }
+    if (wmax > 9.0e15) {
+        err = "binomial weights of the row multiplicities exceed 2^53";
+        return 3;
     }
     p.S = S;
     p.scale_exp = static_cast<int>(sr - 1);
@@ -368,8 +391,14 @@ void Planner::finish() {
         // fits both the lane's steps and the table limit
         const int nd = p.nd;
         int order[PQG_MAX_OUTER];
-        for (int i = 0; i < nd; ++i) order[i] = i;
-        std::stable_sort(order, order + nd, [&](int x, int y) { return p.m[x] < p.m[y]; });
+        for (int i = 0; i < nd; ++i) {  // stable insertion sort (nd <= 60; no allocation)
+            int at = i;
+            while (at > 0 && p.m[order[at - 1]] > p.m[i]) {
+                order[at] = order[at - 1];
+                --at;
+            }
+            order[at] = i;
+        }
         const double p_target = std::min<double>(static_cast<double>(p_max), lane_steps);
         int inner[PQG_MAX_INNER], outer[PQG_MAX_OUTER];
         int K_ = 0, no = 0;

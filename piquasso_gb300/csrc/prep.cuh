@@ -17,7 +17,8 @@
 //
 // Work split: `slices` blocks per problem; every block of a problem computes
 // the (cheap) column scales, slice 0 writes the seeds and rows, all slices
-// share the prefix-table entries.  The grid loops over (problem, slice).
+// share the prefix table's tiles of codes.  The grid loops over (problem,
+// slice).  Launched with 256 threads (one per code of a tile).
 #pragma once
 #include "walk_common.cuh"
 
@@ -67,6 +68,8 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
     __shared__ int colix[PQG_MAX_COLS];
     __shared__ double cscale[PQG_MAX_COLS];
     __shared__ int eshift[PQG_MAX_COLS];
+    __shared__ double2 inrow[PQG_MAX_INNER][PQG_MAX_COLS];  // inner digits' rows (unscaled)
+    __shared__ uint8_t gt[256][PQG_MAX_INNER];               // Gray digits of a tile's codes
     const double *mat = reinterpret_cast<const double *>(A.arena + A.matrix_off);
     const int64_t total = static_cast<int64_t>(A.n_probs) * A.slices;
     for (int64_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
@@ -170,38 +173,51 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             }
         }
 
-        // prefix table: entries (t, j) of this problem, spread over its slices
-        const int64_t n_ent = static_cast<int64_t>(pr->P) * nc;
-        for (int64_t e = static_cast<int64_t>(slice) * blockDim.x + threadIdx.x; e < n_ent;
-             e += static_cast<int64_t>(A.slices) * blockDim.x) {
-            const int64_t t = e / nc;
-            const int j = static_cast<int>(e - t * nc);
-            uint8_t g[PQG_MAX_INNER];
-            gray_decode_inner(pr->inner_m, K, static_cast<uint32_t>(t), g);
-            double re = 0.0, im = 0.0;
-            for (int k = 0; k < K; ++k) {
-                if (!g[k]) continue;
-                const double f = -2.0 * g[k];
-                const double2 a = ad(no + k, j);
-                re = __fma_rn(f, a.x, re);
-                im = __fma_rn(f, a.y, im);
-            }
-            re *= cscale[j];
-            im *= cscale[j];
-            const int64_t at = pr->delta_begin + e;
-            if constexpr (FMT == PREP_F64) {
-                reinterpret_cast<double2 *>(A.delta)[at] = make_double2(re, im);
-            } else if constexpr (FMT == PREP_F32) {
-                const float fr = __double2float_rn(re), fi = __double2float_rn(im);
-                if (A.dup)
-                    reinterpret_cast<float4 *>(A.delta)[at] = make_float4(fr, fr, fi, fi);
-                else
-                    reinterpret_cast<float2 *>(A.delta)[at] = make_float2(fr, fi);
-            } else {
-                float4 v;
-                split_df(re, v.x, v.y);
-                split_df(im, v.z, v.w);
-                reinterpret_cast<float4 *>(A.delta)[at] = v;
+        // prefix table, in tiles of blockDim.x codes spread over the slices:
+        // every code's Gray digits decoded once (one thread per code) and the
+        // inner rows staged in shared memory, then one thread per entry (t, j)
+        for (int k = threadIdx.x; k < K * nc; k += blockDim.x) {
+            const int kk = k / nc, j = k - kk * nc;
+            inrow[kk][j] = ad(no + kk, j);
+        }
+        const int P = pr->P;
+        const int n_tiles = (P + blockDim.x - 1) / blockDim.x;
+        for (int tile = slice; tile < n_tiles; tile += A.slices) {
+            const int t0 = tile * blockDim.x;
+            const int tc = min(static_cast<int>(blockDim.x), P - t0);
+            __syncthreads();  // inrow written / the previous tile's digits read
+            if (static_cast<int>(threadIdx.x) < tc)
+                gray_decode_inner(pr->inner_m, K, static_cast<uint32_t>(t0 + threadIdx.x), gt[threadIdx.x]);
+            __syncthreads();
+            for (int e = threadIdx.x; e < tc * nc; e += blockDim.x) {
+                const int tl = e / nc;
+                const int j = e - tl * nc;
+                const uint8_t *g = gt[tl];
+                double re = 0.0, im = 0.0;
+                for (int k = 0; k < K; ++k) {
+                    if (!g[k]) continue;
+                    const double f = -2.0 * g[k];
+                    const double2 a = inrow[k][j];
+                    re = __fma_rn(f, a.x, re);
+                    im = __fma_rn(f, a.y, im);
+                }
+                re *= cscale[j];
+                im *= cscale[j];
+                const int64_t at = pr->delta_begin + static_cast<int64_t>(t0) * nc + e;
+                if constexpr (FMT == PREP_F64) {
+                    reinterpret_cast<double2 *>(A.delta)[at] = make_double2(re, im);
+                } else if constexpr (FMT == PREP_F32) {
+                    const float fr = __double2float_rn(re), fi = __double2float_rn(im);
+                    if (A.dup)
+                        reinterpret_cast<float4 *>(A.delta)[at] = make_float4(fr, fr, fi, fi);
+                    else
+                        reinterpret_cast<float2 *>(A.delta)[at] = make_float2(fr, fi);
+                } else {
+                    float4 v;
+                    split_df(re, v.x, v.y);
+                    split_df(im, v.z, v.w);
+                    reinterpret_cast<float4 *>(A.delta)[at] = v;
+                }
             }
         }
         __syncthreads();  // the shared index and scale arrays are reused

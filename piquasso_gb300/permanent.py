@@ -232,6 +232,40 @@ def permanent_laplace_batch(matrix, rows, cols):
     return (o[..., 0] + 1j * o[..., 1]).astype(np.complex64 if single else np.complex128)
 
 
+def sampler_step_batch(matrix, rows, cols, uniforms):
+    """One fused step of the batched exact sampler for many shots.
+
+    ``rows`` (batch, d): the output photons each shot has drawn so far (at
+    least one); ``cols`` (batch, n_cols): its input photons so far (at least
+    one); ``uniforms`` (batch,) in [0, 1).  The Laplace permanents L of every
+    shot stay on the GPU, where a second kernel forms the pmf
+    p_i = |sum_j cols_j L_j U[i, j]|^2 over the d output modes and draws
+    min(#{i : cdf_i < u * cdf_last}, d - 1) — the permanent_laplace call, pmf
+    and draw of one iteration of the reference's sampling loop
+    (piquasso/_simulators/passive/sampling.py:723-749).  Returns an int64
+    array (batch,) of output modes.
+    """
+    m = _as_matrix(matrix)
+    R = np.ascontiguousarray(np.asarray(rows).astype(np.int32, casting="unsafe"))
+    C = np.ascontiguousarray(np.asarray(cols).astype(np.int32, casting="unsafe"))
+    u = np.ascontiguousarray(np.asarray(uniforms, dtype=np.float64).reshape(-1))
+    if R.ndim != 2 or R.shape[1] != m.shape[0] or C.shape != (R.shape[0], m.shape[1]) or len(u) != R.shape[0]:
+        raise PermanentInputError("rows must be (batch, %d), cols (batch, %d) and uniforms (batch,)" % m.shape)
+    out = np.zeros(R.shape[0], dtype=np.int32)
+    L = _lib.load()
+    if m.dtype == np.complex64:
+        st = L.pqg_sampler_step_c64(_ptr(m, ctypes.c_float), m.shape[0], m.shape[1], _ptr(R, ctypes.c_int32),
+                                    _ptr(C, ctypes.c_int32), R.shape[0], _ptr(u, ctypes.c_double),
+                                    _ptr(out, ctypes.c_int32))
+    else:
+        st = L.pqg_sampler_step_c128(_ptr(m, ctypes.c_double), m.shape[0], m.shape[1], _ptr(R, ctypes.c_int32),
+                                     _ptr(C, ctypes.c_int32), R.shape[0], _ptr(u, ctypes.c_double),
+                                     _ptr(out, ctypes.c_int32))
+    if st:
+        _raise_for(st)
+    return out.astype(np.int64)
+
+
 def permanent_grad(matrix, rows, cols):
     """Gradient of ``permanent(matrix, rows, cols)`` with respect to every
     matrix entry: G[i, j] = rows[i] * cols[j] * permanent(matrix, rows - e_i,

@@ -21,7 +21,7 @@ import random
 
 import numpy as np
 
-from .permanent import permanent_laplace_batch
+from .permanent import permanent_laplace_batch, sampler_step_batch
 
 
 def to_first_quantized(occupation_numbers):
@@ -263,9 +263,9 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
     (multinomial over |U[:, j]|^2), the rest go through the exact sampler.
     Shots with fewer photons left simply sit out the later steps.
 
-    ``timings`` (optional dict) receives the seconds spent in the batched
-    Laplace calls summed over the workers ("laplace_s") and the wall time
-    ("total_s").
+    ``timings`` (optional dict) receives the seconds spent in the fused
+    engine steps (Laplace permanents, pmf and draw: ``sampler_step_batch``)
+    summed over the workers ("laplace_s") and the wall time ("total_s").
     """
     import time
     from concurrent.futures import ThreadPoolExecutor
@@ -320,21 +320,22 @@ def generate_samples_batched(input_state, shots, interferometer, seed, batch_siz
             act = rows[counts > k]
             current[act, photons[act, k]] += 1
             first = samples[act].sum(axis=1) == 0
-            lap = np.zeros((len(act), d), dtype=np.complex128)
+            u = rng.random(len(act))
+            idx = np.zeros(len(act), dtype=np.int64)
             if np.any(~first):
+                # Laplace permanents, pmf sum_j cur_j L_j U[idx, j] and draw:
+                # one fused engine call, only the drawn modes come back
                 t0 = time.perf_counter()
                 sel = act[~first]
-                lap[~first] = permanent_laplace_batch(U, samples[sel], current[sel]).astype(np.complex128)
+                idx[~first] = sampler_step_batch(U, samples[sel], current[sel], u[~first])
                 t_lap += time.perf_counter() - t0
             if np.any(first):
-                # empty output: the Laplace vector is [1] at the only input column
-                f = act[first]
-                lap[np.nonzero(first)[0], photons[f, k]] = 1.0
-            amp = (current[act] * lap) @ U128.T  # amp[s, idx] = sum_j cur_j L_j U[idx, j]
-            pmf = np.abs(amp) ** 2
-            cdf = np.cumsum(pmf, axis=1)
-            u = rng.random(len(act)) * cdf[:, -1]
-            idx = np.minimum((cdf < u[:, None]).sum(axis=1), d - 1)
+                # empty output: the Laplace vector is [1] at the only input
+                # column, so the pmf is |U[idx, j]|^2 of that column
+                f = np.nonzero(first)[0]
+                pmf = np.abs(U128[:, photons[act[f], k]].T) ** 2
+                cdf = np.cumsum(pmf, axis=1)
+                idx[f] = np.minimum((cdf < (u[f] * cdf[:, -1])[:, None]).sum(axis=1), d - 1)
             samples[act, idx] += 1
         return samples + dist_out, t_lap
 
