@@ -505,7 +505,7 @@ int laplace_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *r
     std::vector<int> slot(static_cast<size_t>(std::max<int64_t>(1, nc)));
     for (int64_t b = 0; b < batch; ++b) {
         const PendingProblem &pp = pl.pending[static_cast<size_t>(b)];
-        const int64_t oi = pl.probs[static_cast<size_t>(b)].out_index;
+        const int64_t oi = pl.out_of[static_cast<size_t>(b)];
         T *o = out + b * stride;
         if (pp.kind == PQG_KIND_CONSTANT) {
             for (int64_t j = 0; j < stride; ++j) o[j] = T(0);
@@ -599,7 +599,7 @@ int grad_batch(const double *mats, int64_t nr, int64_t nc, const int32_t *rows, 
         const Minor &mi = minors[q];
         const PendingProblem &pp = pl.pending[q];
         laplace_slots(pp, nc, slot.data());
-        const int64_t oi = pl.probs[q].out_index;
+        const int64_t oi = pl.out_of[q];
         const int32_t *rb = rows + mi.b * nr, *cb = cols + mi.b * nc;
         T *o = out + static_cast<size_t>(mi.b) * per + 2 * mi.i * nc;
         for (int64_t j = 0; j < nc; ++j) {
@@ -945,7 +945,7 @@ int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) {
     unsigned char *o = static_cast<unsigned char *>(out);
     for (size_t b = 0; b < h->pl.pending.size(); ++b) {
         const PendingProblem &pp = h->pl.pending[b];
-        const int64_t oi = h->pl.probs[b].out_index;
+        const int64_t oi = h->pl.out_of[b];
         unsigned char *ob = o + b * stride * 2 * es;
         std::memset(ob, 0, stride * 2 * es);
         if (pp.kind == PQG_KIND_CONSTANT) {

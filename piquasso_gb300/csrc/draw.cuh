@@ -27,7 +27,7 @@ __global__ void draw_modes(const PqgProblem *__restrict__ probs, int n_probs, co
     if (ip >= n_probs) return;  // uniform over the warp
     const PqgProblem *pr = probs + ip;
     if (pr->kind != PQG_KIND_WALK) {  // the host rejects these before the launch
-        if (lane == 0) modes[ip] = -1;
+        if (lane == 0) modes[pr->index] = -1;
         return;
     }
     const int32_t *col = reinterpret_cast<const int32_t *>(arena + pr->off_idx) + 1 + pr->n_outer + pr->K;
@@ -67,7 +67,7 @@ __global__ void draw_modes(const PqgProblem *__restrict__ probs, int n_probs, co
     };
     double total = 0.0;
     for (int64_t i0 = 0; i0 < n_modes; i0 += 32) total += __shfl_sync(full, scan(prob(i0 + lane)), 31);
-    const double thr = uniforms[ip] * total;
+    const double thr = uniforms[pr->index] * total;
     double carry = 0.0;
     int64_t found = n_modes - 1;
     for (int64_t i0 = 0; i0 < n_modes; i0 += 32) {
@@ -79,7 +79,7 @@ __global__ void draw_modes(const PqgProblem *__restrict__ probs, int n_probs, co
         }
         carry += __shfl_sync(full, s, 31);
     }
-    if (lane == 0) modes[ip] = static_cast<int32_t>(found < n_modes - 1 ? found : n_modes - 1);
+    if (lane == 0) modes[pr->index] = static_cast<int32_t>(found < n_modes - 1 ? found : n_modes - 1);
 }
 
 }  // namespace pqg

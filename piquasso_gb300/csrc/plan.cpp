@@ -352,14 +352,32 @@ void Planner::finish() {
     };
     const int64_t d_elem = prec_ == Precision::C64 ? 8 : 16;  // one D element: float2, else double2 / float4
 
+    // Outputs stay in the caller's order; the work runs longest items first.
+    // The device queue hands out items in problem order, so the problems are
+    // laid out by descending steps per lane (an item's duration): the short
+    // items come last and fill the end of the launch (longest-processing-
+    // time-first), instead of a long item starting when the others are done.
+    out_of.assign(np, 0);
+    for (size_t b = 0; b < np; ++b) {
+        out_of[b] = total_outputs;
+        total_outputs += pending[b].n_out;
+    }
+    std::vector<double> key(np, 0.0);
+    std::vector<int32_t> order(np);
+    for (size_t b = 0; b < np; ++b) {
+        order[b] = static_cast<int32_t>(b);
+        if (pending[b].kind == PQG_KIND_WALK) key[b] = std::max(1.0, std::min(steps_per_lane, pending[b].S / 32.0));
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return key[x] > key[y]; });
+
     for (size_t ip = 0; ip < np; ++ip) {
-        PendingProblem &p = pending[ip];
+        PendingProblem &p = pending[static_cast<size_t>(order[ip])];
         PqgProblem &q = probs[ip];
         std::memset(&q, 0, sizeof(q));
         q.kind = p.kind;
+        q.index = order[ip];
         q.n_out = p.n_out;
-        q.out_index = total_outputs;
-        total_outputs += p.n_out;
+        q.out_index = out_of[static_cast<size_t>(order[ip])];
         q.item_begin = total_items;
         q.part_begin = total_parts;
         q.chunk_begin = static_cast<int64_t>(chunks.size());
@@ -419,6 +437,14 @@ void Planner::finish() {
         q.Q = static_cast<int64_t>(std::llround(p.S / P));
         q.R = std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
         q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / 32));
+        // whole warps: the outer positions spread evenly over the nearest
+        // count of items, so a problem's last item is not mostly idle lanes
+        // (an item is one warp; its lanes all run about R inner walks)
+        {
+            const int64_t per_item = PQG_ITEM_LANES * q.R;
+            const int64_t n_it = std::max<int64_t>(1, (q.Q + per_item / 2) / per_item);
+            q.R = (q.Q + PQG_ITEM_LANES * n_it - 1) / (PQG_ITEM_LANES * n_it);
+        }
         for (int o = 0; o < no; ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
         for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
 

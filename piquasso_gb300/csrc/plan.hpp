@@ -77,7 +77,8 @@ class Planner {
     void set_config(const PlanConfig &cfg) { cfg_ = cfg; }
 
     std::vector<PendingProblem> pending;
-    std::vector<PqgProblem> probs;
+    std::vector<PqgProblem> probs;     // in work order (PqgProblem::index: the pending problem)
+    std::vector<int64_t> out_of;       // first output slot of pending problem b (caller's order)
     std::vector<int64_t> item_begin;   // n_probs + 1
     std::vector<PqgChunk> chunks;
     std::vector<unsigned char> arena;  // weight tables and the matrix, by byte offset

@@ -43,7 +43,7 @@ struct PqgProblem {
     int32_t cm_max;     // largest column multiplicity
     int32_t n_out;      // outputs of this problem (1, or the Laplace count)
     int32_t col_shift;  // sum_j e_j cm_j of the double-float column scales 2^-e_j (device-written)
-    int32_t pad0;
+    int32_t index;      // the caller's problem index (problems are laid out in work order)
     int64_t Q;          // outer positions
     int64_t R;          // outer positions per lane
     int64_t item_begin; // first work item
