@@ -815,7 +815,7 @@ int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) {
     if (items_per_smsp < 0 || p_max < 0 || p_max > 32768 || seed_steps < 0)
         return fail(PQG_ERR_INVALID, "invalid tuning values");
     PlanConfig d;
-    C.cfg.items_per_smsp = items_per_smsp ? items_per_smsp : d.items_per_smsp;
+    C.cfg.items_per_smsp = items_per_smsp;  // 0: the per-arithmetic default
     C.cfg.p_max = p_max ? p_max : d.p_max;
     C.cfg.p_max_user = p_max != 0;
     C.cfg.seed_steps = seed_steps;

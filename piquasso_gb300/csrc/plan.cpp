@@ -331,7 +331,12 @@ void Planner::finish() {
     for (auto &p : pending)
         if (p.kind == PQG_KIND_WALK) S_tot += p.S;
     const double resident_warps = 4.0 * cfg_.num_sms * 3.0;
-    const double balance = S_tot / (32.0 * 4.0 * cfg_.num_sms * static_cast<double>(cfg_.items_per_smsp));
+    // (complex64 plain walks aim for twice as many items: a batch of short
+    // problems then gives each problem several consecutive items, which
+    // neighbouring warps take together and whose prefix table they share in L1)
+    const int64_t items = cfg_.items_per_smsp > 0 ? cfg_.items_per_smsp
+                                                  : (prec_ == Precision::C64 && form_ == Form::PLAIN ? 32 : 16);
+    const double balance = S_tot / (32.0 * 4.0 * cfg_.num_sms * static_cast<double>(items));
     const double seed_floor = std::min<double>(static_cast<double>(cfg_.seed_steps > 0 ? cfg_.seed_steps
                                                                                     : min_steps_per_seed(prec_)),
                                                S_tot / (32.0 * resident_warps));

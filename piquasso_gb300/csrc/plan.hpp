@@ -23,7 +23,7 @@ enum class Form { PLAIN, LAPLACE };
 
 struct PlanConfig {
     int num_sms = 152;
-    int64_t items_per_smsp = 16;  // work items per SM sub-partition the split aims for
+    int64_t items_per_smsp = 0;   // work items per SM sub-partition the split aims for (0: per arithmetic)
     int64_t p_max = 2048;         // longest inner walk (table length)
     bool p_max_user = false;      // p_max was set explicitly (overrides the per-arithmetic cap)
     int64_t seed_steps = 0;       // steps per lane that amortise a seed; 0: per-precision default

@@ -329,25 +329,32 @@ __device__ __forceinline__ void two_sum_acc2(float2 &s, float2 &c, float2 y) {
 
 // Product over the columns of (seed + table row t) for both lanes: even and
 // odd columns in two packed chains (four independent chains in all).
-template <int NC>
-__device__ __forceinline__ void row_product_packed(const float2 (&sr)[NC], const float2 (&si)[NC],
-                                                   const float4 *__restrict__ d, const uint8_t *__restrict__ cm,
+// With REFILL, software-pipelined table loads: dq holds row t on entry; each
+// entry's register is refilled with row `next`'s entry right after its column
+// sum is formed, so the next code's loads are in flight a whole product
+// ahead.  The rows then stay live across codes, which only the narrower
+// kernels' register budgets allow (REFILL_MAX_NC).
+constexpr int REFILL_MAX_NC = 24;
+template <int NC, bool REFILL>
+__device__ __forceinline__ void row_product_packed(const float2 (&sr)[NC], const float2 (&si)[NC], float4 (&dq)[NC],
+                                                   const float4 *__restrict__ next, const uint8_t *__restrict__ cm,
                                                    bool ones, float2 &pr, float2 &pi) {
     constexpr bool two = NC >= 4;
-    const float4 d0 = d[0];
-    const float2 c0r = __fadd2_rn(sr[0], make_float2(d0.x, d0.y)), c0i = __fadd2_rn(si[0], make_float2(d0.z, d0.w));
+    const float2 c0r = __fadd2_rn(sr[0], make_float2(dq[0].x, dq[0].y));
+    const float2 c0i = __fadd2_rn(si[0], make_float2(dq[0].z, dq[0].w));
+    if constexpr (REFILL) dq[0] = next[0];
     float2 xr = c0r, xi = c0i, yr, yi;
     if constexpr (two) {
-        const float4 d1 = d[1];
-        yr = __fadd2_rn(sr[1], make_float2(d1.x, d1.y));
-        yi = __fadd2_rn(si[1], make_float2(d1.z, d1.w));
+        yr = __fadd2_rn(sr[1], make_float2(dq[1].x, dq[1].y));
+        yi = __fadd2_rn(si[1], make_float2(dq[1].z, dq[1].w));
+        if constexpr (REFILL) dq[1] = next[1];
     }
     if (ones) {
 #pragma unroll
         for (int j = two ? 2 : 1; j < NC; ++j) {
-            const float4 dj = d[j];
-            const float2 cr = __fadd2_rn(sr[j], make_float2(dj.x, dj.y));
-            const float2 ci = __fadd2_rn(si[j], make_float2(dj.z, dj.w));
+            const float2 cr = __fadd2_rn(sr[j], make_float2(dq[j].x, dq[j].y));
+            const float2 ci = __fadd2_rn(si[j], make_float2(dq[j].z, dq[j].w));
+            if constexpr (REFILL) dq[j] = next[j];
             if (two && (j & 1))
                 cmul2(yr, yi, cr, ci);
             else
@@ -361,9 +368,9 @@ __device__ __forceinline__ void row_product_packed(const float2 (&sr)[NC], const
         }
 #pragma unroll
         for (int j = two ? 2 : 1; j < NC; ++j) {
-            const float4 dj = d[j];
-            const float2 cr = __fadd2_rn(sr[j], make_float2(dj.x, dj.y));
-            const float2 ci = __fadd2_rn(si[j], make_float2(dj.z, dj.w));
+            const float2 cr = __fadd2_rn(sr[j], make_float2(dq[j].x, dq[j].y));
+            const float2 ci = __fadd2_rn(si[j], make_float2(dq[j].z, dq[j].w));
+            if constexpr (REFILL) dq[j] = next[j];
             for (int r = 0; r < cm[j]; ++r) {
                 if (two && (j & 1))
                     cmul2(yr, yi, cr, ci);
@@ -440,9 +447,23 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                     }
                     const double wb = outer_weight(pr, st);
                     float2 accr = make_float2(0.0f, 0.0f), accrc = accr, acci = accr, accic = accr;
+                    constexpr bool refill = NC <= REFILL_MAX_NC;
+                    float4 dq[NC];
+                    if constexpr (refill) {
+#pragma unroll
+                        for (int j = 0; j < NC; ++j) dq[j] = delta[j];
+                    }
                     for (int t = 0; t < P; ++t) {
                         float2 xr, xi;
-                        row_product_packed<NC>(pr2, pi2, delta + static_cast<int64_t>(t) * NC, cm, ones, xr, xi);
+                        if constexpr (!refill) {
+                            const float4 *row = delta + static_cast<int64_t>(t) * NC;
+#pragma unroll
+                            for (int j = 0; j < NC; ++j) dq[j] = row[j];
+                        }
+                        // the last code reloads its own row (in bounds, unused)
+                        const int tn = t + 1 < P ? t + 1 : t;
+                        row_product_packed<NC, refill>(pr2, pi2, dq, delta + static_cast<int64_t>(tn) * NC, cm, ones, xr,
+                                                       xi);
                         const float wf = tab[t].wf;
                         const float2 w2 = make_float2(wf, wf);
                         two_sum_acc2(accr, accrc, __fmul2_rn(w2, xr));
