@@ -12,7 +12,8 @@
 //   * the seeds, the column sums with every digit at 0: a0 + sum_i m_i a_i,
 //     TwoSum-compensated in FP64;
 //   * the outer digits' rows a_o, and the one-digit update rows -2 a_o / +2 a_o;
-//   * the prefix table Delta(t)_j = sum_k -2 g_k(t) a_kj over the inner codes.
+//   * the prefix table Delta(t)_j = sum_k -2 g_k(t) a_kj over the inner codes,
+//     as the sum of two sub-tables over two groups of the inner digits.
 // A neutral padding column (index -1) has a0 = 1 and zero rows.
 //
 // Work split: `slices` blocks per problem; every block of a problem computes
@@ -25,6 +26,10 @@
 namespace pqg {
 
 enum PrepFormat : int { PREP_F64 = 0, PREP_F32 = 1, PREP_DF = 2 };
+
+// Sub-table rows (both groups) above which the prefix table is built term by
+// term instead (PL + PH > 56 needs P > 700 with the best split).
+#define PREP_SUB_MAX 56
 
 struct PrepArgs {
     PqgProblem *probs;
@@ -68,8 +73,10 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
     __shared__ int colix[PQG_MAX_COLS];
     __shared__ double cscale[PQG_MAX_COLS];
     __shared__ int eshift[PQG_MAX_COLS];
-    __shared__ double2 inrow[PQG_MAX_INNER][PQG_MAX_COLS];  // inner digits' rows (unscaled)
+    __shared__ double2 inrow[PQG_MAX_INNER][PQG_MAX_COLS];  // inner digits' rows (unscaled; unsplit tables)
+    __shared__ double2 subtab[PREP_SUB_MAX][PQG_MAX_COLS];   // DL then DH (unscaled; split tables)
     __shared__ uint8_t gt[256][PQG_MAX_INNER];               // Gray digits of a tile's codes
+    __shared__ int16_t gix[256][2];                          // their sub-table rows
     const double *mat = reinterpret_cast<const double *>(A.arena + A.matrix_off);
     const int64_t total = static_cast<int64_t>(A.n_probs) * A.slices;
     for (int64_t vb = blockIdx.x; vb < total; vb += gridDim.x) {
@@ -173,33 +180,98 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             }
         }
 
-        // prefix table, in tiles of blockDim.x codes spread over the slices:
-        // every code's Gray digits decoded once (one thread per code) and the
-        // inner rows staged in shared memory, then one thread per entry (t, j)
-        for (int k = threadIdx.x; k < K * nc; k += blockDim.x) {
-            const int kk = k / nc, j = k - kk * nc;
-            inrow[kk][j] = ad(no + kk, j);
-        }
+        // Prefix table, in tiles of blockDim.x codes spread over the slices.
+        // The inner digits split into a low group (digits 0..K1-1) and a high
+        // group: Delta(t) = DL(low digits) + DH(high digits), where DL and DH
+        // are the same sums over each group alone, tabulated in shared memory
+        // for every value of the group's digits (PL + PH entries per column
+        // instead of P, each a sum of at most K FMAs).  An entry of the table
+        // then costs one FP64 add instead of K FMAs.  Every code's Gray digits
+        // are decoded once, into its two sub-table indices.
         const int P = pr->P;
+        int K1 = 0, PL = 1, PH = P;
+        {
+            int best = 1 + P, pl = 1;
+            for (int k1 = 0; k1 <= K; ++k1) {
+                if (k1 > 0) pl *= pr->inner_m[k1 - 1] + 1;
+                const int ph = P / pl;
+                if (pl + ph < best) {
+                    best = pl + ph;
+                    K1 = k1;
+                    PL = pl;
+                    PH = ph;
+                }
+            }
+        }
+        const bool split = PL + PH <= PREP_SUB_MAX;
+        if (split) {
+            for (int e = threadIdx.x; e < (PL + PH) * nc; e += blockDim.x) {
+                const int u = e / nc, j = e - u * nc;
+                const bool low = u < PL;
+                int rest = low ? u : u - PL;
+                double re = 0.0, im = 0.0;
+                for (int k = low ? 0 : K1; k < (low ? K1 : K); ++k) {
+                    const int L = pr->inner_m[k] + 1;
+                    const int g = rest % L;
+                    rest /= L;
+                    if (!g) continue;
+                    const double f = -2.0 * g;
+                    const double2 a = ad(no + k, j);
+                    re = __fma_rn(f, a.x, re);
+                    im = __fma_rn(f, a.y, im);
+                }
+                subtab[u][j] = make_double2(re, im);
+            }
+        } else {
+            for (int k = threadIdx.x; k < K * nc; k += blockDim.x) {
+                const int kk = k / nc, j = k - kk * nc;
+                inrow[kk][j] = ad(no + kk, j);
+            }
+        }
         const int n_tiles = (P + blockDim.x - 1) / blockDim.x;
         for (int tile = slice; tile < n_tiles; tile += A.slices) {
             const int t0 = tile * blockDim.x;
             const int tc = min(static_cast<int>(blockDim.x), P - t0);
-            __syncthreads();  // inrow written / the previous tile's digits read
-            if (static_cast<int>(threadIdx.x) < tc)
-                gray_decode_inner(pr->inner_m, K, static_cast<uint32_t>(t0 + threadIdx.x), gt[threadIdx.x]);
+            __syncthreads();  // sub-tables / rows written, the previous tile's digits read
+            if (static_cast<int>(threadIdx.x) < tc) {
+                uint8_t *g = gt[threadIdx.x];
+                gray_decode_inner(pr->inner_m, K, static_cast<uint32_t>(t0 + threadIdx.x), g);
+                if (split) {
+                    int il = 0, ih = 0, sl = 1, sh = 1;
+                    for (int k = 0; k < K; ++k) {
+                        const int L = pr->inner_m[k] + 1;
+                        if (k < K1) {
+                            il += g[k] * sl;
+                            sl *= L;
+                        } else {
+                            ih += g[k] * sh;
+                            sh *= L;
+                        }
+                    }
+                    gix[threadIdx.x][0] = static_cast<int16_t>(il);
+                    gix[threadIdx.x][1] = static_cast<int16_t>(PL + ih);
+                }
+            }
             __syncthreads();
             for (int e = threadIdx.x; e < tc * nc; e += blockDim.x) {
                 const int tl = e / nc;
                 const int j = e - tl * nc;
-                const uint8_t *g = gt[tl];
-                double re = 0.0, im = 0.0;
-                for (int k = 0; k < K; ++k) {
-                    if (!g[k]) continue;
-                    const double f = -2.0 * g[k];
-                    const double2 a = inrow[k][j];
-                    re = __fma_rn(f, a.x, re);
-                    im = __fma_rn(f, a.y, im);
+                double re, im;
+                if (split) {
+                    const double2 l = subtab[gix[tl][0]][j], h = subtab[gix[tl][1]][j];
+                    re = l.x + h.x;
+                    im = l.y + h.y;
+                } else {
+                    const uint8_t *g = gt[tl];
+                    re = 0.0;
+                    im = 0.0;
+                    for (int k = 0; k < K; ++k) {
+                        if (!g[k]) continue;
+                        const double f = -2.0 * g[k];
+                        const double2 a = inrow[k][j];
+                        re = __fma_rn(f, a.x, re);
+                        im = __fma_rn(f, a.y, im);
+                    }
                 }
                 re *= cscale[j];
                 im *= cscale[j];
