@@ -231,15 +231,17 @@ int pqg_mlp_adam(float *w, void *w_bf16, const float *g, float *m1, float *m2, i
  * photons): pqg_proposal_features writes the 16 BF16 features of mode j and
  * the feasible occupation range [lo, hi]; pqg_proposal_sample draws mode j's
  * occupation from the masked softmax of `logits` (row stride 8) with a
- * counter-based generator (seed, chain, j), adds its log-probability to logq,
+ * counter-based generator (seed, chain, j) — the seed read from device memory
+ * at seed_dev when that is not null (so a captured CUDA graph of the whole
+ * draw can be replayed with new seeds) — adds its log-probability to logq,
  * and updates samples, n_rem and the mean shifts of the later modes (C: d x d
  * mode covariances; mode_stats: 12 floats per mode: p(0..4), Pr(X >= 5), mean,
  * variance, suffix sum of the means, 3 pad).  Occupations 0..7. */
 int pqg_proposal_features(int32_t j, int32_t B, int32_t d, int32_t n, const float *mode_stats, const int32_t *n_rem,
                           const float *shift, void *X_bf16, int8_t *lo, int8_t *hi, void *stream);
 int pqg_proposal_sample(int32_t j, int32_t B, int32_t d, const float *logits, const int8_t *lo, const int8_t *hi,
-                        uint64_t seed, int8_t *samples, int32_t *n_rem, float *shift, const float *C,
-                        const float *mode_stats, float *logq, void *stream);
+                        uint64_t seed, const uint64_t *seed_dev, int8_t *samples, int32_t *n_rem, float *shift,
+                        const float *C, const float *mode_stats, float *logq, void *stream);
 
 /* Allocation-free permanent — no counterpart in the reference.
  *

@@ -65,7 +65,8 @@ __global__ void features_kernel(int j, int B, int d, int n, const float *__restr
 }
 
 __global__ void sample_kernel(int j, int B, int d, const float *__restrict__ logits, const int8_t *__restrict__ lo,
-                              const int8_t *__restrict__ hi, uint64_t seed, int8_t *__restrict__ samples,
+                              const int8_t *__restrict__ hi, uint64_t seed_val, const uint64_t *__restrict__ seed_dev,
+                              int8_t *__restrict__ samples,
                               int32_t *__restrict__ n_rem, float *__restrict__ shift, const float *__restrict__ C,
                               const float *__restrict__ ms, float *__restrict__ logq) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,6 +77,7 @@ __global__ void sample_kernel(int j, int B, int d, const float *__restrict__ log
     for (int c = l; c <= h; ++c) mx = fmaxf(mx, z[c]);
     float tot = 0.0f;
     for (int c = l; c <= h; ++c) tot += expf(z[c] - mx);
+    const uint64_t seed = seed_dev ? *seed_dev : seed_val;
     const float u = uniform01(seed, static_cast<uint64_t>(b), static_cast<uint64_t>(j)) * tot;
     int pick = h;
     float acc = 0.0f;
@@ -119,14 +121,14 @@ int pqg_proposal_features(int32_t j, int32_t B, int32_t d, int32_t n, const floa
 }
 
 int pqg_proposal_sample(int32_t j, int32_t B, int32_t d, const float *logits, const int8_t *lo, const int8_t *hi,
-                        uint64_t seed, int8_t *samples, int32_t *n_rem, float *shift, const float *C,
-                        const float *mode_stats, float *logq, void *stream) {
+                        uint64_t seed, const uint64_t *seed_dev, int8_t *samples, int32_t *n_rem, float *shift,
+                        const float *C, const float *mode_stats, float *logq, void *stream) {
     if (B <= 0 || d <= 0 || j < 0 || j >= d) {
         pqg::set_last_error("pqg_proposal_sample: invalid arguments");
         return PQG_ERR_INVALID;
     }
     sample_kernel<<<(B + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
-        j, B, d, logits, lo, hi, seed, samples, n_rem, shift, C, mode_stats, logq);
+        j, B, d, logits, lo, hi, seed, seed_dev, samples, n_rem, shift, C, mode_stats, logq);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail(e, "pqg_proposal_sample");
 }

@@ -71,6 +71,8 @@ class ProposalSampler:
         self.n_rem = torch.zeros(B, dtype=torch.int32, device=device)
         self.shift = torch.zeros(B, self.d, dtype=torch.float32, device=device)
         self.logq = torch.zeros(B, dtype=torch.float32, device=device)
+        self.seed_dev = torch.zeros(1, dtype=torch.int64, device=device)
+        self.graph = None
         if baseline:
             # exact one-mode marginals; the tail mass spread over occupations 5..7
             lg = np.zeros((self.d, LD), dtype=np.float32)
@@ -79,23 +81,49 @@ class ProposalSampler:
             self.base_logits = torch.from_numpy(lg).to(device)
 
     def propose(self, seed):
+        """Draws the B patterns for `seed`: (samples int8 (B, d), logq (B,)),
+        the sampler's own device buffers (copy them before the next call).
+
+        The whole autoregressive draw (d rounds of features, the MLP and the
+        sampling kernel) is captured once as a CUDA graph and replayed with
+        the seed in device memory: hundreds of small launches become one."""
+        torch = self.torch
+        if self.graph is None:
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self._draw_rounds()  # first use: kernel attributes, allocations
+            torch.cuda.current_stream().wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                self._draw_rounds()
+            self.graph = g
+        v = int(seed) % (1 << 64)  # the bits of the uint64 seed, stored as int64
+        self.seed_dev.fill_(v - (1 << 64) if v >= (1 << 63) else v)
+        self.graph.replay()
+        return self.samples, self.logq
+
+    def _draw_rounds(self):
         L = _lib.load()
+        torch = self.torch
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self.n_rem.fill_(self.n)
         self.shift.zero_()
         self.logq.zero_()
         B, d, n = self.B, self.d, self.n
+        seed_ptr = ctypes.c_void_p(self.seed_dev.data_ptr())
         for j in range(d):
             st = L.pqg_proposal_features(j, B, d, n, _fp(self.ms), _i32(self.n_rem), _fp(self.shift),
-                                         ctypes.c_void_p(self.X.data_ptr()), _i8(self.lo), _i8(self.hi), None)
+                                         ctypes.c_void_p(self.X.data_ptr()), _i8(self.lo), _i8(self.hi), stream)
             if st:
                 raise RuntimeError(_lib.last_error())
             if self.baseline:
                 logits = self.base_logits[j].expand(B, LD).contiguous()
             else:
-                logits = self.mlp.forward(self.X)
-            st = L.pqg_proposal_sample(j, B, d, _fp(logits), _i8(self.lo), _i8(self.hi), ctypes.c_uint64(seed),
+                logits = self.mlp.forward(self.X, stream=stream)
+            st = L.pqg_proposal_sample(j, B, d, _fp(logits), _i8(self.lo), _i8(self.hi), ctypes.c_uint64(0), seed_ptr,
                                        _i8(self.samples), _i32(self.n_rem), _fp(self.shift), _fp(self.C),
-                                       _fp(self.ms), _fp(self.logq), None)
+                                       _fp(self.ms), _fp(self.logq), stream)
             if st:
                 raise RuntimeError(_lib.last_error())
         return self.samples, self.logq

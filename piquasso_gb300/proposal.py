@@ -163,12 +163,13 @@ class MLP:
         self._transpose(self.Wb[i], self.WbT[i])
 
     # ---------------------------------------------------------------- kernels
-    def _gemm(self, A, lda, B, ldb, M, N, K, epi, C, Cb=None, bias=None, pre=None, scratch=None, splits=0):
+    def _gemm(self, A, lda, B, ldb, M, N, K, epi, C, Cb=None, bias=None, pre=None, scratch=None, splits=0,
+              stream=None):
         """C = A[M x K] . B[N x K]^T (BF16, K-major) with epilogue `epi`."""
         L = _lib.load()
         fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float)) if t is not None else None  # noqa
         st = L.pqg_mlp_gemm_tc(_ptr(A), lda, _ptr(B), ldb, M, N, K, epi, fp(C), _ptr(Cb) if Cb is not None else None,
-                               fp(bias), fp(pre), fp(scratch), int(splits), None)
+                               fp(bias), fp(pre), fp(scratch), int(splits), stream)
         if st:
             raise RuntimeError("pqg_mlp_gemm_tc failed: " + _lib.last_error())
 
@@ -188,8 +189,9 @@ class MLP:
         self._transpose(src, dst)
         return dst
 
-    def forward(self, Xb, keep=False):
-        """Xb: (M, F) bf16 -> logits (M, LD) fp32 (+ activations if keep)."""
+    def forward(self, Xb, keep=False, stream=None):
+        """Xb: (M, F) bf16 -> logits (M, LD) fp32 (+ activations if keep);
+        `stream`: the CUDA stream of the GEMMs (None: the default stream)."""
         torch = self.torch
         M = Xb.shape[0]
         acts = [Xb]
@@ -199,12 +201,12 @@ class MLP:
             pre = torch.empty(M, HIDDEN, device=self.device, dtype=torch.float32)
             act = torch.empty(M, HIDDEN, device=self.device, dtype=torch.bfloat16)
             fi = h.shape[1]
-            self._gemm(h, fi, self.WbT[i], fi, M, HIDDEN, fi, 1, pre, Cb=act, bias=self.b[i])
+            self._gemm(h, fi, self.WbT[i], fi, M, HIDDEN, fi, 1, pre, Cb=act, bias=self.b[i], stream=stream)
             pres.append(pre)
             acts.append(act)
             h = act
         logits = torch.empty(M, LD, device=self.device, dtype=torch.float32)
-        self._gemm(h, HIDDEN, self.WbT[3], HIDDEN, M, LD, HIDDEN, 3, logits, bias=self.b[3])
+        self._gemm(h, HIDDEN, self.WbT[3], HIDDEN, M, LD, HIDDEN, 3, logits, bias=self.b[3], stream=stream)
         if keep:
             return logits, acts, pres
         return logits
