@@ -243,6 +243,18 @@ int pqg_proposal_sample(int32_t j, int32_t B, int32_t d, const float *logits, co
                         uint64_t seed, const uint64_t *seed_dev, int8_t *samples, int32_t *n_rem, float *shift,
                         const float *C, const float *mode_stats, float *logq, void *stream);
 
+/* The whole proposal step for mode j fused into one tensor-core kernel:
+ * pqg_proposal_features, the four-layer MLP (W1^T 256x16, W2^T and W3^T
+ * 256x256, W4^T 8x256: BF16, K-major; FP32 biases b1..b4; bias + GELU after
+ * the hidden layers) and pqg_proposal_sample, with the same roundings, per
+ * tile of 128 chains (TMA-streamed weights, TMEM accumulators, activations in
+ * shared memory).  The same chain state and seed arguments as the separate
+ * calls. */
+int pqg_proposal_step_tc(int32_t j, int32_t B, int32_t d, int32_t n, const float *mode_stats, const void *w1t,
+                         const void *w2t, const void *w3t, const void *w4t, const float *b1, const float *b2,
+                         const float *b3, const float *b4, uint64_t seed, const uint64_t *seed_dev, int8_t *samples,
+                         int32_t *n_rem, float *shift, const float *C, float *logq, void *stream);
+
 /* Allocation-free permanent — no counterpart in the reference.
  *
  * For callers that cannot allocate device memory: applications whose own

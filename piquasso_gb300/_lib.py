@@ -72,6 +72,8 @@ SIGNATURES = {
                               ctypes.c_int),
     "pqg_proposal_sample": ([_I32, _I32, _I32, _f, _i8, _i8, ctypes.c_uint64, ctypes.c_void_p, _i8, _i32, _f, _f,
                              _f, _f, ctypes.c_void_p], ctypes.c_int),
+    "pqg_proposal_step_tc": ([_I32, _I32, _I32, _I32, _f] + [ctypes.c_void_p] * 4 + [_f] * 4 +
+                             [ctypes.c_uint64, ctypes.c_void_p, _i8, _i32, _f, _f, _f, ctypes.c_void_p], ctypes.c_int),
     "pqg_set_tuning": ([_I64, _I64, _I64], ctypes.c_int),
     "pqg_get_tuning": ([_i64, _i64, _i64], ctypes.c_int),
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),

@@ -33,6 +33,7 @@
 #include <mutex>
 
 #include "../../include/pqperm_gb300.h"
+#include "proposal_math.cuh"
 
 namespace pqg {
 void set_last_error(const char *msg);
@@ -354,6 +355,222 @@ __global__ void tc_splitk_reduce(const float *__restrict__ part, int splits, int
     }
 }
 
+// ---------------------------------------------------------------------------
+// The learned proposal's whole autoregressive step for output mode j, fused:
+// per tile of 128 chains, the 16 features (FP32, rounded to BF16 as the
+// separate feature kernel does), the four layers 16 -> 256 -> 256 -> 256 -> 8
+// on tcgen05 (BF16 operands, FP32 accumulation in TMEM) with the bias + GELU
+// epilogues written back to shared memory as the next layer's A operand, and
+// the masked-softmax draw in the last epilogue.  The same instructions and
+// roundings as the separate kernels, so the patterns are the same bit for bit;
+// what goes is five launches per mode and the activations' round trips
+// through HBM.
+//
+// Shared memory (1024-aligned): the activation tile, 4 K-chunks of 128 rows x
+// 128 bytes in the 128-byte swizzle (the features use chunk 0, K = 16), two
+// 32 KB weight stages, then the barriers.  The weights (W1^T 256 x 16,
+// W2^T and W3^T 256 x 256, W4^T 8 x 256, K-major) stream through the stages as
+// 13 TMA chunks: one of W1, four each of W2, W3 and W4 (W4's 16-row boxes
+// zero-fill rows 8..15, so the last layer runs with N = 16).
+// 256 threads: warps 0-3 own the rows (thread t: row t) for the features and
+// the draw; in the hidden-layer epilogues warp w reads TMEM lanes
+// 32 (w % 4) .. + 31 and columns 128 (w / 4) .. + 127.
+constexpr int PS_THREADS = 256;
+constexpr uint32_t PS_ACT_CHUNK = TC_BM * 128;  // 16 KB
+constexpr uint32_t PS_STAGE = 256 * 128;        // 32 KB
+constexpr int PS_CHUNKS = 13;
+
+struct PsArgs {
+    int j, B, d, n;
+    const float *ms;
+    const float *bias[4];
+    const uint64_t *seed_dev;
+    uint64_t seed;
+    int8_t *samples;
+    int32_t *n_rem;
+    float *shift;
+    const float *C;
+    float *logq;
+};
+
+// byte offset of (row r, k) in a 128-row activation chunk (128-byte swizzle:
+// 16-byte piece k / 8 of row r sits at piece (k / 8) ^ (r % 8))
+__device__ __forceinline__ uint32_t act_off(int r, int k) {
+    return static_cast<uint32_t>((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 3) ^ (r & 7)) & 7) << 4) + (k & 7) * 2);
+}
+
+__global__ void __launch_bounds__(PS_THREADS, 1)
+    proposal_step_tc(const __grid_constant__ CUtensorMap w1, const __grid_constant__ CUtensorMap w2,
+                     const __grid_constant__ CUtensorMap w3, const __grid_constant__ CUtensorMap w4, PsArgs a) {
+    using namespace pqg::prop;
+    extern __shared__ uint8_t ps_smem_raw[];
+    const uint32_t raw = smem_u32(ps_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t *gbase = ps_smem_raw + (base - raw);
+    const uint32_t act = base, wst = base + 4 * PS_ACT_CHUNK;
+    const uint32_t bar0 = wst + 2 * PS_STAGE;  // full[2] at +0/+8, empty[2] at +16/+24, done at +32
+    const uint32_t full0 = bar0, empty0 = bar0 + 16, done = bar0 + 32;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(gbase + (bar0 + 40 - base));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_BM;
+
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(256)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+
+    // weight chunk g: its map, K offset and bytes
+    auto issue = [&](int g) {
+        const int s = g & 1;
+        const CUtensorMap *m = g == 0 ? &w1 : (g < 5 ? &w2 : (g < 9 ? &w3 : &w4));
+        const int c = g == 0 ? 0 : (g - 1) & 3;
+        const uint32_t bytes = g < 9 ? PS_STAGE : 16 * 128;
+        mbar_expect_tx(full0 + 8 * s, bytes);
+        tma_load_2d(wst + s * PS_STAGE, m, 64 * c, 0, full0 + 8 * s);
+    };
+    int issued = 0, consumed = 0;  // thread 0's TMA bookkeeping
+    if (tid == 0) {
+        issue(0);
+        issue(1);
+        issued = 2;
+    }
+
+    // features of this thread's row, into activation chunk 0 (K = 16)
+    int lo = 0, hi = 0;
+    const int b = m0 + tid;
+    if (tid < TC_BM) {
+        float x[kF];
+        if (b < a.B) {
+            features(a.j, a.d, a.n, a.ms, a.n_rem[b], a.shift[static_cast<int64_t>(b) * a.d + a.j], x, lo, hi);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kF; ++k) x[k] = 0.0f;
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            uint4 w;
+            uint32_t *wv = reinterpret_cast<uint32_t *>(&w);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                __nv_bfloat162 v = __floats2bfloat162_rn(x[8 * p + 2 * q], x[8 * p + 2 * q + 1]);
+                wv[q] = *reinterpret_cast<uint32_t *>(&v);
+            }
+            *reinterpret_cast<uint4 *>(gbase + act_off(tid, 8 * p)) = w;
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    bool ok = true;   // thread 0: every wait so far succeeded
+    bool have = true; // every thread: every layer's accumulators arrived
+    for (int layer = 0; layer < 4; ++layer) {
+        const int bn = layer < 3 ? 256 : 16;
+        if (tid == 0) {
+            const int g0 = layer == 0 ? 0 : 1 + 4 * (layer - 1), nch = layer == 0 ? 1 : 4;
+            const uint32_t idesc = idesc_bf16(bn);
+            for (int c = 0; c < nch && ok; ++c) {
+                const int g = g0 + c, s = g & 1;
+                const uint32_t parity = static_cast<uint32_t>((g >> 1) & 1);
+                if (!mbar_wait(full0 + 8 * s, parity)) {
+                    record_error(11);
+                    ok = false;
+                    break;
+                }
+                consumed = g + 1;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const int nk = layer == 0 ? 1 : 4;  // K = 16 per instruction
+                for (int kk = 0; kk < nk; ++kk)
+                    umma_bf16(tmem, sdesc_sw128(act + c * PS_ACT_CHUNK + 32u * kk),
+                              sdesc_sw128(wst + s * PS_STAGE + 32u * kk), idesc, (c > 0 || kk > 0) ? 1 : 0);
+                umma_commit(empty0 + 8 * s);
+                if (g + 2 < PS_CHUNKS) {
+                    // the stage is refilled once these MMAs have read it
+                    if (!mbar_wait(empty0 + 8 * s, parity)) {
+                        record_error(12);
+                        ok = false;
+                        break;
+                    }
+                    issue(g + 2);
+                    issued = g + 3;
+                }
+            }
+            umma_commit(done);  // arrives when every MMA issued so far has completed
+        }
+        __syncwarp();
+        const bool arrived = __all_sync(0xffffffffu, mbar_wait(done, static_cast<uint32_t>(layer & 1)));
+        if (!arrived && lane == 0) record_error(13);
+        have = have && arrived;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int q = warp & 3;
+        const uint32_t taddr = tmem + (static_cast<uint32_t>(q * 32) << 16);
+        const int r = q * 32 + lane;
+        if (layer < 3) {
+            // bias + GELU, BF16, into the activation tile (row r, 128 columns)
+            if (have) {
+                const float *bias = a.bias[layer];
+                const int c0 = (warp >> 2) * 128;
+                for (int j0 = c0; j0 < c0 + 128; j0 += 32) {
+                    float v[32];
+                    tmem_ld32(taddr + static_cast<uint32_t>(j0), v);
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) {
+                        uint4 w;
+                        uint32_t *wv = reinterpret_cast<uint32_t *>(&w);
+#pragma unroll
+                        for (int h = 0; h < 4; ++h) {
+                            const int col = j0 + 8 * p + 2 * h;
+                            const float y0 = v[8 * p + 2 * h] + bias[col];
+                            const float y1 = v[8 * p + 2 * h + 1] + bias[col + 1];
+                            __nv_bfloat162 t = __floats2bfloat162_rn(gelu(y0), gelu(y1));
+                            wv[h] = *reinterpret_cast<uint32_t *>(&t);
+                        }
+                        const int k = (j0 & 63) + 8 * p;
+                        *reinterpret_cast<uint4 *>(gbase + (j0 >> 6) * PS_ACT_CHUNK + act_off(r, k)) = w;
+                    }
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        } else if (warp < 4 && have) {
+            // logits (8 of the 16 columns) + bias, then the draw of row r
+            float v[16];
+            tmem_ld16(taddr, v);
+            float z[kLD];
+#pragma unroll
+            for (int c = 0; c < kLD; ++c) z[c] = v[c] + a.bias[3][c];
+            if (b < a.B) {
+                const uint64_t seed = a.seed_dev ? *a.seed_dev : a.seed;
+                draw(a.j, b, a.d, z, lo, hi, seed, a.samples, a.n_rem, a.shift, a.C, a.ms, a.logq);
+            }
+        }
+    }
+    // copies still in flight after a failed wait: wait for them (bounded)
+    // before the shared memory goes away
+    if (tid == 0) {
+        for (int g = consumed; g < issued; ++g)
+            if (!mbar_wait(full0 + 8 * (g & 1), static_cast<uint32_t>((g >> 1) & 1))) record_error(14);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+}
+
 int fail(int code, const char *msg) {
     pqg::set_last_error(msg);
     return code;
@@ -481,6 +698,53 @@ int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t 
         static_cast<const __nv_bfloat16 *>(src), rows, cols, ld_src, static_cast<__nv_bfloat16 *>(dst), ld_dst);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_transpose_bf16");
+}
+
+int pqg_proposal_step_tc(int32_t j, int32_t B, int32_t d, int32_t n, const float *mode_stats, const void *w1t,
+                         const void *w2t, const void *w3t, const void *w4t, const float *b1, const float *b2,
+                         const float *b3, const float *b4, uint64_t seed, const uint64_t *seed_dev, int8_t *samples,
+                         int32_t *n_rem, float *shift, const float *C, float *logq, void *stream) {
+    if (B <= 0 || d <= 0 || n <= 0 || j < 0 || j >= d || !mode_stats || !w1t || !w2t || !w3t || !w4t || !b1 ||
+        !b2 || !b3 || !b4 || !samples || !n_rem || !shift || !C || !logq)
+        return fail(PQG_ERR_INVALID, "pqg_proposal_step_tc: invalid arguments");
+    for (const void *p : {w1t, w2t, w3t, w4t})
+        if (reinterpret_cast<uintptr_t>(p) % 16)
+            return fail(PQG_ERR_INVALID, "pqg_proposal_step_tc: weights need 16-byte alignment");
+    CUtensorMap m1, m2, m3, m4;
+    int st = make_map(&m1, w1t, 256, 16, 16, 256);
+    if (!st) st = make_map(&m2, w2t, 256, 256, 256, 256);
+    if (!st) st = make_map(&m3, w3t, 256, 256, 256, 256);
+    if (!st) st = make_map(&m4, w4t, 8, 256, 256, 16);
+    if (st) return st;
+    PsArgs g{};
+    g.j = j;
+    g.B = B;
+    g.d = d;
+    g.n = n;
+    g.ms = mode_stats;
+    g.bias[0] = b1;
+    g.bias[1] = b2;
+    g.bias[2] = b3;
+    g.bias[3] = b4;
+    g.seed_dev = seed_dev;
+    g.seed = seed;
+    g.samples = samples;
+    g.n_rem = n_rem;
+    g.shift = shift;
+    g.C = C;
+    g.logq = logq;
+    const size_t smem = 1024 + 4 * PS_ACT_CHUNK + 2 * PS_STAGE + 64;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [smem] {
+        attr_err = cudaFuncSetAttribute(proposal_step_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(smem));
+    });
+    if (attr_err != cudaSuccess) return fail_cuda(attr_err, "pqg_proposal_step_tc (shared memory attribute)");
+    proposal_step_tc<<<static_cast<unsigned>((B + TC_BM - 1) / TC_BM), PS_THREADS, smem,
+                       static_cast<cudaStream_t>(stream)>>>(m1, m2, m3, m4, g);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_proposal_step_tc");
 }
 
 int pqg_mlp_tc_status(int32_t *code) {

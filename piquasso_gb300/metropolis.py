@@ -46,7 +46,7 @@ def _i32(t):
 class ProposalSampler:
     """Draws B patterns and their log q on the device."""
 
-    def __init__(self, mlp, stats: ModeStats, B, baseline=False, device="cuda"):
+    def __init__(self, mlp, stats: ModeStats, B, baseline=False, device="cuda", fused=True):
         import torch
 
         self.torch = torch
@@ -73,6 +73,9 @@ class ProposalSampler:
         self.logq = torch.zeros(B, dtype=torch.float32, device=device)
         self.seed_dev = torch.zeros(1, dtype=torch.int64, device=device)
         self.graph = None
+        # one fused tensor-core kernel per mode (pqg_proposal_step_tc) unless
+        # asked for the separate feature / GEMM / sampling kernels
+        self.fused = bool(fused) and not baseline
         if baseline:
             # exact one-mode marginals; the tail mass spread over occupations 5..7
             lg = np.zeros((self.d, LD), dtype=np.float32)
@@ -112,6 +115,17 @@ class ProposalSampler:
         self.logq.zero_()
         B, d, n = self.B, self.d, self.n
         seed_ptr = ctypes.c_void_p(self.seed_dev.data_ptr())
+        if self.fused:
+            m = self.mlp
+            w = [ctypes.c_void_p(t.data_ptr()) for t in m.WbT]
+            for j in range(d):
+                st = L.pqg_proposal_step_tc(j, B, d, n, _fp(self.ms), w[0], w[1], w[2], w[3], _fp(m.b[0]),
+                                            _fp(m.b[1]), _fp(m.b[2]), _fp(m.b[3]), ctypes.c_uint64(0), seed_ptr,
+                                            _i8(self.samples), _i32(self.n_rem), _fp(self.shift), _fp(self.C),
+                                            _fp(self.logq), stream)
+                if st:
+                    raise RuntimeError(_lib.last_error())
+            return
         for j in range(d):
             st = L.pqg_proposal_features(j, B, d, n, _fp(self.ms), _i32(self.n_rem), _fp(self.shift),
                                          ctypes.c_void_p(self.X.data_ptr()), _i8(self.lo), _i8(self.hi), stream)
