@@ -356,6 +356,12 @@ void Planner::finish() {
         return off;
     };
     const int64_t d_elem = prec_ == Precision::C64 ? 8 : 16;  // one D element: float2, else double2 / float4
+    // items a block takes at once: the complex64 plain walk hands out groups
+    // of PQG_ITEM_GROUP consecutive items (one per warp of a block), so a
+    // block's warps walk one problem's prefix table together and share it in
+    // L1; its problems then come in whole groups of items
+    const int64_t group = (prec_ == Precision::C64 && form_ == Form::PLAIN) ? PQG_ITEM_GROUP : 1;
+    item_group = static_cast<int>(group);
 
     // Outputs stay in the caller's order; the work runs longest items first.
     // The device queue hands out items in problem order, so the problems are
@@ -441,14 +447,15 @@ void Planner::finish() {
         q.n_outer = no;
         q.Q = static_cast<int64_t>(std::llround(p.S / P));
         q.R = std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
-        q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / 32));
-        // whole warps: the outer positions spread evenly over the nearest
-        // count of items, so a problem's last item is not mostly idle lanes
-        // (an item is one warp; its lanes all run about R inner walks)
+        q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / (PQG_ITEM_LANES * group)));
+        // whole warps (whole groups): the outer positions spread evenly over
+        // the nearest count of item groups, so a problem's last item is not
+        // mostly idle lanes (an item is one warp; its lanes all run about R
+        // inner walks)
         {
-            const int64_t per_item = PQG_ITEM_LANES * q.R;
-            const int64_t n_it = std::max<int64_t>(1, (q.Q + per_item / 2) / per_item);
-            q.R = (q.Q + PQG_ITEM_LANES * n_it - 1) / (PQG_ITEM_LANES * n_it);
+            const int64_t per_group = PQG_ITEM_LANES * group * q.R;
+            const int64_t n_grp = std::max<int64_t>(1, (q.Q + per_group / 2) / per_group);
+            q.R = (q.Q + PQG_ITEM_LANES * group * n_grp - 1) / (PQG_ITEM_LANES * group * n_grp);
         }
         for (int o = 0; o < no; ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
         for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
@@ -505,6 +512,7 @@ void Planner::finish() {
 
         const int64_t lanes = (q.Q + q.R - 1) / q.R;
         q.n_items = (lanes + PQG_ITEM_LANES - 1) / PQG_ITEM_LANES;
+        q.n_items = (q.n_items + group - 1) / group * group;  // trailing items of a group may be empty
         total_items += q.n_items;
         total_parts += q.n_items * q.n_out;
         item_begin[ip + 1] = total_items;

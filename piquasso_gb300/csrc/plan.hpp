@@ -90,6 +90,7 @@ class Planner {
     int64_t matrix_off = 0;            // byte offset of the matrix in the arena
     int64_t mat_rows = 0, mat_cols = 0;
     int max_nc = 0;
+    int item_group = 1;                // items a walk block takes at once (total_items is a multiple)
     bool all_ones = true;              // every walk problem's columns have multiplicity 1
     double total_steps = 0.0;          // sum over problems of the Gray-code space
     double total_flops = 0.0;          // algorithmic flop count, see algorithmic_flops()

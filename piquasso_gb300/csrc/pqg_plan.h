@@ -27,6 +27,7 @@
 // chunks spread the double-double sums over every SM (the FP64 pipe of an SM
 // completes about two lanes per clock).
 #define PQG_CHUNK_ITEMS 64
+#define PQG_ITEM_GROUP 4  // items (warps) a block of the complex64 plain walk takes at once
 
 enum PqgProblemKind : int32_t {
     PQG_KIND_WALK = 0,      // Gray-code walk on the device

@@ -401,8 +401,24 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
     using d_t = typename Ar::d_t;
     using t_t = typename Ar::t_t;
     const int lane = threadIdx.x & 31;
+    // complex64: a block takes PQG_ITEM_GROUP consecutive items at once (one
+    // per warp; the plan makes every problem a whole number of groups), so its
+    // warps walk the same problem's prefix table together and share its lines
+    // in L1; the exit is uniform over the block (total_items is a multiple of
+    // the group)
+    constexpr bool grouped = Ar::kTwoSeeds;
+    static_assert(!grouped || PQG_ITEM_GROUP * 32 == PQG_WALK_THREADS, "one item per warp of a block");
+    __shared__ unsigned long long s_group;
     for (;;) {
-        const int64_t item = next_item(A.counter, lane);
+        int64_t item;
+        if constexpr (grouped) {
+            __syncthreads();  // every warp has read the previous group
+            if (threadIdx.x == 0) s_group = atomicAdd(A.counter, 1ULL);
+            __syncthreads();
+            item = static_cast<int64_t>(s_group) * PQG_ITEM_GROUP + (threadIdx.x >> 5);
+        } else {
+            item = next_item(A.counter, lane);
+        }
         if (item >= A.total_items) return;
         const int ip = find_problem(A.item_begin, A.n_probs, item);
         const PqgProblem *pr = A.probs + ip;
