@@ -537,7 +537,12 @@ def profile_case(name):
       laplace24  — 1024 complex64 Laplace permanents shaped like the exact
                    sampler's last photon step at n=24, d=48, 3 calls;
       df24       — one n=24 complex128 permanent (double-float walk), 4 calls;
-      df28       — the n=28 headline permanent (double-float walk), 3 calls."""
+      df28       — the n=28 headline permanent (double-float walk), 3 calls;
+      propose8192 — the fused tensor-core proposal step for 8192 chains at
+                   n=24, d=48 (48 launches per draw): one eager draw, then 3
+                   graph replays;
+      draw2048   — the exact sampler's fused step (Laplace permanents + pmf +
+                   draw) for 2048 shots after 16 photons at n=24, d=48, 3 calls."""
     import ctypes
 
     import __graft_entry__
@@ -587,6 +592,27 @@ def profile_case(name):
         cols = np.broadcast_to(inp, rows.shape)
         for _ in range(3):
             pge.permanent_laplace_batch(U.astype(np.complex64), rows, cols)
+    elif name == "propose8192":
+        U = workloads.haar_unitary(48, 3)
+        inp = np.array([1] * 24 + [0] * 24)
+        ps = metropolis.ProposalSampler(proposal.load_mlp(), proposal.ModeStats(U, inp), 8192)
+        for s_ in range(4):  # the first call runs eagerly and captures the graph
+            ps.propose(seed=s_)
+        torch.cuda.synchronize()
+    elif name == "draw2048":
+        from piquasso_gb300 import sampling
+
+        U = workloads.haar_unitary(48, 3).astype(np.complex64)
+        inp = np.array([1] * 24 + [0] * 24)
+        # 2048 shots with 16 photons placed: exact samples of the first 16 inputs
+        rows = sampling.generate_samples_batched(np.array([1] * 16 + [0] * 32), 2048, U, 5)
+        rng = np.random.default_rng(2)
+        cols = np.zeros_like(rows)
+        for s_ in range(len(cols)):
+            cols[s_, rng.permutation(24)[:17]] = 1
+        u = rng.random(len(rows))
+        for _ in range(3):
+            pge.sampler_step_batch(U, rows, cols, u)
     elif name == "df28":
         A = haar_unitary(56, 0)[:28, :28].copy()
         for _ in range(3):

@@ -204,6 +204,11 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             }
         }
         const bool split = PL + PH <= PREP_SUB_MAX;
+        const int n_tiles = (P + blockDim.x - 1) / blockDim.x;
+        if (slice >= n_tiles) {
+            __syncthreads();  // no tile for this slice: the shared arrays are reused
+            continue;
+        }
         if (split) {
             for (int e = threadIdx.x; e < (PL + PH) * nc; e += blockDim.x) {
                 const int u = e / nc, j = e - u * nc;
@@ -228,7 +233,6 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                 inrow[kk][j] = ad(no + kk, j);
             }
         }
-        const int n_tiles = (P + blockDim.x - 1) / blockDim.x;
         for (int tile = slice; tile < n_tiles; tile += A.slices) {
             const int t0 = tile * blockDim.x;
             const int tc = min(static_cast<int>(blockDim.x), P - t0);
