@@ -167,8 +167,7 @@ int pqg_plan_destroy(pqg_plan_t *plan);
 
 /* Work-split knobs of the planner (process-wide; 0 restores a default):
  * items_per_smsp — warps of work per SM sub-partition the split aims for
- * (default 32 for the complex64 plain walk, whose short batched problems then
- * spread over several warps that share a prefix table in L1, else 16); p_max — longest inner walk, i.e. step-table length (default
+ * (default 16); p_max — longest inner walk, i.e. step-table length (default
  * 2048, at most 32768); seed_steps — Gray-code steps per lane that amortise
  * one seed (default depends on the arithmetic).  The autotuner sets these. */
 int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps);

@@ -235,7 +235,7 @@ int walk_launch_config(Context &C, const Planner &pl, const KernelInfo **k, int6
     const KernelInfo &kk = kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, &which);
     int &occ = C.occ_cache[which][pl.max_nc];
     if (occ < 0) {
-        if (kk.smem_bytes > 48 * 1024)
+        if (kk.smem_bytes > 0)
             PQG_CUDA(cudaFuncSetAttribute(kk.fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(kk.smem_bytes)));
         int b = 0;

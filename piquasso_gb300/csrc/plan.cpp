@@ -299,8 +299,8 @@ void Planner::finish() {
     // Laplace form a neutral column's own output is never read, and the shared
     // output of the zero-multiplicity columns moves behind the padded ones.
     bool any_walk = false;
+    int ncmax = 1;
     {
-        int ncmax = 1;
         for (auto &p : pending)
             if (p.kind == PQG_KIND_WALK) {
                 ncmax = std::max(ncmax, p.nc);
@@ -331,11 +331,7 @@ void Planner::finish() {
     for (auto &p : pending)
         if (p.kind == PQG_KIND_WALK) S_tot += p.S;
     const double resident_warps = 4.0 * cfg_.num_sms * 3.0;
-    // (complex64 plain walks aim for twice as many items: a batch of short
-    // problems then gives each problem several consecutive items, which
-    // neighbouring warps take together and whose prefix table they share in L1)
-    const int64_t items = cfg_.items_per_smsp > 0 ? cfg_.items_per_smsp
-                                                  : (prec_ == Precision::C64 && form_ == Form::PLAIN ? 32 : 16);
+    const int64_t items = cfg_.items_per_smsp > 0 ? cfg_.items_per_smsp : 16;
     const double balance = S_tot / (32.0 * 4.0 * cfg_.num_sms * static_cast<double>(items));
     const double seed_floor = std::min<double>(static_cast<double>(cfg_.seed_steps > 0 ? cfg_.seed_steps
                                                                                     : min_steps_per_seed(prec_)),
@@ -346,8 +342,13 @@ void Planner::finish() {
     // bound by its arithmetic pipe and tolerates longer tables
     int64_t p_cap = prec_ == Precision::C128 ? 512 : 256;
     if (cfg_.p_max_user) p_cap = cfg_.p_max;
-    const int64_t p_max = laplace ? std::min<int64_t>(std::min<int64_t>(cfg_.p_max, p_cap), 512)
-                                  : std::min<int64_t>(cfg_.p_max, p_cap);
+    int64_t p_max = laplace ? std::min<int64_t>(std::min<int64_t>(cfg_.p_max, p_cap), 512)
+                            : std::min<int64_t>(cfg_.p_max, p_cap);
+    // the complex64 plain walk of 17..24 columns stages each problem's table
+    // in shared memory, which holds PQG_SMEM_TABLE_P codes (a hard limit, over
+    // any tuning)
+    if (prec_ == Precision::C64 && !laplace && ncmax >= PQG_SMEM_TABLE_NC_MIN && ncmax <= PQG_SMEM_TABLE_NC_MAX)
+        p_max = std::min<int64_t>(p_max, PQG_SMEM_TABLE_P);
     // per-problem device data (built by the prep kernel), by offset from the
     // start of that region; the region follows the uploaded arena
     auto pdata = [&](int64_t bytes) {

@@ -219,7 +219,7 @@ struct LaplaceC64Cfg {
 // 24-column step with it did not fit the instruction cache (ncu: 9.7
 // no-instruction stalls per issue, 11 % issue).
 template <int NC, bool ONES>
-__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_laplace_c64(WalkArgs A) {
+__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) walk_laplace_c64(WalkArgs A) {
     using Cfg = LaplaceC64Cfg<NC>;
     extern __shared__ double2 lap_smem64[];
     const int lane = threadIdx.x & 31;

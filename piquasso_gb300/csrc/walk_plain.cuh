@@ -384,19 +384,77 @@ __device__ __forceinline__ void row_product_packed(const float2 (&sr)[NC], const
     pi = xi;
 }
 
+// The same product reading the table row from shared memory column by
+// column: a compiler barrier every G columns keeps at most G entries in
+// flight, so the row never occupies 4 x NC registers (the three-block
+// register budget of the shared-table kernels).
+template <int NC, int G>
+__device__ __forceinline__ void row_product_packed_smem(const float2 (&sr)[NC], const float2 (&si)[NC],
+                                                        const float4 *row, const uint8_t *__restrict__ cm, bool ones,
+                                                        float2 &pr, float2 &pi) {
+    float2 xr, xi, yr, yi;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        if (j % G == 0) asm volatile("" ::: "memory");
+        const float4 dj = row[j];
+        const float2 cr = __fadd2_rn(sr[j], make_float2(dj.x, dj.y));
+        const float2 ci = __fadd2_rn(si[j], make_float2(dj.z, dj.w));
+        if (j == 0) {
+            xr = cr;
+            xi = ci;
+            if (!ones)
+                for (int r = 1; r < cm[0]; ++r) cmul2(xr, xi, cr, ci);
+        } else if (j == 1) {
+            yr = cr;
+            yi = ci;
+            if (!ones)
+                for (int r = 1; r < cm[1]; ++r) cmul2(yr, yi, cr, ci);
+        } else {
+            const int reps = ones ? 1 : cm[j];
+            for (int r = 0; r < reps; ++r) {
+                if (j & 1)
+                    cmul2(yr, yi, cr, ci);
+                else
+                    cmul2(xr, xi, cr, ci);
+            }
+        }
+    }
+    cmul2(xr, xi, yr, yi);
+    pr = xr;
+    pi = xi;
+}
+
 // Blocks per SM the register allocation must allow: the column sums of the
 // wider kernels need up to 255 registers per thread, and a spill inside the
 // step loop costs more than the occupancy it buys.
 template <int NC>
-constexpr int walk_min_blocks() {
+constexpr int walk_min_blocks_cols() {
     return NC <= 8 ? 4 : (NC <= 16 ? 3 : 2);
+}
+
+// The two-seed complex64 walk of 17..24 columns reads its prefix table from
+// shared memory (at most SMEM_TAB_P codes; the planner caps P there) and runs
+// three blocks per SM.
+constexpr int SMEM_TAB_NC_MIN = PQG_SMEM_TABLE_NC_MIN, SMEM_TAB_NC_MAX = PQG_SMEM_TABLE_NC_MAX,
+              SMEM_TAB_P = PQG_SMEM_TABLE_P, SMEM_TAB_G = 8;
+template <class Ar, int NC>
+__host__ __device__ constexpr bool plain_smem_table() {
+    return Ar::kTwoSeeds && NC >= SMEM_TAB_NC_MIN && NC <= SMEM_TAB_NC_MAX;
+}
+template <class Ar, int NC>
+struct PlainCfg {
+    static constexpr size_t smem_bytes = plain_smem_table<Ar, NC>() ? SMEM_TAB_P * NC * sizeof(float4) : 0;
+};
+template <class Ar, int NC>
+constexpr int walk_min_blocks() {
+    return (plain_smem_table<Ar, NC>() && NC <= 20) ? 3 : walk_min_blocks_cols<NC>();
 }
 
 // ONES: every column of every problem has multiplicity 1 (the usual case:
 // unit input photons), so the repeated-factor code is compiled out — a
 // smaller loop body for the instruction cache and the register allocator.
 template <class Ar, int NC, bool ONES>
-__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_plain(WalkArgs A) {
+__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) walk_plain(WalkArgs A) {
     using cs_t = typename Ar::cs_t;
     using d_t = typename Ar::d_t;
     using t_t = typename Ar::t_t;
@@ -409,6 +467,12 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
     constexpr bool grouped = Ar::kTwoSeeds;
     static_assert(!grouped || PQG_ITEM_GROUP * 32 == PQG_WALK_THREADS, "one item per warp of a block");
     __shared__ unsigned long long s_group;
+    // 17..24 columns: the group's prefix table in shared memory (dynamic,
+    // SMEM_TAB_P x NC entries), read by all four warps; without the table row
+    // in registers the kernel fits three blocks per SM
+    constexpr bool smem_tab = plain_smem_table<Ar, NC>();
+    extern __shared__ float4 s_tab[];
+    int staged = -1;
     for (;;) {
         int64_t item;
         if constexpr (grouped) {
@@ -422,6 +486,17 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
         if (item >= A.total_items) return;
         const int ip = find_problem(A.item_begin, A.n_probs, item);
         const PqgProblem *pr = A.probs + ip;
+        if constexpr (smem_tab) {
+            // the block's four items belong to one problem: stage its prefix
+            // table once (every warp finished its previous item at the loop top)
+            if (ip != staged) {
+                const float4 *src = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin;
+                const int n = (pr->P < SMEM_TAB_P ? pr->P : SMEM_TAB_P) * NC;
+                for (int e = threadIdx.x; e < n; e += PQG_WALK_THREADS) s_tab[e] = src[e];
+                staged = ip;
+                __syncthreads();
+            }
+        }
         const int64_t local = item - pr->item_begin;
         const int64_t R = pr->R;
         const int64_t Q = pr->Q;
@@ -449,37 +524,52 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                 // positions in pairs (seg, seg+1) in the two lanes of packed
                 // FP32 instructions: lane .x the current seed, lane .y the
                 // seed one outer step on; both walk the inner codes forward
-                // (the column sums are seed + Delta(t), so the walk order is free)
+                // (the column sums are seed + Delta(t), so the walk order is free).
+                // The current seed lives in the pairs' .x lanes from here on, so
+                // `seed` is not live across the inner walks (a remainder
+                // position takes its seed back from the .x lanes)
+                float2 pr2[NC], pi2[NC];
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    pr2[j].x = seed[j].r;
+                    pi2[j].x = seed[j].i;
+                }
                 for (; seg + 1 < my_R; seg += 2) {
-                    float2 pr2[NC], pi2[NC];
                     bool up = false;
                     int k = outer_next(pr, st, &up);
                     const d_t *db = D + (2 * k + (up ? 0 : 1)) * NC;
 #pragma unroll
                     for (int j = 0; j < NC; ++j) {
                         const d_t dj = db[j];
-                        pr2[j] = make_float2(seed[j].r, __fadd_rn(seed[j].r, dj.x));
-                        pi2[j] = make_float2(seed[j].i, __fadd_rn(seed[j].i, dj.y));
+                        pr2[j].y = __fadd_rn(pr2[j].x, dj.x);
+                        pi2[j].y = __fadd_rn(pi2[j].x, dj.y);
                     }
                     const double wb = outer_weight(pr, st);
                     float2 accr = make_float2(0.0f, 0.0f), accrc = accr, acci = accr, accic = accr;
-                    constexpr bool refill = NC <= REFILL_MAX_NC;
+                    constexpr bool refill = !smem_tab && NC <= REFILL_MAX_NC;
                     float4 dq[NC];
                     if constexpr (refill) {
 #pragma unroll
                         for (int j = 0; j < NC; ++j) dq[j] = delta[j];
                     }
-                    for (int t = 0; t < P; ++t) {
+                    // (the staged table holds at most SMEM_TAB_P codes: the plan
+                    // guarantees P fits; the bound keeps every read inside it)
+                    const int Pw = smem_tab ? (P < SMEM_TAB_P ? P : SMEM_TAB_P) : P;
+                    for (int t = 0; t < Pw; ++t) {
                         float2 xr, xi;
-                        if constexpr (!refill) {
-                            const float4 *row = delta + static_cast<int64_t>(t) * NC;
+                        if constexpr (smem_tab) {
+                            row_product_packed_smem<NC, SMEM_TAB_G>(pr2, pi2, s_tab + t * NC, cm, ones, xr, xi);
+                        } else {
+                            if constexpr (!refill) {
+                                const float4 *row = delta + static_cast<int64_t>(t) * NC;
 #pragma unroll
-                            for (int j = 0; j < NC; ++j) dq[j] = row[j];
+                                for (int j = 0; j < NC; ++j) dq[j] = row[j];
+                            }
+                            // the last code reloads its own row (in bounds, unused)
+                            const int tn = t + 1 < P ? t + 1 : t;
+                            row_product_packed<NC, refill>(pr2, pi2, dq, delta + static_cast<int64_t>(tn) * NC, cm,
+                                                           ones, xr, xi);
                         }
-                        // the last code reloads its own row (in bounds, unused)
-                        const int tn = t + 1 < P ? t + 1 : t;
-                        row_product_packed<NC, refill>(pr2, pi2, dq, delta + static_cast<int64_t>(tn) * NC, cm, ones, xr,
-                                                       xi);
                         const float wf = tab[t].wf;
                         const float2 w2 = make_float2(wf, wf);
                         two_sum_acc2(accr, accrc, __fmul2_rn(w2, xr));
@@ -491,13 +581,15 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<NC>()) walk_
                         k = outer_next(pr, st, &up);
                         const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
 #pragma unroll
-                        for (int j = 0; j < NC; ++j) {
-                            seed[j] = cs_t{pr2[j].y, pi2[j].y};
-                            Ar::update(seed[j], d[j]);
+                        for (int j = 0; j < NC; ++j) {  // Ar::update of the .y seed
+                            pr2[j].x = __fadd_rn(pr2[j].y, d[j].x);
+                            pi2[j].x = __fadd_rn(pi2[j].y, d[j].y);
                         }
                         wout = outer_weight(pr, st);
                     }
                 }
+#pragma unroll
+                for (int j = 0; j < NC; ++j) seed[j] = cs_t{pr2[j].x, pi2[j].x};
             }
             for (; seg < my_R; ++seg) {
                 typename Ar::acc_t acc = Ar::zero();
