@@ -433,21 +433,29 @@ constexpr int walk_min_blocks_cols() {
 }
 
 // The two-seed complex64 walk of 17..24 columns reads its prefix table from
-// shared memory (at most SMEM_TAB_P codes; the planner caps P there) and runs
-// three blocks per SM.
+// shared memory, staged once per group of items: at most smem_tab_codes<NC>()
+// codes (the planner caps P there).  The table row then needs no registers.
+// (Wider walks would need half-length tables to fit two blocks on an SM; at
+// 28 columns that measured slower than the register-pipelined rows.)
 constexpr int SMEM_TAB_NC_MIN = PQG_SMEM_TABLE_NC_MIN, SMEM_TAB_NC_MAX = PQG_SMEM_TABLE_NC_MAX,
-              SMEM_TAB_P = PQG_SMEM_TABLE_P, SMEM_TAB_G = 8;
+              SMEM_TAB_G = 8;
+template <int NC>
+__host__ __device__ constexpr int smem_tab_codes() {
+    return NC > PQG_SMEM_TABLE_NC_WIDE ? PQG_SMEM_TABLE_P / 2 : PQG_SMEM_TABLE_P;
+}
 template <class Ar, int NC>
 __host__ __device__ constexpr bool plain_smem_table() {
     return Ar::kTwoSeeds && NC >= SMEM_TAB_NC_MIN && NC <= SMEM_TAB_NC_MAX;
 }
 template <class Ar, int NC>
 struct PlainCfg {
-    static constexpr size_t smem_bytes = plain_smem_table<Ar, NC>() ? SMEM_TAB_P * NC * sizeof(float4) : 0;
+    static constexpr size_t smem_bytes = plain_smem_table<Ar, NC>() ? smem_tab_codes<NC>() * NC * sizeof(float4) : 0;
 };
 template <class Ar, int NC>
 constexpr int walk_min_blocks() {
-    return (plain_smem_table<Ar, NC>() && NC <= 20) ? 3 : walk_min_blocks_cols<NC>();
+    // three blocks where their tables fit an SM's 228 KB and 168 registers
+    // hold the kernel without spills (measured: up to 18 columns)
+    return (plain_smem_table<Ar, NC>() && NC <= 18) ? 3 : walk_min_blocks_cols<NC>();
 }
 
 // ONES: every column of every problem has multiplicity 1 (the usual case:
@@ -468,7 +476,7 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
     static_assert(!grouped || PQG_ITEM_GROUP * 32 == PQG_WALK_THREADS, "one item per warp of a block");
     __shared__ unsigned long long s_group;
     // 17..24 columns: the group's prefix table in shared memory (dynamic,
-    // SMEM_TAB_P x NC entries), read by all four warps; without the table row
+    // smem_tab_codes<NC>() x NC entries), read by all four warps; without the table row
     // in registers the kernel fits three blocks per SM
     constexpr bool smem_tab = plain_smem_table<Ar, NC>();
     extern __shared__ float4 s_tab[];
@@ -491,7 +499,7 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
             // table once (every warp finished its previous item at the loop top)
             if (ip != staged) {
                 const float4 *src = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin;
-                const int n = (pr->P < SMEM_TAB_P ? pr->P : SMEM_TAB_P) * NC;
+                const int n = (pr->P < smem_tab_codes<NC>() ? pr->P : smem_tab_codes<NC>()) * NC;
                 for (int e = threadIdx.x; e < n; e += PQG_WALK_THREADS) s_tab[e] = src[e];
                 staged = ip;
                 __syncthreads();
@@ -552,9 +560,9 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
 #pragma unroll
                         for (int j = 0; j < NC; ++j) dq[j] = delta[j];
                     }
-                    // (the staged table holds at most SMEM_TAB_P codes: the plan
+                    // (the staged table holds at most smem_tab_codes<NC>() codes: the plan
                     // guarantees P fits; the bound keeps every read inside it)
-                    const int Pw = smem_tab ? (P < SMEM_TAB_P ? P : SMEM_TAB_P) : P;
+                    const int Pw = smem_tab ? (P < smem_tab_codes<NC>() ? P : smem_tab_codes<NC>()) : P;
                     for (int t = 0; t < Pw; ++t) {
                         float2 xr, xi;
                         if constexpr (smem_tab) {
