@@ -205,3 +205,43 @@ def test_cpu_baseline_port_agrees_with_engine(engine):
             assert abs(got - want) <= 1e-10 * abs(want)
         lap = oracle.port_laplace(A, r2, o)
         assert np.allclose(lap, engine.permanent_laplace(A, r2, o), rtol=1e-10, atol=0)
+
+
+def test_complex64_shared_table_batches_match_oracle(engine):
+    """17..24 distinct columns: the complex64 walk stages each problem's
+    prefix table in shared memory, restaged when a block moves on to another
+    problem of the batch; unit columns (all-ones kernel) and one doubled input
+    column (repeated-column kernel), rows with collisions."""
+    rng = np.random.default_rng(41)
+    d = 34
+    U = haar_unitary(d, 41).astype(np.complex64)
+    for cols in (np.array([1] * 17 + [0] * 17), np.array([1] * 17 + [2] + [0] * 16)):
+        n = int(cols.sum())
+        R = np.stack([np.bincount(rng.integers(0, d, n), minlength=d) for _ in range(24)])
+        got = engine.permanent_batch(U, R, cols)
+        for b in range(len(R)):
+            dd = oracle.permanent(U.astype(np.complex128), R[b], cols)
+            assert abs(got[b] - dd) <= tol64(U, R[b], cols, dd), b
+
+
+def test_complex64_target_batch_matches_complex128(engine):
+    """The Metropolis target shape at full size (n=24 photons in 48 modes, 512
+    patterns with occupations <= 4, one batched launch): complex64 against
+    the double-float complex128 path (relative error ~1e-12), within the
+    complex64 bound max(1e-5 |perm|, 2^-22 perm(|A|))."""
+    rng = np.random.default_rng(7)
+    d, n = 48, 24
+    U = haar_unitary(d, 3)
+    inp = np.array([1] * n + [0] * (d - n))
+    R = []
+    while len(R) < 512:
+        r = np.bincount(rng.integers(0, d, n), minlength=d)
+        if r.max() <= 4:
+            R.append(r)
+    R = np.stack(R)
+    got = engine.permanent_batch(U.astype(np.complex64), R, inp).astype(np.complex128)
+    ref = engine.permanent_batch(U, R, inp)
+    pabs = engine.permanent_batch(np.abs(U).astype(np.complex128), R, inp).real
+    err = np.abs(got - ref)
+    bound = np.maximum(1e-5 * np.abs(ref), 2.0 ** -22 * pabs)
+    assert np.all(err <= bound), (np.max(err / bound), int(np.argmax(err / bound)))
