@@ -92,7 +92,7 @@ struct Context {
     HostBuf h_plan, h_out;
     PlanConfig cfg;
     int blocks_per_sm = 0;  // 0: as many as fit (occupancy)
-    std::vector<int> occ_cache[9];  // blocks per SM, per kernel table, per column count
+    std::vector<int> occ_cache[10];  // blocks per SM, per kernel table, per column count
 
     int init() {
         if (ready) return PQG_OK;
@@ -141,6 +141,10 @@ const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_on
         }
         *which = 3;
         return kernel_for(k_laplace_c64_0, k_laplace_c64_1, nc);
+    }
+    if (prec == Precision::C128DF) {  // the plan falls back to FP64 unless every column has multiplicity 1
+        *which = 9;
+        return kernel_for(k_laplace_dfo_0, k_laplace_dfo_1, nc);
     }
     *which = 2;
     return kernel_for(k_laplace_c128_0, k_laplace_c128_1, nc);
@@ -437,6 +441,16 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     return run_plan<T>(C, pl, out, out_lo);
 }
 
+// The double-float Laplace walk serves all-ones columns in the double-float
+// domain, up to 25 columns (wider instantiations spill); any other complex128
+// Laplace plan is redone for the FP64 walk.
+void laplace_precision_fallback(Planner &pl) {
+    if (pl.precision() == Precision::C128DF && (!pl.df_ok || !pl.all_ones || pl.max_nc > 25)) {
+        pl.set_precision(Precision::C128);
+        pl.finish();
+    }
+}
+
 // Plans `batch` Laplace problems over one matrix (outside the context lock;
 // the lock is taken only to read the device's configuration).
 int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int64_t nc, const int32_t *rows,
@@ -458,6 +472,7 @@ int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int6
     cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
     pl.set_config(cfg);
     pl.finish();
+    laplace_precision_fallback(pl);
     return PQG_OK;
 }
 
@@ -591,6 +606,7 @@ int grad_batch(const double *mats, int64_t nr, int64_t nc, const int32_t *rows, 
     cfg.num_sms = C.cfg.num_sms;
     pl.set_config(cfg);
     pl.finish();
+    laplace_precision_fallback(pl);
     std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
     st = run_plan<T>(C, pl, res.data(), nullptr);
     if (st) return st;
@@ -762,7 +778,7 @@ int pqg_permanent_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols,
 
 int pqg_permanent_laplace_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                                const int32_t *cols, double *out, int64_t *n_out) {
-    return laplace_one<double>(matrix, n_rows, n_cols, rows, cols, Precision::C128, out, n_out);
+    return laplace_one<double>(matrix, n_rows, n_cols, rows, cols, c128_precision(PQG_MODE_AUTO), out, n_out);
 }
 
 int pqg_permanent_laplace_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
@@ -774,7 +790,8 @@ int pqg_permanent_laplace_c64(const float *matrix, int64_t n_rows, int64_t n_col
 
 int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                                      const int32_t *cols, int64_t batch, double *out, int64_t *n_out) {
-    return laplace_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, Precision::C128, out, n_out);
+    return laplace_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(PQG_MODE_AUTO), out,
+                                 n_out);
 }
 
 int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
@@ -786,7 +803,8 @@ int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t
 
 int pqg_sampler_step_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                           const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) {
-    return sampler_step<double>(matrix, n_rows, n_cols, rows, cols, batch, Precision::C128, uniforms, modes);
+    return sampler_step<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(PQG_MODE_AUTO), uniforms,
+                                modes);
 }
 
 int pqg_sampler_step_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
@@ -798,7 +816,7 @@ int pqg_sampler_step_c64(const float *matrix, int64_t n_rows, int64_t n_cols, co
 
 int pqg_permanent_grad_c128(const double *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                             const int32_t *cols, int64_t batch, double *out) {
-    return grad_batch<double>(matrices, n_rows, n_cols, rows, cols, batch, Precision::C128, out);
+    return grad_batch<double>(matrices, n_rows, n_cols, rows, cols, batch, c128_precision(PQG_MODE_AUTO), out);
 }
 
 int pqg_permanent_grad_c64(const float *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
@@ -867,8 +885,7 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
     const Form fm = form == 1 ? Form::LAPLACE : Form::PLAIN;
-    // the Laplace walk has FP64 and FP32 kernels only
-    const Precision prec = dtype == 1 ? Precision::C64 : (fm == Form::LAPLACE ? Precision::C128 : c128_precision(mode));
+    const Precision prec = dtype == 1 ? Precision::C64 : c128_precision(mode);
     PlanHandle *h = new PlanHandle();
     h->pl = Planner(prec, fm, C.cfg);
     h->single = dtype == 1;
@@ -889,7 +906,9 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     }
     h->pl.set_config(C.cfg);
     h->pl.finish();
-    if (prec == Precision::C128DF && !h->pl.df_ok) {
+    if (fm == Form::LAPLACE) {
+        laplace_precision_fallback(h->pl);
+    } else if (prec == Precision::C128DF && !h->pl.df_ok) {
         h->pl.set_precision(Precision::C128);
         h->pl.finish();
     }

@@ -404,6 +404,7 @@ void Planner::finish() {
             continue;
         }
         q.nc = p.nc;
+        q.laplace = laplace ? 1 : 0;
         max_nc = std::max(max_nc, p.nc);
         q.scale_exp = p.scale_exp;
         int cm_max = 1;
@@ -413,6 +414,14 @@ void Planner::finish() {
         }
         q.cm_max = cm_max;
         all_ones = all_ones && cm_max == 1;
+        if (df && laplace) {
+            // the double-float Laplace walk folds the whole step weight (inner
+            // times outer) into one FP32 value: its largest, the product over
+            // every digit of C(m, m/2), must be exact in FP32
+            double wmax = 1.0;
+            for (int i = 0; i < p.nd; ++i) wmax *= binom_d(p.m[i], p.m[i] / 2);
+            if (wmax > 16777216.0) df_ok = false;
+        }
 
         // this problem's steps per lane: the plan's, but never so many that
         // the problem fills less than one warp

@@ -77,7 +77,8 @@ struct PqgProblem {
     uint8_t cm[PQG_MAX_COLS];         // column multiplicities
     uint8_t outer_m[PQG_MAX_OUTER];   // outer digit multiplicities (radix m + 1)
     uint8_t inner_m[PQG_MAX_INNER];   // inner digit multiplicities
-    uint8_t pad1[4];
+    int32_t laplace;                  // Laplace form: output k < nc lacks one factor of column k
+    int16_t col_e[PQG_MAX_COLS];      // column scale exponents e_j (device-written; 0 unless double-float)
 };
 
 // Inner code t: its signed binomial weight (-1)^sum(g) prod C(m, g), in FP64

@@ -8,7 +8,8 @@
 //     the modulus to within one power of two, and cheap), so no double-float
 //     column sum exceeds 1 in magnitude
 //     (powers of two are exact; sum_j e_j cm_j goes to col_shift and is
-//     multiplied back in the final scaling);
+//     multiplied back in the final scaling, and each e_j to col_e, which a
+//     Laplace output lacking one factor of column j takes off again);
 //   * the seeds, the column sums with every digit at 0: a0 + sum_i m_i a_i,
 //     TwoSum-compensated in FP64;
 //   * the outer digits' rows a_o, and the one-digit update rows -2 a_o / +2 a_o;
@@ -120,6 +121,7 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             }
             cscale[j] = s;
             eshift[j] = e * pr->cm[j];
+            if (slice == 0) pr->col_e[j] = static_cast<int16_t>(e);
         }
         __syncthreads();
 

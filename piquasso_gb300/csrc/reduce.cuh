@@ -126,7 +126,9 @@ __global__ void finish_problems(const PqgProblem *__restrict__ probs, int n_prob
         if (mine) {
             // scaling by a power of two is exact in both words; ldexp avoids an
             // intermediate 2^-scale_exp that would itself overflow
-            const int e = pr->col_shift - pr->scale_exp;
+            // (a Laplace output of kept column o lacks one factor of that
+            // column, so one scale exponent e_o less)
+            const int e = pr->col_shift - pr->scale_exp - (pr->laplace && o < pr->nc ? pr->col_e[o] : 0);
             const double rh = ldexp(r.hi, e), rl = ldexp(r.lo, e), ih = ldexp(i.hi, e), il = ldexp(i.lo, e);
             if constexpr (sizeof(T) == 8) {
                 out[2 * (oi + o)] = rh;

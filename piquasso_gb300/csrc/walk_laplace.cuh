@@ -392,4 +392,155 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
     }
 }
 
+template <int NC>
+struct LaplaceDfCfg {
+    static constexpr size_t smem_bytes = size_t(2 * NC + 1) * PQG_WALK_THREADS * sizeof(float4);
+};
+
+// Complex128 Laplace walk in double-float arithmetic on the FP32 pipes (the
+// default for complex128 when every column has multiplicity 1 -- the
+// sampler's case -- and the plan is in the double-float domain): double-float
+// seeds and column sums seed + Delta(t), prefix and suffix products with
+// unnormalised double-float pairs (df_cmul_lazy), and the step's whole weight
+// w(t) * w_outer folded into the suffix's start -- an exact FP32 integer, as
+// the plan checks (max inner weight x max outer weight <= 2^24), so that one
+// set of per-output double-float sums (renormalising adds) spans all of a
+// lane's positions.  Those sums and the prefix products live in shared memory
+// (registers hold the seeds); lanes are combined in double-double.  About
+// 2^-48 per operation, against 2^-53 for the FP64 walk, on pipes 61x faster.
+template <int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs A) {
+    extern __shared__ float4 lap_smem_df[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<float4, NC + 1, true> acc;  // per-output sums {re_hi, re_lo, im_hi, im_lo}
+    acc.init(lap_smem_df, threadIdx.x);
+    LaneArray<float4, NC, true> pre;  // prefix products, the same layout
+    pre.init(lap_smem_df + (NC + 1) * PQG_WALK_THREADS, threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        const bool active = r0 < pr->Q;
+        if (active) {
+            dfl sr0[NC], si0[NC];  // double-float seed of the current outer position
+            OuterState st;
+            outer_decode(pr, r0, st);
+            {
+                ArDF::cs_t s[NC];
+                seed_lane<ArDF, NC>(pr, A.arena, st, s);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
+                }
+            }
+            double wout = outer_weight(pr, st);
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const float4 *D = reinterpret_cast<const float4 *>(A.arena + pr->off_D);
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const float4 *delta = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin;
+            const int P = pr->P;
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) acc.set(l, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+            auto add_to = [&](int l, dfl tr, dfl ti) {
+                const float4 a = acc.get(l);
+                const dfl r = df_add(dfl{a.x, a.y}, tr), i = df_add(dfl{a.z, a.w}, ti);
+                acc.set(l, make_float4(r.hi, r.lo, i.hi, i.lo));
+            };
+
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+                for (int t = 0; t < P; ++t) {
+                    // the whole weight, an exact FP32 integer (checked by the plan)
+                    const float w = static_cast<float>(__ldg(&tab[t].wd) * wout);
+                    const float4 *d = delta + static_cast<int64_t>(t) * NC;
+                    auto col = [&](int j, dfl &cr, dfl &ci) {
+                        const float4 v = __ldg(d + j);
+                        cr = df_add_lazy(sr0[j], dfl{v.x, v.y});
+                        ci = df_add_lazy(si0[j], dfl{v.z, v.w});
+                    };
+                    // prefix products: pre_l = prod_{k<l} c_k
+                    dfl xr{1.0f, 0.0f}, xi{0.0f, 0.0f};
+#pragma unroll
+                    for (int j = 0; j + 1 < NC; ++j) {
+                        dfl cr, ci;
+                        col(j, cr, ci);
+                        if (j == 0) {
+                            xr = cr;
+                            xi = ci;
+                        } else {
+                            df_cmul_lazy(xr, xi, cr, ci);
+                        }
+                        pre.set(j + 1, make_float4(xr.hi, xr.lo, xi.hi, xi.lo));
+                    }
+                    // suffix pass: out_l += w * pre_l * prod_{k>l} c_k
+                    dfl sr{w, 0.0f}, si{0.0f, 0.0f};
+#pragma unroll
+                    for (int l = NC - 1; l >= 0; --l) {
+                        dfl cr, ci;
+                        col(l, cr, ci);
+                        dfl tr, ti;
+                        if (l == NC - 1) {
+                            // (pre_0 = 1 is never stored: one column reads the constant)
+                            const float4 p = l == 0 ? make_float4(1.0f, 0.0f, 0.0f, 0.0f) : pre.get(l);
+                            tr = df_scale(dfl{p.x, p.y}, w);
+                            ti = df_scale(dfl{p.z, p.w}, w);
+                        } else if (l == 0) {
+                            tr = sr;
+                            ti = si;
+                        } else {
+                            const float4 p = pre.get(l);
+                            tr = dfl{p.x, p.y};
+                            ti = dfl{p.z, p.w};
+                            df_cmul_lazy(tr, ti, sr, si);
+                        }
+                        add_to(l, tr, ti);
+                        if (l > 0 || full) {
+                            if (l == NC - 1) {
+                                sr = df_scale(cr, w);
+                                si = df_scale(ci, w);
+                            } else {
+                                df_cmul_lazy(sr, si, cr, ci);
+                            }
+                        }
+                    }
+                    if (full) add_to(NC, sr, si);
+                }
+                if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                    bool up = false;
+                    const int k = outer_next(pr, st, &up);
+                    const float4 *dd = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) {
+                        const float4 v = dd[j];
+                        sr0[j] = df_add(sr0[j], dfl{v.x, v.y});
+                        si0[j] = df_add(si0[j], dfl{v.z, v.w});
+                    }
+                    wout = outer_weight(pr, st);
+                }
+            }
+        }
+        for (int l = 0; l < n_out; ++l) {
+            ddv r{0.0, 0.0}, i{0.0, 0.0};
+            if (active) {
+                const float4 a = acc.get(l);
+                r = dd_add_d(ddv{static_cast<double>(a.x), 0.0}, static_cast<double>(a.y));
+                i = dd_add_d(ddv{static_cast<double>(a.z), 0.0}, static_cast<double>(a.w));
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r = dd_add(r, dd_shfl_down(r, off));
+                i = dd_add(i, dd_shfl_down(i, off));
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+        }
+    }
+}
+
 }  // namespace pqg

@@ -1,0 +1,563 @@
+// Laplace-expansion walk kernels: for every column l, the permanent with the
+// multiplicity of column l lowered by one, all from ONE Gray-code walk
+// (Lemma 1 of arXiv:2005.04214, as the reference's
+// src/permanent_laplace.cpp:43-240).  The reference forms each of the nc
+// products separately, O(nc * N) multiplies per step; here a prefix pass and
+// a suffix pass give all nc products in O(nc):
+//     out_l += w * prefix_l * suffix_l * c_l^(m_l - 1),
+// and the final suffix w * prod_l c_l^(m_l) is the value shared by every
+// column of multiplicity zero (their exponent stays 0 in the reference).
+// Work split (R consecutive outer positions per lane), seeding, one-digit
+// outer steps, prefix tables and reductions are those of the plain kernels.
+#pragma once
+#include "walk_plain.cuh"
+
+namespace pqg {
+
+// Per-thread arrays that live either in registers or in a column-major slice
+// of dynamic shared memory (stride = threads per block).
+template <typename T, int N, bool SMEM>
+struct LaneArray;
+
+template <typename T, int N>
+struct LaneArray<T, N, false> {
+    T v[N];
+    __device__ __forceinline__ void init(T *, int) {}
+    __device__ __forceinline__ T get(int j) const { return v[j]; }
+    __device__ __forceinline__ void set(int j, T x) { v[j] = x; }
+};
+
+template <typename T, int N>
+struct LaneArray<T, N, true> {
+    T *p;
+    __device__ __forceinline__ void init(T *base, int tid) { p = base + tid; }
+    __device__ __forceinline__ T get(int j) const { return p[j * PQG_WALK_THREADS]; }
+    __device__ __forceinline__ void set(int j, T x) { p[j * PQG_WALK_THREADS] = x; }
+};
+
+template <int NC>
+struct LaplaceC128Cfg {
+    static constexpr bool PRE_SMEM = NC > 16;
+    static constexpr bool ACC_SMEM = NC > 20;
+    static constexpr size_t smem_bytes =
+        (PRE_SMEM ? size_t(NC) * PQG_WALK_THREADS * sizeof(double2) : 0) +
+        (ACC_SMEM ? size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) : 0);
+};
+
+// Complex128 Laplace walk.  R consecutive outer positions per lane, seeded in
+// FP64 and moved on by one-digit updates; the column sums of inner code t are
+// seed + Delta(t).  Per-lane sums are
+// plain FP64 over one inner walk (at most 512 codes), combined across lanes,
+// items and chunks in double-double.
+template <int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 1) walk_laplace_c128(WalkArgs A) {
+    using Cfg = LaplaceC128Cfg<NC>;
+    extern __shared__ double2 lap_smem[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<double2, NC, Cfg::PRE_SMEM> pre;
+    LaneArray<double2, NC + 1, Cfg::ACC_SMEM> acc;
+    pre.init(lap_smem, threadIdx.x);
+    acc.init(lap_smem + (Cfg::PRE_SMEM ? NC * PQG_WALK_THREADS : 0), threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        const bool active = r0 < pr->Q;
+        if (active) {
+            double sr0[NC], si0[NC];  // FP64 seed of this lane's current outer position
+            OuterState st;
+            outer_decode(pr, r0, st);
+            {
+                ArF64::cs_t s[NC];
+                seed_lane<ArF64, NC>(pr, A.arena, st, s);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
+                }
+            }
+            double wout = outer_weight(pr, st);
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const double2 *D = reinterpret_cast<const double2 *>(A.arena + pr->off_D);
+            int cm[NC];
+#pragma unroll
+            for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
+            const bool ones = pr->cm_max == 1;
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const double2 *delta = reinterpret_cast<const double2 *>(A.delta) + pr->delta_begin;
+            const int P = pr->P;
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) acc.set(l, make_double2(0.0, 0.0));
+
+            // R consecutive outer positions: the outer weight rides on every
+            // step weight (their product stays an exact integer below 2^53)
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+            for (int t = 0; t < P; ++t) {
+                const double w = __ldg(&tab[t].wd) * wout;
+                // column sums of inner code t are seed + prefix-table row t,
+                // formed where they are used (no per-step array of sums)
+                const double2 *d = delta + static_cast<int64_t>(t) * NC;
+                auto col = [&](int j, double &cr, double &ci) {
+                    const double2 v = __ldg(d + j);
+                    cr = __dadd_rn(sr0[j], v.x);
+                    ci = __dadd_rn(si0[j], v.y);
+                };
+                // prefix products: pre_l = prod_{k<l} c_k^(m_k)
+                double xr = 1.0, xi = 0.0;
+                pre.set(0, make_double2(1.0, 0.0));
+#pragma unroll
+                for (int j = 0; j + 1 < NC; ++j) {
+                    double cr, ci;
+                    col(j, cr, ci);
+                    if (j == 0 && (ones || cm[0] == 1)) {
+                        xr = cr;
+                        xi = ci;
+                    } else {
+                        const int e = ones ? 1 : cm[j];
+                        for (int r = 0; r < e; ++r) cmul(xr, xi, cr, ci);
+                    }
+                    pre.set(j + 1, make_double2(xr, xi));
+                }
+                // suffix pass
+                double sr = w, si = 0.0;
+#pragma unroll
+                for (int l = NC - 1; l >= 0; --l) {
+                    double cr, ci;
+                    col(l, cr, ci);
+                    const double2 p = pre.get(l);
+                    double tr, ti;
+                    if (l == NC - 1) {
+                        tr = p.x * w;
+                        ti = p.y * w;
+                    } else if (l == 0) {
+                        tr = sr;
+                        ti = si;
+                    } else {
+                        tr = p.x;
+                        ti = p.y;
+                        cmul(tr, ti, sr, si);
+                    }
+                    if (!ones)
+                        for (int r = 1; r < cm[l]; ++r) cmul(tr, ti, cr, ci);
+                    double2 a = acc.get(l);
+                    a.x = __dadd_rn(a.x, tr);
+                    a.y = __dadd_rn(a.y, ti);
+                    acc.set(l, a);
+                    if (l > 0 || full) {
+                        if (l == NC - 1) {
+                            sr = w * cr;
+                            si = w * ci;
+                            if (!ones)
+                                for (int r = 1; r < cm[l]; ++r) cmul(sr, si, cr, ci);
+                        } else {
+                            const int e = ones ? 1 : cm[l];
+                            for (int r = 0; r < e; ++r) cmul(sr, si, cr, ci);
+                        }
+                    }
+                }
+                if (full) {
+                    double2 a = acc.get(NC);
+                    a.x = __dadd_rn(a.x, sr);
+                    a.y = __dadd_rn(a.y, si);
+                    acc.set(NC, a);
+                }
+            }
+            if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                bool up = false;
+                const int k = outer_next(pr, st, &up);
+                const double2 *d = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = __dadd_rn(sr0[j], d[j].x);
+                    si0[j] = __dadd_rn(si0[j], d[j].y);
+                }
+                wout = outer_weight(pr, st);
+            }
+            }
+        }
+        // one output at a time: reduce over the warp, store
+        // (unrolled so that a register-resident accumulator array keeps static indices)
+#pragma unroll
+        for (int l = 0; l <= NC; ++l) {
+            if (l >= n_out) break;
+            ddv r{0.0, 0.0}, i{0.0, 0.0};
+            if (active) {
+                const double2 a = acc.get(l);
+                r = ddv{a.x, 0.0};
+                i = ddv{a.y, 0.0};
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r = dd_add(r, dd_shfl_down(r, off));
+                i = dd_add(i, dd_shfl_down(i, off));
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+        }
+    }
+}
+
+template <int NC>
+struct LaplaceC64Cfg {
+    static constexpr bool PRE_SMEM = NC > 16;
+    static constexpr size_t smem_bytes =
+        (PRE_SMEM ? size_t(NC) * PQG_WALK_THREADS * sizeof(float2) : 0) +
+        size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2);
+};
+
+// Complex64 Laplace walk: seed in double-float rounded to FP32, column sums
+// seed + Delta(t) and products in FP32, FP32 partial sums over 32 codes folded
+// into per-lane FP64 sums held in shared memory, lanes combined in FP64 (the
+// output is complex64).  ONES: every column has multiplicity 1 (the sampler's
+// case), so the repeated-factor code is compiled out; a fully unrolled
+// 24-column step with it did not fit the instruction cache (ncu: 9.7
+// no-instruction stalls per issue, 11 % issue).
+template <int NC, bool ONES>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) walk_laplace_c64(WalkArgs A) {
+    using Cfg = LaplaceC64Cfg<NC>;
+    extern __shared__ double2 lap_smem64[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<double2, NC + 1, true> acc64;
+    acc64.init(lap_smem64, threadIdx.x);
+    LaneArray<float2, NC, Cfg::PRE_SMEM> pre;
+    pre.init(reinterpret_cast<float2 *>(lap_smem64 + (NC + 1) * PQG_WALK_THREADS), threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        const bool active = r0 < pr->Q;
+        if (active) {
+            float sr0[NC], si0[NC];  // seed of the current outer position (double-float, rounded)
+            OuterState st;
+            outer_decode(pr, r0, st);
+            {
+                ArF32::cs_t s[NC];
+                seed_lane<ArF32, NC>(pr, A.arena, st, s);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
+                }
+            }
+            double wout = outer_weight(pr, st);
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
+            int cm[ONES ? 1 : NC];
+            if constexpr (!ONES) {
+#pragma unroll
+                for (int j = 0; j < NC; ++j) cm[j] = pr->cm[j];
+            }
+            const bool ones = ONES || pr->cm_max == 1;
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const float2 *delta = reinterpret_cast<const float2 *>(A.delta) + pr->delta_begin;
+            const int P = pr->P;
+            float ar[NC + 1], ai[NC + 1];
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) {
+                ar[l] = 0.0f;
+                ai[l] = 0.0f;
+                acc64.set(l, make_double2(0.0, 0.0));
+            }
+
+            // R consecutive outer positions; the FP32 partial sums fold into
+            // the FP64 accumulators weighted by the current outer weight
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+            for (int t = 0; t < P; ++t) {
+                const float w = __ldg(&tab[t].wf);
+                const float2 *d = delta + static_cast<int64_t>(t) * NC;
+                auto col = [&](int j, float &cr, float &ci) {
+                    const float2 v = __ldg(d + j);
+                    cr = __fadd_rn(sr0[j], v.x);
+                    ci = __fadd_rn(si0[j], v.y);
+                };
+                float xr = 1.0f, xi = 0.0f;
+                pre.set(0, make_float2(1.0f, 0.0f));
+#pragma unroll
+                for (int j = 0; j + 1 < NC; ++j) {
+                    float cr, ci;
+                    col(j, cr, ci);
+                    if constexpr (ONES) {
+                        if (j == 0) {
+                            xr = cr;
+                            xi = ci;
+                        } else {
+                            cmulf(xr, xi, cr, ci);
+                        }
+                    } else if (j == 0 && (ones || cm[0] == 1)) {
+                        xr = cr;
+                        xi = ci;
+                    } else {
+                        const int ee = ones ? 1 : cm[j];
+                        for (int r = 0; r < ee; ++r) cmulf(xr, xi, cr, ci);
+                    }
+                    pre.set(j + 1, make_float2(xr, xi));
+                }
+                float sr = w, si = 0.0f;
+#pragma unroll
+                for (int l = NC - 1; l >= 0; --l) {
+                    float cr, ci;
+                    col(l, cr, ci);
+                    const float2 p = pre.get(l);
+                    float tr, ti;
+                    if (l == NC - 1) {
+                        tr = p.x * w;
+                        ti = p.y * w;
+                    } else if (l == 0) {
+                        tr = sr;
+                        ti = si;
+                    } else {
+                        tr = p.x;
+                        ti = p.y;
+                        cmulf(tr, ti, sr, si);
+                    }
+                    if constexpr (!ONES) {
+                        if (!ones)
+                            for (int r = 1; r < cm[l]; ++r) cmulf(tr, ti, cr, ci);
+                    }
+                    ar[l] += tr;
+                    ai[l] += ti;
+                    if (l > 0 || full) {
+                        if (l == NC - 1) {
+                            sr = w * cr;
+                            si = w * ci;
+                            if constexpr (!ONES) {
+                                if (!ones)
+                                    for (int r = 1; r < cm[l]; ++r) cmulf(sr, si, cr, ci);
+                            }
+                        } else if constexpr (ONES) {
+                            cmulf(sr, si, cr, ci);
+                        } else {
+                            const int ee = ones ? 1 : cm[l];
+                            for (int r = 0; r < ee; ++r) cmulf(sr, si, cr, ci);
+                        }
+                    }
+                }
+                if (full) {
+                    ar[NC] += sr;
+                    ai[NC] += si;
+                }
+                if ((t & 31) == 31 || t == P - 1) {
+#pragma unroll
+                    for (int l = 0; l <= NC; ++l) {
+                        if (l == NC && !full) continue;
+                        double2 a = acc64.get(l);
+                        a.x = __fma_rn(wout, static_cast<double>(ar[l]), a.x);
+                        a.y = __fma_rn(wout, static_cast<double>(ai[l]), a.y);
+                        acc64.set(l, a);
+                        ar[l] = 0.0f;
+                        ai[l] = 0.0f;
+                    }
+                }
+            }
+            if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                bool up = false;
+                const int k = outer_next(pr, st, &up);
+                const float2 *d = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = __fadd_rn(sr0[j], d[j].x);
+                    si0[j] = __fadd_rn(si0[j], d[j].y);
+                }
+                wout = outer_weight(pr, st);
+            }
+            }
+        }
+        for (int l = 0; l < n_out; ++l) {
+            double r = 0.0, i = 0.0;
+            if (active) {
+                const double2 a = acc64.get(l);
+                r = a.x;
+                i = a.y;
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r += __shfl_down_sync(PQG_FULL_MASK, r, off);
+                i += __shfl_down_sync(PQG_FULL_MASK, i, off);
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, ddv{r, 0.0}, ddv{i, 0.0});
+        }
+    }
+}
+
+template <int NC>
+struct LaplaceDfCfg {
+    static constexpr size_t smem_bytes =
+        size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) + size_t(NC) * PQG_WALK_THREADS * sizeof(float4);
+};
+
+// Complex128 Laplace walk in double-float arithmetic on the FP32 pipes (the
+// default for complex128 when every column has multiplicity 1 -- the
+// sampler's case -- and the plan is in the double-float domain, as for the
+// plain walk): double-float seeds and column sums seed + Delta(t), prefix and
+// suffix products with unnormalised double-float pairs (df_cmul_lazy), the
+// step weight folded into the suffix's start, per-output double-float sums
+// (renormalising adds) over one inner walk in registers, folded with the
+// outer weight into per-lane FP64 sums in shared memory and combined across
+// lanes in double-double.  About 2^-48 per operation, against 2^-53 for the
+// FP64 walk, at the FP32 pipes' 61x higher rate.
+template <int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs A) {
+    extern __shared__ double2 lap_smem_df[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<double2, NC + 1, true> acc64;  // per-lane FP64 sums of every output
+    acc64.init(lap_smem_df, threadIdx.x);
+    LaneArray<float4, NC, true> pre;  // prefix products {re_hi, re_lo, im_hi, im_lo}
+    pre.init(reinterpret_cast<float4 *>(lap_smem_df + (NC + 1) * PQG_WALK_THREADS), threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        const bool active = r0 < pr->Q;
+        if (active) {
+            dfl sr0[NC], si0[NC];  // double-float seed of the current outer position
+            OuterState st;
+            outer_decode(pr, r0, st);
+            {
+                ArDF::cs_t s[NC];
+                seed_lane<ArDF, NC>(pr, A.arena, st, s);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
+                }
+            }
+            double wout = outer_weight(pr, st);
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const float4 *D = reinterpret_cast<const float4 *>(A.arena + pr->off_D);
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const float4 *delta = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin;
+            const int P = pr->P;
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) acc64.set(l, make_double2(0.0, 0.0));
+
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+                dfl ar[NC + 1], ai[NC + 1];  // this position's sums over the inner walk
+#pragma unroll
+                for (int l = 0; l <= NC; ++l) {
+                    ar[l] = dfl{0.0f, 0.0f};
+                    ai[l] = dfl{0.0f, 0.0f};
+                }
+                for (int t = 0; t < P; ++t) {
+                    const float w = __ldg(&tab[t].wf);  // exact in FP32 (the plan checks)
+                    const float4 *d = delta + static_cast<int64_t>(t) * NC;
+                    auto col = [&](int j, dfl &cr, dfl &ci) {
+                        const float4 v = __ldg(d + j);
+                        cr = df_add_lazy(sr0[j], dfl{v.x, v.y});
+                        ci = df_add_lazy(si0[j], dfl{v.z, v.w});
+                    };
+                    // prefix products: pre_l = prod_{k<l} c_k
+                    dfl xr{1.0f, 0.0f}, xi{0.0f, 0.0f};
+#pragma unroll
+                    for (int j = 0; j + 1 < NC; ++j) {
+                        dfl cr, ci;
+                        col(j, cr, ci);
+                        if (j == 0) {
+                            xr = cr;
+                            xi = ci;
+                        } else {
+                            df_cmul_lazy(xr, xi, cr, ci);
+                        }
+                        pre.set(j + 1, make_float4(xr.hi, xr.lo, xi.hi, xi.lo));
+                    }
+                    // suffix pass: out_l += w * pre_l * prod_{k>l} c_k.  The barrier
+                    // makes the pass reload its table entries and form the column
+                    // sums again, instead of keeping the prefix pass's NC sums live
+                    // (4 NC registers the kernel does not have)
+                    asm volatile("" ::: "memory");
+                    dfl sr{w, 0.0f}, si{0.0f, 0.0f};
+#pragma unroll
+                    for (int l = NC - 1; l >= 0; --l) {
+                        dfl cr, ci;
+                        col(l, cr, ci);
+                        dfl tr, ti;
+                        if (l == NC - 1) {
+                            const float4 p = pre.get(l);
+                            tr = df_scale(dfl{p.x, p.y}, w);
+                            ti = df_scale(dfl{p.z, p.w}, w);
+                        } else if (l == 0) {
+                            tr = sr;
+                            ti = si;
+                        } else {
+                            const float4 p = pre.get(l);
+                            tr = dfl{p.x, p.y};
+                            ti = dfl{p.z, p.w};
+                            df_cmul_lazy(tr, ti, sr, si);
+                        }
+                        { double2 q = acc64.get(l); q.x += tr.hi; q.y += ti.hi; acc64.set(l, q); }
+                        if (l > 0 || full) {
+                            if (l == NC - 1) {
+                                sr = df_scale(cr, w);
+                                si = df_scale(ci, w);
+                            } else {
+                                df_cmul_lazy(sr, si, cr, ci);
+                            }
+                        }
+                    }
+                    if (full) {
+                        ar[NC] = df_add(ar[NC], sr);
+                        ai[NC] = df_add(ai[NC], si);
+                    }
+                }
+                // fold this position's sums, weighted by the outer weight
+#pragma unroll
+                for (int l = 0; l <= NC; ++l) {
+                    if (l == NC && !full) continue;
+                    double2 a = acc64.get(l);
+                    a.x = __fma_rn(wout, static_cast<double>(ar[l].hi), a.x);
+                    a.x = __fma_rn(wout, static_cast<double>(ar[l].lo), a.x);
+                    a.y = __fma_rn(wout, static_cast<double>(ai[l].hi), a.y);
+                    a.y = __fma_rn(wout, static_cast<double>(ai[l].lo), a.y);
+                    acc64.set(l, a);
+                }
+                if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                    bool up = false;
+                    const int k = outer_next(pr, st, &up);
+                    const float4 *dd = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) {
+                        const float4 v = dd[j];
+                        sr0[j] = df_add(sr0[j], dfl{v.x, v.y});
+                        si0[j] = df_add(si0[j], dfl{v.z, v.w});
+                    }
+                    wout = outer_weight(pr, st);
+                }
+            }
+        }
+        for (int l = 0; l < n_out; ++l) {
+            ddv r{0.0, 0.0}, i{0.0, 0.0};
+            if (active) {
+                const double2 a = acc64.get(l);
+                r = ddv{a.x, 0.0};
+                i = ddv{a.y, 0.0};
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r = dd_add(r, dd_shfl_down(r, off));
+                i = dd_add(i, dd_shfl_down(i, off));
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+        }
+    }
+}
+
+}  // namespace pqg

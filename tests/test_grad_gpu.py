@@ -71,14 +71,20 @@ def test_batched_matches_single(engine):
     G = engine.permanent_grad(As, rows, cols)
     assert G.shape == As.shape
     for idx in np.ndindex(3, 2):
+        # the batch and a single call may walk in different arithmetics (a
+        # batch with a repeated column takes the FP64 Laplace walk for all
+        # its matrices, an all-ones matrix alone the double-float one): they
+        # agree to complex128 accuracy
         single = engine.permanent_grad(As[idx], rows[idx], cols[idx])
-        assert np.array_equal(G[idx], single)
+        scale = max(1.0, float(np.max(np.abs(single))))
+        assert np.max(np.abs(G[idx] - single)) <= 1e-11 * scale
         _check(engine, As[idx], rows[idx], cols[idx])
     # shared multiplicities broadcast over the batch
     r1, c1 = np.array([1, 2, 0, 1, 1]), np.array([1, 1, 1, 1, 1])
     Gb = engine.permanent_grad(As, r1, c1)
     for idx in np.ndindex(3, 2):
-        assert np.array_equal(Gb[idx], engine.permanent_grad(As[idx], r1, c1))
+        single = engine.permanent_grad(As[idx], r1, c1)
+        assert np.max(np.abs(Gb[idx] - single)) <= 1e-11 * max(1.0, float(np.max(np.abs(single))))
 
 
 def test_edge_cases(engine):

@@ -82,3 +82,28 @@ def test_seeded_sampler_golden(engine):
     samples = osampler.generate_samples(np.array(g["input"]), g["shots"], engine.permanent_laplace, U, g["seed"])
     assert [list(s) for s in samples] == g["generated_samples"]
     assert [list(s) for s in osampler.result_samples(samples, g["seed"])] == g["expected_samples"]
+
+
+def test_double_float_laplace_matches_fp64_at_full_size(engine):
+    """complex128 Laplace permanents take the double-float walk by default
+    (all-ones columns); at the sampler's full size (23 output photons with
+    collisions, 24 unit input columns, d=48) they agree with the FP64 walk
+    within the complex128 bound max(1e-10 |value|, 1e-14 perm(|A|)) -- the
+    permanent of |A| with column l lowered bounds every output l."""
+    rng = np.random.default_rng(12)
+    d, n = 48, 24
+    U = haar_unitary(d, 3)
+    cols = np.array([1] * n + [0] * (d - n))
+    R = np.stack([np.bincount(rng.integers(0, d, n - 1), minlength=d) for _ in range(64)])
+    with engine.PermanentPlan(U, R, cols, form="laplace", mode="df") as p:
+        df = p.run()
+    with engine.PermanentPlan(U, R, cols, form="laplace", mode="fp64") as p:
+        f64 = p.run()
+    with engine.PermanentPlan(np.abs(U).astype(np.complex128), R, cols, form="laplace", mode="fp64") as p:
+        pabs = np.abs(p.run())
+    assert df.shape == f64.shape == (64, d)
+    bound = np.maximum(1e-10 * np.abs(f64), 1e-14 * pabs)
+    assert np.all(np.abs(df - f64) <= bound), float(np.max(np.abs(df - f64) / np.maximum(bound, 1e-300)))
+    # the default entry point (double-float) agrees as well
+    direct = engine.permanent_laplace_batch(U, R, np.broadcast_to(cols, R.shape))
+    assert np.all(np.abs(direct - f64) <= bound)
