@@ -542,7 +542,8 @@ def profile_case(name):
                    n=24, d=48 (48 launches per draw): one eager draw, then 3
                    graph replays;
       draw2048   — the exact sampler's fused step (Laplace permanents + pmf +
-                   draw) for 2048 shots after 16 photons at n=24, d=48, 3 calls."""
+                   draw) for 2048 shots after 16 photons at n=24, d=48, 3 calls;
+      laplace24c128 — laplace24 in complex128 (the double-float Laplace walk)."""
     import ctypes
 
     import __graft_entry__
@@ -576,7 +577,7 @@ def profile_case(name):
         pats = y.cpu().numpy().astype(np.int64)
         for _ in range(3):
             pge.permanent_batch(U.astype(np.complex64), pats, inp)
-    elif name == "laplace24":
+    elif name in ("laplace24", "laplace24c128"):
         # the exact sampler's last photon step at n=24, d=48: 1024 shots with 23
         # photons placed (exact samples less one photon), 24 input columns
         from piquasso_gb300 import sampling
@@ -590,8 +591,9 @@ def profile_case(name):
             nz = np.nonzero(rows[s_])[0]
             rows[s_, nz[rng.integers(len(nz))]] -= 1
         cols = np.broadcast_to(inp, rows.shape)
+        dt = np.complex64 if name == "laplace24" else np.complex128
         for _ in range(3):
-            pge.permanent_laplace_batch(U.astype(np.complex64), rows, cols)
+            pge.permanent_laplace_batch(U.astype(dt), rows, cols)
     elif name == "propose8192":
         U = workloads.haar_unitary(48, 3)
         inp = np.array([1] * 24 + [0] * 24)

@@ -58,3 +58,40 @@ def test_plan_complex64_and_laplace(engine):
     for k in range(len(pats)):
         dd = oracle.permanent(U64.astype(np.complex128), pats[k], cols)
         assert abs(v[k] - dd) <= max(1e-5 * abs(dd), 2.0 ** -23 * oracle.perm_abs(U64, pats[k], cols))
+
+
+@pytest.mark.parametrize("dtype,mode", [(np.complex64, "auto"), (np.complex128, "auto"), (np.complex128, "fp64")])
+@pytest.mark.parametrize("seed", range(3))
+def test_random_batches_against_oracle(engine, dtype, mode, seed):
+    """Randomised batches that exercise the planner's work split: problems of
+    very different sizes (longest items first, outputs in caller order), whole
+    warps and groups of items with empty trailing items, 1..20 distinct
+    columns padded to the batch's widest (shared-memory tables from 17
+    columns), repeated rows and columns, and constant (empty) problems."""
+    rng = np.random.default_rng(1000 + seed)
+    d = 22
+    U = haar_unitary(d, 50 + seed).astype(dtype)
+    R, C = [], []
+    for b in range(40):
+        n = int(rng.integers(0, 19)) if b % 13 else 0
+        rows = np.bincount(rng.integers(0, d, n), minlength=d)
+        if b % 3 == 0:  # distinct input columns
+            cols = np.zeros(d, dtype=int)
+            cols[rng.permutation(d)[:n]] = 1
+        else:
+            cols = np.bincount(rng.integers(0, d, n), minlength=d)
+        R.append(rows)
+        C.append(cols)
+    R, C = np.stack(R), np.stack(C)
+    if mode == "auto":
+        got = engine.permanent_batch(U, R, C)
+    else:
+        with engine.PermanentPlan(U, R, C, mode=mode) as p:
+            got = p.run()
+    for b in range(len(R)):
+        dd = oracle.permanent(U.astype(np.complex128), R[b], C[b])
+        if dtype == np.complex64:
+            tol = max(1e-5 * abs(dd), 2.0 ** -22 * oracle.perm_abs(U.astype(np.complex128), R[b], C[b]))
+        else:
+            tol = max(1e-10 * abs(dd), 1e-14 * oracle.perm_abs(U.astype(np.complex128), R[b], C[b]))
+        assert abs(complex(got[b]) - dd) <= tol, (b, got[b], dd)
