@@ -348,7 +348,7 @@ void Planner::finish() {
     // in shared memory, which holds PQG_SMEM_TABLE_P codes (a hard limit, over
     // any tuning)
     if (prec_ == Precision::C64 && !laplace && ncmax >= PQG_SMEM_TABLE_NC_MIN && ncmax <= PQG_SMEM_TABLE_NC_MAX)
-        p_max = std::min<int64_t>(p_max, ncmax > PQG_SMEM_TABLE_NC_WIDE ? PQG_SMEM_TABLE_P / 2 : PQG_SMEM_TABLE_P);
+        p_max = std::min<int64_t>(p_max, PQG_SMEM_TABLE_P);
     // per-problem device data (built by the prep kernel), by offset from the
     // start of that region; the region follows the uploaded arena
     auto pdata = [&](int64_t bytes) {

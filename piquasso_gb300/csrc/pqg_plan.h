@@ -29,11 +29,9 @@
 #define PQG_CHUNK_ITEMS 64
 #define PQG_ITEM_GROUP 4  // items (warps) a block of the complex64 plain walk takes at once
 // complex64 plain walks of these column counts read the prefix table from
-// shared memory, which holds at most PQG_SMEM_TABLE_P codes (half that above
-// PQG_SMEM_TABLE_NC_WIDE columns, so two blocks' tables still fit an SM)
+// shared memory, which holds at most PQG_SMEM_TABLE_P codes
 #define PQG_SMEM_TABLE_NC_MIN 17
 #define PQG_SMEM_TABLE_NC_MAX 24
-#define PQG_SMEM_TABLE_NC_WIDE 24
 #define PQG_SMEM_TABLE_P 256
 
 enum PqgProblemKind : int32_t {

@@ -333,8 +333,9 @@ __device__ __forceinline__ void two_sum_acc2(float2 &s, float2 &c, float2 y) {
 // entry's register is refilled with row `next`'s entry right after its column
 // sum is formed, so the next code's loads are in flight a whole product
 // ahead.  The rows then stay live across codes, which only the narrower
-// kernels' register budgets allow (REFILL_MAX_NC).
-constexpr int REFILL_MAX_NC = 24;
+// kernels' register budgets allow (REFILL_MAX_NC; from 17 columns on the
+// rows come from the block's shared-memory table instead).
+constexpr int REFILL_MAX_NC = 16;
 template <int NC, bool REFILL>
 __device__ __forceinline__ void row_product_packed(const float2 (&sr)[NC], const float2 (&si)[NC], float4 (&dq)[NC],
                                                    const float4 *__restrict__ next, const uint8_t *__restrict__ cm,
@@ -441,7 +442,7 @@ constexpr int SMEM_TAB_NC_MIN = PQG_SMEM_TABLE_NC_MIN, SMEM_TAB_NC_MAX = PQG_SME
               SMEM_TAB_G = 8;
 template <int NC>
 __host__ __device__ constexpr int smem_tab_codes() {
-    return NC > PQG_SMEM_TABLE_NC_WIDE ? PQG_SMEM_TABLE_P / 2 : PQG_SMEM_TABLE_P;
+    return PQG_SMEM_TABLE_P;
 }
 template <class Ar, int NC>
 __host__ __device__ constexpr bool plain_smem_table() {
