@@ -425,6 +425,54 @@ __device__ __forceinline__ void row_product_packed_smem(const float2 (&sr)[NC], 
     pi = xi;
 }
 
+// Two codes (rows a and b of the shared-memory table) at once, columns
+// interleaved: eight independent packed chains.  Each product is the same
+// operation sequence as row_product_packed_smem's, so the accumulation of
+// code a then code b is bit-identical to two single calls.
+template <int NC, int G>
+__device__ __forceinline__ void row_product_packed_smem_pair(const float2 (&sr)[NC], const float2 (&si)[NC],
+                                                             const float4 *a, const float4 *b,
+                                                             const uint8_t *__restrict__ cm, bool ones, float2 &pra,
+                                                             float2 &pia, float2 &prb, float2 &pib) {
+    float2 xra, xia, yra, yia, xrb, xib, yrb, yib;
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        if (j % G == 0) asm volatile("" ::: "memory");
+        const float4 da = a[j], db = b[j];
+        const float2 cra = __fadd2_rn(sr[j], make_float2(da.x, da.y));
+        const float2 cia = __fadd2_rn(si[j], make_float2(da.z, da.w));
+        const float2 crb = __fadd2_rn(sr[j], make_float2(db.x, db.y));
+        const float2 cib = __fadd2_rn(si[j], make_float2(db.z, db.w));
+        const int reps = ones ? 1 : cm[j];
+        if (j == 0) {
+            xra = cra, xia = cia, xrb = crb, xib = cib;
+            for (int r = 1; r < reps; ++r) {
+                cmul2(xra, xia, cra, cia);
+                cmul2(xrb, xib, crb, cib);
+            }
+        } else if (j == 1) {
+            yra = cra, yia = cia, yrb = crb, yib = cib;
+            for (int r = 1; r < reps; ++r) {
+                cmul2(yra, yia, cra, cia);
+                cmul2(yrb, yib, crb, cib);
+            }
+        } else {
+            for (int r = 0; r < reps; ++r) {
+                if (j & 1) {
+                    cmul2(yra, yia, cra, cia);
+                    cmul2(yrb, yib, crb, cib);
+                } else {
+                    cmul2(xra, xia, cra, cia);
+                    cmul2(xrb, xib, crb, cib);
+                }
+            }
+        }
+    }
+    cmul2(xra, xia, yra, yia);
+    cmul2(xrb, xib, yrb, yib);
+    pra = xra, pia = xia, prb = xrb, pib = xib;
+}
+
 // Blocks per SM the register allocation must allow: the column sums of the
 // wider kernels need up to 255 registers per thread, and a spill inside the
 // step loop costs more than the occupancy it buys.
@@ -564,7 +612,20 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
                     // (the staged table holds at most smem_tab_codes<NC>() codes: the plan
                     // guarantees P fits; the bound keeps every read inside it)
                     const int Pw = smem_tab ? (P < smem_tab_codes<NC>() ? P : smem_tab_codes<NC>()) : P;
-                    for (int t = 0; t < Pw; ++t) {
+                    int t = 0;
+                    if constexpr (smem_tab) {  // two codes at a time, then a last odd one
+                        for (; t + 1 < Pw; t += 2) {
+                            float2 xra, xia, xrb, xib;
+                            row_product_packed_smem_pair<NC, SMEM_TAB_G>(pr2, pi2, s_tab + t * NC, s_tab + (t + 1) * NC,
+                                                                         cm, ones, xra, xia, xrb, xib);
+                            const float wa = tab[t].wf, wb2 = tab[t + 1].wf;
+                            two_sum_acc2(accr, accrc, __fmul2_rn(make_float2(wa, wa), xra));
+                            two_sum_acc2(acci, accic, __fmul2_rn(make_float2(wa, wa), xia));
+                            two_sum_acc2(accr, accrc, __fmul2_rn(make_float2(wb2, wb2), xrb));
+                            two_sum_acc2(acci, accic, __fmul2_rn(make_float2(wb2, wb2), xib));
+                        }
+                    }
+                    for (; t < Pw; ++t) {
                         float2 xr, xi;
                         if constexpr (smem_tab) {
                             row_product_packed_smem<NC, SMEM_TAB_G>(pr2, pi2, s_tab + t * NC, cm, ones, xr, xi);
