@@ -513,12 +513,21 @@ def run_ours(args, world, rank, local, pg):
                                   "achieved_tflops": F / w / 1e12, "peak_fp32_tflops": peaks["fp32_tflops"],
                                   "frac": F / w / 1e12 / peaks["fp32_tflops"],
                                   "rel_diff_vs_default": abs(complex(r32) - complex(result)) / abs(complex(result))}
+    def section(fn, *a, **kw):
+        # a secondary line that fails records its error instead of taking
+        # the headline line down with it
+        try:
+            return fn(*a, **kw)
+        except Exception as e:  # noqa: BLE001
+            return {"error": "%s: %s" % (type(e).__name__, e)}
+
     if not args.no_variants:
-        line["batch_4096_d40_n20"] = bench_batch(pg_engine, torch, flush, args, cpu=(rank == 0 and not args.no_cpu_baseline))
+        line["batch_4096_d40_n20"] = section(bench_batch, pg_engine, torch, flush, args,
+                                             cpu=(rank == 0 and not args.no_cpu_baseline))
     if not args.no_variants and not args.no_sampling:
-        line["sampling_n24_d48"] = bench_sampling(args)
-        line["training_mlp"] = bench_training(args)
-        line["next_rows"] = bench_next_rows(args, cpu=(rank == 0 and not args.no_cpu_baseline))
+        line["sampling_n24_d48"] = section(bench_sampling, args)
+        line["training_mlp"] = section(bench_training, args)
+        line["next_rows"] = section(bench_next_rows, args, cpu=(rank == 0 and not args.no_cpu_baseline))
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
         line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",
