@@ -525,8 +525,8 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
     static_assert(!grouped || PQG_ITEM_GROUP * 32 == PQG_WALK_THREADS, "one item per warp of a block");
     __shared__ unsigned long long s_group;
     // 17..24 columns: the group's prefix table in shared memory (dynamic,
-    // smem_tab_codes<NC>() x NC entries), read by all four warps; without the table row
-    // in registers the kernel fits three blocks per SM
+    // smem_tab_codes<NC>() x NC entries, up to 96 KB: two blocks per SM), read
+    // by all four warps; the table rows then need no registers
     constexpr bool smem_tab = plain_smem_table<Ar, NC>();
     extern __shared__ float4 s_tab[];
     int staged = -1;
