@@ -1,0 +1,62 @@
+// Test driver for the host planner (compiled with g++ by tests/test_planner_cpu.py;
+// no CUDA): reads problems from stdin, plans them, prints the plan as JSON.
+//
+// stdin: prec form nr nc batch, then the matrix is all zeros except entry
+// (0,0) = 1 (the planner copies it and never reads values), then batch lines
+// of nr row multiplicities followed by nc column multiplicities.
+// prec: 0 = C128, 1 = C64, 2 = C128DF; form: 0 = plain, 1 = Laplace.
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "plan.hpp"
+
+using namespace pqg;
+
+int main() {
+    int prec_i, form_i;
+    long long nr, nc, batch;
+    if (scanf("%d %d %lld %lld %lld", &prec_i, &form_i, &nr, &nc, &batch) != 5) return 2;
+    const Precision prec = prec_i == 0 ? Precision::C128 : (prec_i == 1 ? Precision::C64 : Precision::C128DF);
+    const Form form = form_i ? Form::LAPLACE : Form::PLAIN;
+    std::vector<double> a(static_cast<size_t>(2 * nr * nc), 0.0);
+    if (!a.empty()) a[0] = 1.0;
+    std::vector<int32_t> rows(static_cast<size_t>(batch * nr)), cols(static_cast<size_t>(batch * nc));
+    for (long long b = 0; b < batch; ++b) {
+        for (long long i = 0; i < nr; ++i) scanf("%d", &rows[b * nr + i]);
+        for (long long j = 0; j < nc; ++j) scanf("%d", &cols[b * nc + j]);
+    }
+    PlanConfig cfg;
+    if (form == Form::LAPLACE) cfg.p_max = 512;
+    Planner pl(prec, form, cfg);
+    pl.set_matrix(a.data(), nr, nc);
+    for (long long b = 0; b < batch; ++b) {
+        std::string err;
+        const int st = pl.add(rows.data() + b * nr, cols.data() + b * nc, err);
+        if (st) {
+            printf("{\"error\": %d, \"problem\": %lld, \"message\": \"%s\"}\n", st, b, err.c_str());
+            return 0;
+        }
+    }
+    pl.finish();
+    printf("{\"total_items\": %lld, \"total_outputs\": %lld, \"item_group\": %d, \"df_ok\": %d, \"all_ones\": %d, "
+           "\"max_nc\": %d, \"out_of\": [",
+           static_cast<long long>(pl.total_items), static_cast<long long>(pl.total_outputs), pl.item_group,
+           pl.df_ok ? 1 : 0, pl.all_ones ? 1 : 0, pl.max_nc);
+    for (size_t b = 0; b < pl.out_of.size(); ++b) printf("%s%lld", b ? ", " : "", static_cast<long long>(pl.out_of[b]));
+    printf("], \"item_begin\": [");
+    for (size_t i = 0; i < pl.item_begin.size(); ++i)
+        printf("%s%lld", i ? ", " : "", static_cast<long long>(pl.item_begin[i]));
+    printf("], \"probs\": [");
+    for (size_t i = 0; i < pl.probs.size(); ++i) {
+        const PqgProblem &q = pl.probs[i];
+        printf("%s{\"index\": %d, \"kind\": %d, \"n_out\": %d, \"out_index\": %lld, \"item_begin\": %lld, "
+               "\"n_items\": %lld, \"P\": %d, \"K\": %d, \"n_outer\": %d, \"Q\": %lld, \"R\": %lld, \"nc\": %d, "
+               "\"S\": %.17g}",
+               i ? ", " : "", q.index, q.kind, q.n_out, static_cast<long long>(q.out_index),
+               static_cast<long long>(q.item_begin), static_cast<long long>(q.n_items), q.P, q.K, q.n_outer,
+               static_cast<long long>(q.Q), static_cast<long long>(q.R), q.nc, pl.pending[q.index].S);
+    }
+    printf("]}\n");
+    return 0;
+}
