@@ -126,6 +126,18 @@ def last_timing():
     return {k: x.value for k, x in zip(keys, v)}
 
 
+def check_tc_status():
+    """Raises if a tensor-core kernel (the MLP GEMM or the fused proposal
+    step) gave up a bounded wait since the last check (its results are then
+    not to be trusted); clears the flag."""
+    code = ctypes.c_int32(0)
+    st = load().pqg_mlp_tc_status(ctypes.byref(code))
+    if st:
+        raise RuntimeError(last_error())
+    if code.value:
+        raise RuntimeError("a tensor-core kernel gave up a bounded wait (code %d)" % code.value)
+
+
 def set_tuning(items_per_smsp=0, p_max=0, seed_steps=0):
     """Planner knobs (0 restores the default); see include/pqperm_gb300.h."""
     st = load().pqg_set_tuning(int(items_per_smsp), int(p_max), int(seed_steps))

@@ -104,6 +104,8 @@ class ProposalSampler:
         v = int(seed) % (1 << 64)  # the bits of the uint64 seed, stored as int64
         self.seed_dev.fill_(v - (1 << 64) if v >= (1 << 63) else v)
         self.graph.replay()
+        if self.fused:
+            _lib.check_tc_status()  # (synchronises; the caller reads the draw at once anyway)
         return self.samples, self.logq
 
     def _draw_rounds(self):

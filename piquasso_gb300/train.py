@@ -16,7 +16,7 @@ import time
 
 import numpy as np
 
-from . import proposal, sampling, workloads
+from . import _lib, proposal, sampling, workloads
 from .metropolis import log_target
 
 
@@ -90,6 +90,7 @@ def train(data, epochs=3, batch=65536, lr=2e-3, seed=0, log=print):
             mlp.adam(gW, gb, lr=lr)
             tot += float(loss.mean().item())
             cnt += 1
+        _lib.check_tc_status()
         history.append(tot / max(1, cnt))
         log("epoch %d: mean cross-entropy %.5f nats/mode (%.1f s)" % (ep, history[-1], time.perf_counter() - t0))
     return mlp, history
