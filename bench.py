@@ -53,10 +53,19 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=25):
         self.gpu = gpu_index
+        self.interval_ms = interval_ms
         self.proc = None
         self.path = None
+        self.mark = 0
+
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return sum(1 for line in f if line.count(",") >= 8)
+        except OSError:
+            return 0
 
     def __enter__(self):
         try:
@@ -64,10 +73,21 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", str(self.interval_ms)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return self
         return self
+
+    def start_region(self):
+        """Marks the start of the timed region: the samples taken from here on
+        are the region's.  Entered before the warm-up, so that nvidia-smi's
+        start-up does not fall into a short region."""
+        t0 = time.perf_counter()
+        while self.proc is not None and self._lines() == 0 and time.perf_counter() - t0 < 5.0 and \
+                self.proc.poll() is None:
+            time.sleep(0.01)
+        self.mark = self._lines() if self.proc is not None else 0
 
     def __exit__(self, *a):
         if self.proc is not None:
@@ -82,7 +102,11 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        rows = [line for line in open(self.path) if line.count(",") >= 8]
+        # the samples taken during the region (the last one before it if the
+        # region was shorter than one interval)
+        rows = rows[self.mark:] or rows[max(0, self.mark - 1):self.mark]
+        for line in rows:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -424,14 +448,15 @@ def run_ours(args, world, rank, local, pg):
     peaks = pg_engine.measure_vector_peaks(20.0)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > L2 (129 MB)
 
-    for _ in range(args.warmup):
-        pg_engine.permanent(U, ones, ones)
-    torch.cuda.synchronize()
-    if pg is not None:
-        pg.barrier()
-
-    launches0 = pg_engine.kernel_launches()
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):  # the timed steps' work, flush included
+            flush.zero_()
+            pg_engine.permanent(U, ones, ones)
+        torch.cuda.synchronize()
+        if pg is not None:
+            pg.barrier()
+        launches0 = pg_engine.kernel_launches()
+        clk.start_region()
         t_region = time.perf_counter()
         dev_ms, walk_ms, e2e_s, tm, result = time_calls(pg_engine, torch, flush, U, ones, args.steps, "api")
         torch.cuda.synchronize()
