@@ -48,6 +48,8 @@ CU_SOURCES = [
     "k_laplace_c64o_1.cu",
     "k_laplace_dfo_0.cu",
     "k_laplace_dfo_1.cu",
+    "k_laplace_df_0.cu",
+    "k_laplace_df_1.cu",
 ]
 CPP_SOURCES = ["plan.cpp"]
 

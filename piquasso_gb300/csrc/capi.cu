@@ -92,7 +92,7 @@ struct Context {
     HostBuf h_plan, h_out;
     PlanConfig cfg;
     int blocks_per_sm = 0;  // 0: as many as fit (occupancy)
-    std::vector<int> occ_cache[10];  // blocks per SM, per kernel table, per column count
+    std::vector<int> occ_cache[11];  // blocks per SM, per kernel table, per column count
 
     int init() {
         if (ready) return PQG_OK;
@@ -142,9 +142,12 @@ const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_on
         *which = 3;
         return kernel_for(k_laplace_c64_0, k_laplace_c64_1, nc);
     }
-    if (prec == Precision::C128DF) {  // the plan falls back to FP64 unless every column has multiplicity 1
-        *which = 9;
-        return kernel_for(k_laplace_dfo_0, k_laplace_dfo_1, nc);
+    if (prec == Precision::C128DF) {
+        // the all-ones instantiations spill above 25 columns; the general ones
+        // (multiplicities read from the problem record) do not
+        const bool ones = all_ones && nc <= 25;
+        *which = ones ? 9 : 10;
+        return ones ? kernel_for(k_laplace_dfo_0, k_laplace_dfo_1, nc) : kernel_for(k_laplace_df_0, k_laplace_df_1, nc);
     }
     *which = 2;
     return kernel_for(k_laplace_c128_0, k_laplace_c128_1, nc);
@@ -441,11 +444,10 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     return run_plan<T>(C, pl, out, out_lo);
 }
 
-// The double-float Laplace walk serves all-ones columns in the double-float
-// domain, up to 25 columns (wider instantiations spill); any other complex128
-// Laplace plan is redone for the FP64 walk.
+// The double-float Laplace walk serves plans in the double-float domain; any
+// other complex128 Laplace plan is redone for the FP64 walk.
 void laplace_precision_fallback(Planner &pl) {
-    if (pl.precision() == Precision::C128DF && (!pl.df_ok || !pl.all_ones || pl.max_nc > 25)) {
+    if (pl.precision() == Precision::C128DF && !pl.df_ok) {
         pl.set_precision(Precision::C128);
         pl.finish();
     }

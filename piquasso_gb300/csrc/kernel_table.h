@@ -33,6 +33,8 @@ extern const KernelInfo k_laplace_c64o_0[16];  // every column of multiplicity 1
 extern const KernelInfo k_laplace_c64o_1[16];
 extern const KernelInfo k_laplace_dfo_0[16];  // double-float, every column of multiplicity 1
 extern const KernelInfo k_laplace_dfo_1[16];
+extern const KernelInfo k_laplace_df_0[16];  // double-float, any column multiplicities
+extern const KernelInfo k_laplace_df_1[16];
 
 // the instantiation for exactly nc columns (1 <= nc <= 32)
 inline const KernelInfo &kernel_for(const KernelInfo *lo_half, const KernelInfo *hi_half, int nc) {

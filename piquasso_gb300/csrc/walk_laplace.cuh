@@ -398,8 +398,8 @@ struct LaplaceDfCfg {
 };
 
 // Complex128 Laplace walk in double-float arithmetic on the FP32 pipes (the
-// default for complex128 when every column has multiplicity 1 -- the
-// sampler's case -- and the plan is in the double-float domain): double-float
+// default for complex128 when the plan is in the double-float domain; ONES:
+// every column has multiplicity 1, the sampler's usual case): double-float
 // seeds and column sums seed + Delta(t), prefix and suffix products with
 // unnormalised double-float pairs (df_cmul_lazy), and the step's whole weight
 // w(t) * w_outer folded into the suffix's start -- an exact FP32 integer, as
@@ -408,7 +408,7 @@ struct LaplaceDfCfg {
 // lane's positions.  Those sums and the prefix products live in shared memory
 // (registers hold the seeds); lanes are combined in double-double.  About
 // 2^-48 per operation, against 2^-53 for the FP64 walk, on pipes 61x faster.
-template <int NC>
+template <int NC, bool ONES>
 __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs A) {
     extern __shared__ float4 lap_smem_df[];
     const int lane = threadIdx.x & 31;
@@ -447,6 +447,9 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
             const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
             const float4 *delta = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin;
             const int P = pr->P;
+            // column multiplicities (repeated-column kernel): read from the
+            // problem record (L1, the same for the whole warp), not registers
+            const uint8_t *cm = pr->cm;
 #pragma unroll
             for (int l = 0; l <= NC; ++l) acc.set(l, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             auto add_to = [&](int l, dfl tr, dfl ti) {
@@ -474,8 +477,12 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
                         if (j == 0) {
                             xr = cr;
                             xi = ci;
-                        } else {
+                            if constexpr (!ONES)
+                                for (int r = 1; r < cm[0]; ++r) df_cmul_lazy(xr, xi, cr, ci);
+                        } else if constexpr (ONES) {
                             df_cmul_lazy(xr, xi, cr, ci);
+                        } else {
+                            for (int r = 0; r < cm[j]; ++r) df_cmul_lazy(xr, xi, cr, ci);
                         }
                         pre.set(j + 1, make_float4(xr.hi, xr.lo, xi.hi, xi.lo));
                     }
@@ -500,13 +507,19 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
                             ti = dfl{p.z, p.w};
                             df_cmul_lazy(tr, ti, sr, si);
                         }
+                        if constexpr (!ONES)  // out_l keeps cols_l - 1 factors of c_l
+                            for (int r = 1; r < cm[l]; ++r) df_cmul_lazy(tr, ti, cr, ci);
                         add_to(l, tr, ti);
                         if (l > 0 || full) {
                             if (l == NC - 1) {
                                 sr = df_scale(cr, w);
                                 si = df_scale(ci, w);
-                            } else {
+                                if constexpr (!ONES)
+                                    for (int r = 1; r < cm[l]; ++r) df_cmul_lazy(sr, si, cr, ci);
+                            } else if constexpr (ONES) {
                                 df_cmul_lazy(sr, si, cr, ci);
+                            } else {
+                                for (int r = 0; r < cm[l]; ++r) df_cmul_lazy(sr, si, cr, ci);
                             }
                         }
                     }

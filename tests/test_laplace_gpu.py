@@ -107,3 +107,33 @@ def test_double_float_laplace_matches_fp64_at_full_size(engine):
     # the default entry point (double-float) agrees as well
     direct = engine.permanent_laplace_batch(U, R, np.broadcast_to(cols, R.shape))
     assert np.all(np.abs(direct - f64) <= bound)
+
+
+def test_double_float_laplace_repeated_columns(engine):
+    """Repeated input columns (multi-photon input modes) take the general
+    double-float Laplace kernel: each output keeps cols_l - 1 factors of its
+    column.  Against the FP64 walk within the complex128 bound."""
+    rng = np.random.default_rng(31)
+    d, n = 30, 19
+    U = haar_unitary(d, 7)
+    C = []
+    for b in range(48):
+        c = np.zeros(d, dtype=int)
+        c[rng.permutation(d)[:n - 4]] = 1
+        c[rng.permutation(np.nonzero(c)[0])[:4]] += 1  # four doubly occupied input modes
+        C.append(c)
+    C = np.stack(C)
+    R = np.stack([np.bincount(rng.integers(0, d, n - 1), minlength=d) for _ in range(48)])
+    with engine.PermanentPlan(U, R, C, form="laplace", mode="df") as p:
+        df = p.run()
+    with engine.PermanentPlan(U, R, C, form="laplace", mode="fp64") as p:
+        f64 = p.run()
+    for b in range(len(R)):
+        for l in np.nonzero(C[b])[0]:
+            cl = C[b].copy()
+            cl[l] -= 1
+            bound = max(1e-10 * abs(f64[b, l]), 1e-14 * oracle.perm_abs(U, R[b], cl))
+            assert abs(df[b, l] - f64[b, l]) <= bound, (b, l)
+    dd = oracle.permanent_laplace_dd(U, R[0], C[0])
+    nz = C[0] > 0
+    assert np.allclose(df[0][nz], dd[nz], rtol=1e-10, atol=0)
