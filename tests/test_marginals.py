@@ -52,3 +52,52 @@ def test_tvd_of_exact_distribution_is_small():
         em = np.zeros_like(ex)
         np.add.at(em, (samples[:, pair[0]], samples[:, pair[1]]), 1.0 / len(samples))
         assert 0.5 * np.abs(ex - em).sum() < 0.01, pair
+
+
+@pytest.fixture
+def marginals_on_cpu(monkeypatch):
+    """piquasso_gb300.marginals with its one device call (the binomial
+    moments of many mode sets) replaced by the oracle's dynamic program."""
+    from oracle import marginals as om
+
+    from piquasso_gb300 import marginals
+
+    def moments_sets(input_photons, U, mode_sets, max_device_bytes=0):
+        return np.stack([om.binomial_moments(input_photons, U, list(s)) for s in mode_sets])
+
+    monkeypatch.setattr(marginals, "binomial_moments_sets", moments_sets)
+    return marginals
+
+
+def test_marginal_host_logic(marginals_on_cpu):
+    """The host side of the GPU marginals: the binomial transform, the
+    postselected probabilities, the conditional marginal sampler and the TVD
+    judge, against the oracle's marginals and brute-force sums."""
+    from oracle import marginals as om
+
+    mg = marginals_on_cpu
+    d = 5
+    U = haar_unitary(d, 12)
+    inp = [1, 0, 2, 0, 1]
+    n = sum(inp)
+    for modes in ([0], [1, 3], [4, 2]):
+        assert np.allclose(mg.marginal(inp, U, modes), om.marginal(inp, U, modes), atol=1e-13)
+    # postselection: Pr(mode 1 has 1 photon and mode 3 has y) from the two-mode marginal
+    joint = mg.marginal(inp, U, [1, 3])
+    post = mg.get_marginal_fock_probabilities(inp, U, [1], [1], [3])
+    assert set(post) == {(a,) for a in range(n)}
+    for (a,), v in post.items():
+        assert abs(v - joint[1, a]) < 1e-14
+    # conditional sampler: its empirical two-mode distribution approaches the exact one
+    S = mg.generate_marginal_samples(inp, U, [0, 2], 4000, seed=3)
+    h = np.zeros((n + 1, n + 1))
+    for a, b in S:
+        h[a, b] += 1.0 / len(S)
+    assert 0.5 * np.abs(h - mg.marginal(inp, U, [0, 2])).sum() < 0.04
+    # the judge on samples drawn from the exact distribution of the pair
+    rng = np.random.default_rng(0)
+    pair = mg.marginal(inp, U, [0, 2])
+    idx = rng.choice(pair.size, size=20000, p=pair.ravel() / pair.sum())
+    full = np.zeros((20000, d), dtype=int)
+    full[:, 0], full[:, 2] = np.unravel_index(idx, pair.shape)
+    assert mg.tvd_two_mode(full, inp, U, [(0, 2)])[0] < 0.02
