@@ -419,12 +419,12 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     // only the device part is serialised); inputs are validated before the
     // device is touched.
     Planner pl(prec, Form::PLAIN, PlanConfig{});
-    pl.pending.reserve(static_cast<size_t>(batch));
     pl.set_matrix(matrix, nr, nc);
-    for (int64_t b = 0; b < batch; ++b) {
+    {
         std::string err;
-        int st = pl.add(rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
-        if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
+        int64_t bad = 0;
+        int st = pl.add_batch(rows, cols, batch, err, &bad);
+        if (st) return fail(st, batch > 1 ? "problem " + std::to_string(bad) + ": " + err : err);
     }
     PlanConfig cfg;
     {
@@ -457,12 +457,12 @@ void laplace_precision_fallback(Planner &pl) {
 // the lock is taken only to read the device's configuration).
 int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int64_t nc, const int32_t *rows,
                  const int32_t *cols, int64_t batch) {
-    pl.pending.reserve(static_cast<size_t>(batch));
     pl.set_matrix(matrix, nr, nc);
-    for (int64_t b = 0; b < batch; ++b) {
+    {
         std::string err;
-        int st = pl.add(rows ? rows + b * nr : nullptr, cols ? cols + b * nc : nullptr, err);
-        if (st) return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
+        int64_t bad = 0;
+        int st = pl.add_batch(rows, cols, batch, err, &bad);
+        if (st) return fail(st, batch > 1 ? "problem " + std::to_string(bad) + ": " + err : err);
     }
     PlanConfig cfg;
     {
@@ -893,12 +893,13 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     h->single = dtype == 1;
     h->n_cols = n_cols;
     h->pl.set_matrix(m, n_rows, n_cols);
-    for (int64_t b = 0; b < batch; ++b) {
+    {
         std::string err;
-        int st = h->pl.add(rows ? rows + b * n_rows : nullptr, cols ? cols + b * n_cols : nullptr, err);
+        int64_t bad = 0;
+        int st = h->pl.add_batch(rows, cols, batch, err, &bad);
         if (st) {
             delete h;
-            return fail(st, batch > 1 ? "problem " + std::to_string(b) + ": " + err : err);
+            return fail(st, batch > 1 ? "problem " + std::to_string(bad) + ": " + err : err);
         }
     }
     int st = C.init();

@@ -16,7 +16,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <thread>
 
 namespace pqg {
 
@@ -32,6 +35,32 @@ double binom_d(int n, int k) {
 }
 
 }  // namespace
+
+int host_threads(int64_t n) {
+    // PQG_HOST_THREADS caps the count (1: plan on the calling thread only)
+    int64_t cap = 8;
+    if (const char *env = std::getenv("PQG_HOST_THREADS")) cap = std::max<int64_t>(1, std::atoll(env));
+    if (n < 2048 || cap == 1) return 1;  // a thread's start costs about what 100 problems do
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int64_t by_size = n / 1024;
+    return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>({cap, by_size, hw ? static_cast<int64_t>(hw) : 1})));
+}
+
+void parallel_ranges(int64_t n, int nt, const std::function<void(int, int64_t, int64_t)> &fn) {
+    if (nt <= 1) {
+        fn(0, 0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(static_cast<size_t>(nt - 1));
+    const int64_t per = (n + nt - 1) / nt;
+    for (int w = 1; w < nt; ++w) {
+        const int64_t lo = std::min<int64_t>(n, w * per), hi = std::min<int64_t>(n, lo + per);
+        pool.emplace_back(fn, w, lo, hi);
+    }
+    fn(0, 0, std::min<int64_t>(n, per));
+    for (auto &t : pool) t.join();
+}
 
 double algorithmic_flops(const PendingProblem &p, Form form) {
     if (p.kind != PQG_KIND_WALK) return 0.0;
@@ -50,10 +79,10 @@ void Planner::set_matrix(const double *a, int64_t nr, int64_t nc) {
     int_nc_ = nc;
 }
 
-int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int64_t row_base,
-                 int64_t n_rows_local) {
+int Planner::make_pending_(PendingProblem &p, const int32_t *rows, const int32_t *cols, std::string &err,
+                           int64_t row_base, int64_t n_rows_local, bool &df_domain) const {
     const int64_t nr = n_rows_local >= 0 ? n_rows_local : int_nr_, nc = int_nc_;
-    PendingProblem p;
+    p = PendingProblem{};
     if (nr < 0 || nc < 0 || (nr > 0 && nc > 0 && a_ == nullptr) || (nr > 0 && !rows) || (nc > 0 && !cols) ||
         row_base < 0 || row_base + nr > int_nr_) {
         err = "invalid matrix or multiplicity buffers";
@@ -97,14 +126,12 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
         if (nr == 0 || nc == 0 || sr == 0) {  // src/permanent.cpp:106-108
             p.kind = PQG_KIND_CONSTANT;
             p.n_out = 1;
-            pending.push_back(p);
             return 0;
         }
     } else {
         if (nr == 0 || nc == 0 || sr == 0 || sc == 0) {  // src/permanent_laplace.cpp:52-57
             p.kind = PQG_KIND_CONSTANT;
             p.n_out = 1;
-            pending.push_back(p);
             return 0;
         }
     }
@@ -118,7 +145,7 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     }
     // the double-float kernel keeps typical terms (>= N^(-N/2) after column
     // scaling) far above the FP32 underflow threshold only for N <= 32
-    if (sr > 32) df_ok_add_ = false;
+    if (sr > 32) df_domain = false;
 
     // columns with nonzero multiplicity (branch-free: a slot is written for
     // every column and kept only when its multiplicity is nonzero)
@@ -197,7 +224,53 @@ int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int
     }
     p.S = S;
     p.scale_exp = static_cast<int>(sr - 1);
+    return 0;
+}
+
+int Planner::add(const int32_t *rows, const int32_t *cols, std::string &err, int64_t row_base,
+                 int64_t n_rows_local) {
+    PendingProblem p;
+    bool dom = true;
+    const int st = make_pending_(p, rows, cols, err, row_base, n_rows_local, dom);
+    if (st) return st;
     pending.push_back(p);
+    if (!dom) df_ok_add_ = false;
+    return 0;
+}
+
+int Planner::add_batch(const int32_t *rows, const int32_t *cols, int64_t batch, std::string &err,
+                       int64_t *err_index) {
+    const size_t base = pending.size();
+    pending.resize(base + static_cast<size_t>(batch));
+    const int nt = host_threads(batch);
+    std::vector<int64_t> bad(static_cast<size_t>(nt), -1);
+    std::vector<int> bad_st(static_cast<size_t>(nt), 0);
+    std::vector<std::string> bad_err(static_cast<size_t>(nt));
+    std::vector<char> dom(static_cast<size_t>(nt), 1);
+    parallel_ranges(batch, nt, [&](int w, int64_t lo, int64_t hi) {
+        for (int64_t b = lo; b < hi; ++b) {
+            bool d = true;
+            const int st = make_pending_(pending[base + static_cast<size_t>(b)], rows ? rows + b * int_nr_ : nullptr,
+                                         cols ? cols + b * int_nc_ : nullptr, bad_err[static_cast<size_t>(w)], 0,
+                                         -1, d);
+            if (!d) dom[static_cast<size_t>(w)] = 0;
+            if (st) {  // the range's first failure; later problems of the range are not needed
+                bad[static_cast<size_t>(w)] = b;
+                bad_st[static_cast<size_t>(w)] = st;
+                return;
+            }
+        }
+    });
+    for (int w = 0; w < nt; ++w) {  // ranges are in order: the first failing range has the lowest index
+        if (bad[static_cast<size_t>(w)] >= 0) {
+            err = bad_err[static_cast<size_t>(w)];
+            if (err_index) *err_index = bad[static_cast<size_t>(w)];
+            pending.resize(base);
+            return bad_st[static_cast<size_t>(w)];
+        }
+    }
+    for (int w = 0; w < nt; ++w)
+        if (!dom[static_cast<size_t>(w)]) df_ok_add_ = false;
     return 0;
 }
 
@@ -382,104 +455,144 @@ void Planner::finish() {
     }
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return key[x] > key[y]; });
 
-    for (size_t ip = 0; ip < np; ++ip) {
-        PendingProblem &p = pending[static_cast<size_t>(order[ip])];
-        PqgProblem &q = probs[ip];
-        std::memset(&q, 0, sizeof(q));
-        q.kind = p.kind;
-        q.index = order[ip];
-        q.n_out = p.n_out;
-        q.out_index = out_of[static_cast<size_t>(order[ip])];
-        q.item_begin = total_items;
-        q.part_begin = total_parts;
-        q.chunk_begin = static_cast<int64_t>(chunks.size());
-        q.delta_begin = total_delta;  // kept monotone for the device's binary search
-        q.off_base64 = q.off_outer64 = q.off_base_df = q.off_outer_df = q.off_D = -1;
-        if (p.kind == PQG_KIND_CONSTANT) {
-            q.cval_re = p.cre;
-            q.cval_im = p.cim;
-            q.P = 1;
-            q.R = 1;
-            item_begin[ip + 1] = total_items;
-            continue;
-        }
-        q.nc = p.nc;
-        q.laplace = laplace ? 1 : 0;
-        max_nc = std::max(max_nc, p.nc);
-        q.scale_exp = p.scale_exp;
-        int cm_max = 1;
-        for (int k = 0; k < p.nc; ++k) {
-            q.cm[k] = static_cast<uint8_t>(p.cm[k]);
-            cm_max = std::max<int>(cm_max, p.cm[k]);
-        }
-        q.cm_max = cm_max;
-        all_ones = all_ones && cm_max == 1;
-        if (df && laplace) {
-            // the double-float Laplace walk folds the whole step weight (inner
-            // times outer) into one FP32 value: its largest, the product over
-            // every digit of C(m, m/2), must be exact in FP32
-            double wmax = 1.0;
-            for (int i = 0; i < p.nd; ++i) wmax *= binom_d(p.m[i], p.m[i] / 2);
-            if (wmax > 16777216.0) df_ok = false;
-        }
-
-        // this problem's steps per lane: the plan's, but never so many that
-        // the problem fills less than one warp
-        const double lane_steps = std::max(1.0, std::min(steps_per_lane, p.S / 32.0));
-        // inner digits: ascending multiplicity, greedily while the inner walk
-        // fits both the lane's steps and the table limit
-        const int nd = p.nd;
-        int order[PQG_MAX_OUTER];
-        for (int i = 0; i < nd; ++i) {  // stable insertion sort (nd <= 60; no allocation)
-            int at = i;
-            while (at > 0 && p.m[order[at - 1]] > p.m[i]) {
-                order[at] = order[at - 1];
-                --at;
+    // Per-problem work in two passes.  The first fills what depends on the
+    // problem alone -- its split into inner and outer digits, the digit
+    // tables, the matrix index rows for the prep kernel, the weight table's
+    // key -- on several host threads for large batches; the second places the
+    // problems in work order (offsets into items, partials, chunks, the arena,
+    // the device-built data and the prefix tables).  The plan is the same
+    // whatever the thread count.
+    constexpr int IDX_STRIDE = 1 + PQG_MAX_OUTER + PQG_MAX_COLS;
+    std::vector<int32_t> idxv(np * IDX_STRIDE);
+    std::vector<int32_t> n_idx(np, 0);
+    std::vector<std::pair<uint64_t, uint64_t>> tkey(np);
+    std::vector<char> lap_too_wide(np, 0);
+    std::vector<double> flops(np, 0.0);
+    parallel_ranges(static_cast<int64_t>(np), host_threads(static_cast<int64_t>(np)), [&](int, int64_t lo,
+                                                                                          int64_t hi) {
+        for (int64_t ipl = lo; ipl < hi; ++ipl) {
+            const size_t ip = static_cast<size_t>(ipl);
+            const PendingProblem &p = pending[static_cast<size_t>(order[ip])];
+            PqgProblem &q = probs[ip];
+            q.kind = p.kind;
+            q.index = order[ip];
+            q.n_out = p.n_out;
+            q.out_index = out_of[static_cast<size_t>(order[ip])];
+            q.off_base64 = q.off_outer64 = q.off_base_df = q.off_outer_df = q.off_D = -1;
+            if (p.kind == PQG_KIND_CONSTANT) {
+                q.cval_re = p.cre;
+                q.cval_im = p.cim;
+                q.P = 1;
+                q.R = 1;
+                continue;
             }
-            order[at] = i;
-        }
-        const double p_target = std::min<double>(static_cast<double>(p_max), lane_steps);
-        int inner[PQG_MAX_INNER], outer[PQG_MAX_OUTER];
-        int K_ = 0, no = 0;
-        double P = 1.0;
-        for (int oi = 0; oi < nd; ++oi) {
-            const int i = order[oi];
-            if (no == 0 && K_ < PQG_MAX_INNER && P * (p.m[i] + 1) <= p_target) {
-                inner[K_++] = i;
-                P *= (p.m[i] + 1);
-            } else {
-                outer[no++] = i;
+            q.nc = p.nc;
+            q.laplace = laplace ? 1 : 0;
+            q.scale_exp = p.scale_exp;
+            int cm_max = 1;
+            for (int k = 0; k < p.nc; ++k) {
+                q.cm[k] = static_cast<uint8_t>(p.cm[k]);
+                cm_max = std::max<int>(cm_max, p.cm[k]);
             }
-        }
-        const size_t K = static_cast<size_t>(K_);
-        q.P = static_cast<int32_t>(P);
-        q.K = static_cast<int32_t>(K);
-        q.n_outer = no;
-        q.Q = static_cast<int64_t>(std::llround(p.S / P));
-        q.R = std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
-        q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / (PQG_ITEM_LANES * group)));
-        // whole warps (whole groups): the outer positions spread evenly over
-        // the nearest count of item groups, so a problem's last item is not
-        // mostly idle lanes (an item is one warp; its lanes all run about R
-        // inner walks)
-        {
-            const int64_t per_group = PQG_ITEM_LANES * group * q.R;
-            const int64_t n_grp = std::max<int64_t>(1, (q.Q + per_group / 2) / per_group);
-            q.R = (q.Q + PQG_ITEM_LANES * group * n_grp - 1) / (PQG_ITEM_LANES * group * n_grp);
-        }
-        for (int o = 0; o < no; ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
-        for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
+            q.cm_max = cm_max;
+            if (df && laplace) {
+                // the double-float Laplace walk folds the whole step weight
+                // (inner times outer) into one FP32 value: its largest, the
+                // product over every digit of C(m, m/2), must be exact in FP32
+                double wmax = 1.0;
+                for (int i = 0; i < p.nd; ++i) wmax *= binom_d(p.m[i], p.m[i] / 2);
+                if (wmax > 16777216.0) lap_too_wide[ip] = 1;
+            }
 
-        // matrix rows and columns for the device prep
-        {
-            int32_t idx[1 + PQG_MAX_OUTER + PQG_MAX_COLS];
+            // this problem's steps per lane: the plan's, but never so many
+            // that the problem fills less than one warp
+            const double lane_steps = std::max(1.0, std::min(steps_per_lane, p.S / 32.0));
+            // inner digits: ascending multiplicity, greedily while the inner
+            // walk fits both the lane's steps and the table limit
+            const int nd = p.nd;
+            int dorder[PQG_MAX_OUTER];
+            for (int i = 0; i < nd; ++i) {  // stable insertion sort (nd <= 60; no allocation)
+                int at = i;
+                while (at > 0 && p.m[dorder[at - 1]] > p.m[i]) {
+                    dorder[at] = dorder[at - 1];
+                    --at;
+                }
+                dorder[at] = i;
+            }
+            const double p_target = std::min<double>(static_cast<double>(p_max), lane_steps);
+            int inner[PQG_MAX_INNER], outer[PQG_MAX_OUTER];
+            int K_ = 0, no = 0;
+            double P = 1.0;
+            for (int oi = 0; oi < nd; ++oi) {
+                const int i = dorder[oi];
+                if (no == 0 && K_ < PQG_MAX_INNER && P * (p.m[i] + 1) <= p_target) {
+                    inner[K_++] = i;
+                    P *= (p.m[i] + 1);
+                } else {
+                    outer[no++] = i;
+                }
+            }
+            const size_t K = static_cast<size_t>(K_);
+            q.P = static_cast<int32_t>(P);
+            q.K = static_cast<int32_t>(K);
+            q.n_outer = no;
+            q.Q = static_cast<int64_t>(std::llround(p.S / P));
+            q.R = std::max<int64_t>(1, static_cast<int64_t>(lane_steps / P));
+            q.R = std::min<int64_t>(q.R, std::max<int64_t>(1, q.Q / (PQG_ITEM_LANES * group)));
+            // whole warps (whole groups): the outer positions spread evenly
+            // over the nearest count of item groups, so a problem's last item
+            // is not mostly idle lanes (an item is one warp; its lanes all run
+            // about R inner walks)
+            {
+                const int64_t per_group = PQG_ITEM_LANES * group * q.R;
+                const int64_t n_grp = std::max<int64_t>(1, (q.Q + per_group / 2) / per_group);
+                q.R = (q.Q + PQG_ITEM_LANES * group * n_grp - 1) / (PQG_ITEM_LANES * group * n_grp);
+            }
+            for (int o = 0; o < no; ++o) q.outer_m[o] = static_cast<uint8_t>(p.m[outer[o]]);
+            for (size_t k = 0; k < K; ++k) q.inner_m[k] = static_cast<uint8_t>(p.m[inner[k]]);
+            const int64_t lanes = (q.Q + q.R - 1) / q.R;
+            q.n_items = (lanes + PQG_ITEM_LANES - 1) / PQG_ITEM_LANES;
+            q.n_items = (q.n_items + group - 1) / group * group;  // trailing items of a group may be empty
+
+            // matrix rows and columns for the device prep
+            int32_t *idx = idxv.data() + ip * IDX_STRIDE;
             int c = 0;
             idx[c++] = p.row0;
             for (int o = 0; o < no; ++o) idx[c++] = p.row[outer[o]];
             for (size_t k = 0; k < K; ++k) idx[c++] = p.row[inner[k]];
             for (int k = 0; k < p.nc; ++k) idx[c++] = p.col[k];
-            q.off_idx = push_bytes_(idx, static_cast<size_t>(c) * sizeof(int32_t));
+            n_idx[ip] = c;
+            // the weight table depends only on the inner multiplicities: K <= 16
+            // of them, each below 256, packed into a 128-bit key
+            std::pair<uint64_t, uint64_t> key{static_cast<uint64_t>(K), 0};
+            for (size_t k = 0; k < K; ++k) {
+                const uint64_t v = p.m[inner[k]];
+                if (k < 7)
+                    key.first |= v << (8 * (k + 1));
+                else
+                    key.second |= v << (8 * (k - 7));
+            }
+            tkey[ip] = key;
+            flops[ip] = algorithmic_flops(p, form_);
         }
+    });
+
+    for (size_t ip = 0; ip < np; ++ip) {
+        const PendingProblem &p = pending[static_cast<size_t>(order[ip])];
+        PqgProblem &q = probs[ip];
+        q.item_begin = total_items;
+        q.part_begin = total_parts;
+        q.chunk_begin = static_cast<int64_t>(chunks.size());
+        q.delta_begin = total_delta;  // kept monotone for the device's binary search
+        if (p.kind == PQG_KIND_CONSTANT) {
+            item_begin[ip + 1] = total_items;
+            continue;
+        }
+        max_nc = std::max(max_nc, p.nc);
+        all_ones = all_ones && q.cm_max == 1;
+        if (lap_too_wide[ip]) df_ok = false;
+        const int no = q.n_outer;
+        q.off_idx = push_bytes_(idxv.data() + ip * IDX_STRIDE, static_cast<size_t>(n_idx[ip]) * sizeof(int32_t));
         // device-built seeds and step rows in the walk's precision
         if (c128) {
             q.off_base64 = pdata(16 * p.nc);
@@ -489,25 +602,14 @@ void Planner::finish() {
             if (no) q.off_outer_df = pdata(16 * int64_t(no) * p.nc);
         }
         if (no) q.off_D = pdata(d_elem * 2 * int64_t(no) * p.nc);
-        q.delta_begin = total_delta;
         total_delta += static_cast<int64_t>(q.P) * p.nc;
 
-        // the weight table depends only on the inner multiplicities: K <= 16
-        // of them, each below 256, packed into a 128-bit key
-        std::pair<uint64_t, uint64_t> key{static_cast<uint64_t>(K), 0};
-        for (size_t k = 0; k < K; ++k) {
-            const uint64_t v = p.m[inner[k]];
-            if (k < 7)
-                key.first |= v << (8 * (k + 1));
-            else
-                key.second |= v << (8 * (k - 7));
-        }
-        auto it = table_cache_.find(key);
+        auto it = table_cache_.find(tkey[ip]);
         if (it != table_cache_.end()) {
             q.off_tab = it->second;
         } else {
-            std::vector<int> mm(K);
-            for (size_t k = 0; k < K; ++k) mm[k] = p.m[inner[k]];
+            std::vector<int> mm(static_cast<size_t>(q.K));
+            for (int k = 0; k < q.K; ++k) mm[static_cast<size_t>(k)] = q.inner_m[k];
             const std::vector<double> w = build_weights(mm, q.P);
             std::vector<PqgStep> tab(q.P);
             for (int64_t t = 0; t < q.P; ++t) {
@@ -517,12 +619,9 @@ void Planner::finish() {
                 if (df && std::fabs(w[t]) > 16777216.0) df_ok = false;  // not exact in FP32
             }
             q.off_tab = push_bytes_(tab.data(), tab.size() * sizeof(PqgStep));
-            table_cache_[key] = q.off_tab;
+            table_cache_[tkey[ip]] = q.off_tab;
         }
 
-        const int64_t lanes = (q.Q + q.R - 1) / q.R;
-        q.n_items = (lanes + PQG_ITEM_LANES - 1) / PQG_ITEM_LANES;
-        q.n_items = (q.n_items + group - 1) / group * group;  // trailing items of a group may be empty
         total_items += q.n_items;
         total_parts += q.n_items * q.n_out;
         item_begin[ip + 1] = total_items;
@@ -537,7 +636,7 @@ void Planner::finish() {
         }
         q.n_chunks = static_cast<int64_t>(chunks.size()) - q.chunk_begin;
         total_steps += p.S;
-        total_flops += algorithmic_flops(p, form_);
+        total_flops += flops[ip];
     }
     item_begin[np] = total_items;
     // the device data follows the uploaded arena: rebase its offsets (an

@@ -7,6 +7,7 @@
 // plan carries the matrix once, and a device kernel (prep.cuh) builds every
 // problem's seeds, step rows and prefix tables in device memory.
 #pragma once
+#include <functional>
 #include <map>
 #include <utility>
 #include <string>
@@ -70,6 +71,12 @@ class Planner {
     int add(const int32_t *rows, const int32_t *cols, std::string &err, int64_t row_base = 0,
             int64_t n_rows_local = -1);
 
+    // Adds `batch` problems (rows: batch x n_rows, cols: batch x n_cols), on
+    // several host threads for large batches; the same problems as `batch`
+    // calls of add().  On failure *err_index receives the first failing
+    // problem and nothing is added.
+    int add_batch(const int32_t *rows, const int32_t *cols, int64_t batch, std::string &err, int64_t *err_index);
+
     // Fixes every problem's split and lays out the arena and the per-problem
     // device data.
     void finish();
@@ -111,6 +118,8 @@ class Planner {
     bool df_ok_add_ = true;
     const double *a_ = nullptr;
     int64_t int_nr_ = 0, int_nc_ = 0;
+    int make_pending_(PendingProblem &p, const int32_t *rows, const int32_t *cols, std::string &err, int64_t row_base,
+                      int64_t n_rows_local, bool &df_domain) const;
     int64_t align_(size_t a);
     int64_t push_bytes_(const void *p, size_t n);
 };
@@ -119,5 +128,10 @@ class Planner {
 // permanent (c column-sum updates of 4 flops, one complex multiply of 6 flops
 // per factor, 4 flops for the weighted accumulation).
 double algorithmic_flops(const PendingProblem &p, Form form);
+
+// Host threads the planner uses for n problems (1 below a few thousand), and
+// a parallel loop over contiguous ranges [lo, hi) of 0..n (worker w).
+int host_threads(int64_t n);
+void parallel_ranges(int64_t n, int nt, const std::function<void(int, int64_t, int64_t)> &fn);
 
 }  // namespace pqg

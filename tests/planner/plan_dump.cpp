@@ -1,10 +1,14 @@
 // Test driver for the host planner (compiled with g++ by tests/test_planner_cpu.py;
 // no CUDA): reads problems from stdin, plans them, prints the plan as JSON.
 //
+// The problems go through Planner::add_batch, which plans on several host
+// threads from 2048 problems on (PQG_HOST_THREADS caps the count).
+//
 // stdin: prec form nr nc batch, then the matrix is all zeros except entry
 // (0,0) = 1 (the planner copies it and never reads values), then batch lines
 // of nr row multiplicities followed by nc column multiplicities.
 // prec: 0 = C128, 1 = C64, 2 = C128DF; form: 0 = plain, 1 = Laplace.
+#include <cstdint>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -30,19 +34,25 @@ int main() {
     if (form == Form::LAPLACE) cfg.p_max = 512;
     Planner pl(prec, form, cfg);
     pl.set_matrix(a.data(), nr, nc);
-    for (long long b = 0; b < batch; ++b) {
-        std::string err;
-        const int st = pl.add(rows.data() + b * nr, cols.data() + b * nc, err);
-        if (st) {
-            printf("{\"error\": %d, \"problem\": %lld, \"message\": \"%s\"}\n", st, b, err.c_str());
-            return 0;
-        }
+    std::string err;
+    int64_t bad = -1;
+    const int st = pl.add_batch(rows.data(), cols.data(), batch, err, &bad);
+    if (st) {
+        printf("{\"error\": %d, \"problem\": %lld, \"message\": \"%s\"}\n", st, static_cast<long long>(bad),
+               err.c_str());
+        return 0;
     }
     pl.finish();
+    uint64_t h = 1469598103934665603ull;  // FNV-1a of the arena: tables, row/column indices, matrix
+    for (unsigned char byte : pl.arena) h = (h ^ byte) * 1099511628211ull;
+    uint64_t hp = 1469598103934665603ull;  // and of the problem records, byte for byte
+    const unsigned char *pb = reinterpret_cast<const unsigned char *>(pl.probs.data());
+    for (size_t i = 0; i < pl.probs.size() * sizeof(PqgProblem); ++i) hp = (hp ^ pb[i]) * 1099511628211ull;
     printf("{\"total_items\": %lld, \"total_outputs\": %lld, \"item_group\": %d, \"df_ok\": %d, \"all_ones\": %d, "
-           "\"max_nc\": %d, \"out_of\": [",
+           "\"max_nc\": %d, \"arena_bytes\": %lld, \"arena_hash\": \"%016llx\", \"probs_hash\": \"%016llx\", \"out_of\": [",
            static_cast<long long>(pl.total_items), static_cast<long long>(pl.total_outputs), pl.item_group,
-           pl.df_ok ? 1 : 0, pl.all_ones ? 1 : 0, pl.max_nc);
+           pl.df_ok ? 1 : 0, pl.all_ones ? 1 : 0, pl.max_nc, static_cast<long long>(pl.arena.size()),
+           static_cast<unsigned long long>(h), static_cast<unsigned long long>(hp));
     for (size_t b = 0; b < pl.out_of.size(); ++b) printf("%s%lld", b ? ", " : "", static_cast<long long>(pl.out_of[b]));
     printf("], \"item_begin\": [");
     for (size_t i = 0; i < pl.item_begin.size(); ++i)

@@ -142,3 +142,36 @@ def test_input_errors(planner):
     assert planner(C128, 0, [[1, 1, 1]], [[1, 1, 0]])["error"] == 1  # sum mismatch
     many = planner(C128, 0, [[1] * 33], [[1] * 33])
     assert many["error"] == 3  # more than 32 distinct columns
+
+
+@pytest.mark.parametrize("prec,form", [(C64, 0), (DF, 1), (C128, 1)])
+def test_threaded_planning_is_deterministic(planner, monkeypatch, prec, form):
+    """From 2048 problems on, add_batch and finish plan on several host
+    threads; the plan (problem records, arena bytes, layout) is the same as
+    on one thread."""
+    rng = np.random.default_rng(40 + prec + form)
+    d, n = 40, 12
+    R, C = [], []
+    for b in range(2600):
+        R.append(np.bincount(rng.integers(0, d, n), minlength=d))
+        c = np.zeros(d, dtype=int)
+        c[rng.permutation(d)[:n]] = 1
+        C.append(c if b % 3 else np.bincount(rng.integers(0, d, n), minlength=d))
+    monkeypatch.setenv("PQG_HOST_THREADS", "1")
+    one = planner(prec, form, R, C)
+    monkeypatch.setenv("PQG_HOST_THREADS", "4")
+    four = planner(prec, form, R, C)
+    assert "error" not in one, one
+    _check_layout(four, len(R))
+    assert one == four
+
+
+def test_threaded_planning_reports_the_first_bad_problem(planner, monkeypatch):
+    d = 6
+    R = [[1, 1, 0, 0, 0, 0]] * 3000
+    C = [[1, 1, 0, 0, 0, 0]] * 3000
+    R[2100] = [1, 1, 1, 0, 0, 0]  # sum mismatch
+    R[2900] = [1, -1, 2, 0, 0, 0]  # negative multiplicity, later
+    monkeypatch.setenv("PQG_HOST_THREADS", "4")
+    bad = planner(C128, 0, R, C)
+    assert bad["error"] == 1 and bad["problem"] == 2100
