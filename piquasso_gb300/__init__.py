@@ -5,7 +5,8 @@ Public API (drop-in for ``piquasso._math.permanent``):
     permanent_laplace(matrix, rows, cols)
 plus the additive ``permanent_batch``, ``permanent_grad`` and the connector in
 ``piquasso_gb300.connector``; the samplers (exact, lossy, partially
-distinguishable) in ``piquasso_gb300.sampling``, batched detection
+distinguishable, postselected through ``piquasso_gb300.postselect``) in
+``piquasso_gb300.sampling``, batched detection
 probabilities and LXEB scoring in ``piquasso_gb300.probabilities``, and the
 learned-proposal Metropolis sampler in ``piquasso_gb300.metropolis``.
 """
@@ -23,6 +24,7 @@ from .permanent import (  # noqa: F401
     sampler_step_batch,
 )
 from .plan import PermanentPlan  # noqa: F401
+from .postselect import InvalidSimulation  # noqa: F401
 from ._lib import EngineUnavailable, get_tuning, kernel_launches, last_timing, set_tuning  # noqa: F401
 
 __version__ = "0.1.0"

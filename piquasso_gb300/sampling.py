@@ -199,15 +199,31 @@ def generate_lossy_samples(input_state, shots, matrix, seed, batch_size=4096, ba
     return [s[:d] for s in generate_samples(state, shots, E, seed, batch_size=batch_size)]
 
 
-def sample(input_state, shots, interferometer, seed, particle_overlap=None, batched=False, batch_size=4096):
+def sample(input_state, shots, interferometer, seed, particle_overlap=None, batched=False, batch_size=4096,
+           postselect=None):
     """The reference's dispatch (passive/simulation_steps.py:315-369): from the
     singular values of the interferometer, lossless (all 1), uniform loss
     (all equal: transmission s_0^2) or non-uniform loss (SVD dilation), with
     optional uniform particle overlap.  Non-uniform loss with partially
     distinguishable photons goes through loop hafnians in the reference and is
-    not on this engine's path."""
+    not on this engine's path.
+
+    ``postselect``: (modes, photon counts[, maximum trials per shot]), the
+    reference's ``PostSelectPhotons`` before the measurement.  Samples then
+    come from ``piquasso_gb300.postselect``: the reference's per-seed sequence,
+    with the shots' photon steps batched, whatever ``batched`` says."""
     M = np.asarray(interferometer)
     sv = np.linalg.svd(M.astype(np.complex128), compute_uv=False)
+    if postselect is not None:
+        from . import postselect as ps
+
+        if np.all(np.isclose(sv, sv[0])):
+            T = None if np.isclose(sv[0], 1.0) else float(sv[0] ** 2)
+            return ps.generate_samples(input_state, shots, M, seed, postselect, transmission=T,
+                                       particle_overlap=particle_overlap)
+        if particle_overlap is not None:
+            raise NotImplementedError("non-uniform loss with partially distinguishable photons (loop hafnians)")
+        return ps.generate_lossy_samples(input_state, shots, M, seed, postselect)
     if np.all(np.isclose(sv, sv[0])):
         T = None if np.isclose(sv[0], 1.0) else float(sv[0] ** 2)
         if batched:

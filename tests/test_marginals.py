@@ -94,7 +94,7 @@ def test_marginal_host_logic(marginals_on_cpu):
     for a, b in S:
         h[a, b] += 1.0 / len(S)
     assert 0.5 * np.abs(h - mg.marginal(inp, U, [0, 2])).sum() < 0.04
-    # the judge on samples drawn from the exact distribution of the pair
+    # the TVD check on samples drawn from the exact distribution of the pair
     rng = np.random.default_rng(0)
     pair = mg.marginal(inp, U, [0, 2])
     idx = rng.choice(pair.size, size=20000, p=pair.ravel() / pair.sum())
