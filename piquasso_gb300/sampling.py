@@ -236,6 +236,77 @@ def sample(input_state, shots, interferometer, seed, particle_overlap=None, batc
     return generate_lossy_samples(input_state, shots, M, seed, batch_size=batch_size, batched=batched)
 
 
+def is_direct_marginal_sampling_cheaper(k, d, n, shots):
+    """The reference's rule for measuring k of d modes (sampling.py:860-887):
+    direct marginal sampling when the marginal algorithm's coefficient count
+    sum_{m<=n} C(m+k-1, k-1)^2 is small enough for the number of shots.  Kept
+    as it is: the two methods draw different samples for a seed."""
+    from math import comb
+
+    if k == d:
+        return False
+    coeffs = sum(comb(m + k - 1, k - 1) ** 2 for m in range(n + 1))
+    if coeffs <= 100_000:
+        return True
+    if coeffs <= 500_000:
+        return shots >= 1_000
+    if coeffs <= 4_000_000:
+        return shots >= 10_000
+    return False
+
+
+def map_to_original_modes(modes, postselected_modes):
+    """Active-mode indices (postselected modes removed) to the original
+    numbering (sampling.py:787-793)."""
+    m = np.asarray(modes, dtype=int).copy()
+    for p in sorted(postselected_modes):
+        m[m >= p] += 1
+    return tuple(int(x) for x in m)
+
+
+def measure(input_state, shots, interferometer, seed, modes=None, postselect=None, particle_overlap=None,
+            batched=False):
+    """``ParticleNumberMeasurement`` with shots, after an optional
+    ``PostSelectPhotons`` (passive/simulation_steps.py:239-399): returns
+    {outcome on ``modes``: count} in order of first occurrence.  ``modes``
+    are numbered among the modes that survive the postselection (all of them
+    by default).  A measurement of some of the modes with ideal or uniformly
+    lossy optics samples the marginal directly when
+    ``is_direct_marginal_sampling_cheaper`` says so (on the GPU marginals,
+    ``marginals.generate_marginal_samples``; the reference takes this branch
+    whatever the particle overlap); otherwise every mode is sampled
+    (``sample``) and the outcomes are projected onto ``modes``."""
+    from . import marginals
+
+    inp = np.asarray(input_state).astype(int)
+    d = len(inp)
+    post_modes = tuple(int(m) for m in postselect[0]) if postselect else ()
+    post_counts = tuple(int(c) for c in postselect[1]) if postselect else ()
+    active = d - len(post_modes)
+    modes = tuple(range(active)) if modes is None else tuple(int(m) for m in modes)
+    marginal_only = set(modes) != set(range(active))
+    M = np.asarray(interferometer)
+    sv = np.linalg.svd(M.astype(np.complex128), compute_uv=False)
+    n = int(inp.sum())
+    if (marginal_only and np.all(np.isclose(sv, sv[0]))
+            and is_direct_marginal_sampling_cheaper(len(modes) + len(post_modes), d, n, shots)):
+        samples = marginals.generate_marginal_samples(inp, M, map_to_original_modes(modes, post_modes), shots, seed,
+                                                      postselected_modes=post_modes,
+                                                      postselected_photons=post_counts)
+        return get_counts(samples)
+    samples = sample(inp, shots, M, seed, particle_overlap=particle_overlap, batched=batched, postselect=postselect)
+    if batched and postselect is None:
+        samples = [tuple(int(x) for x in row) for row in samples]
+    counts = get_counts(samples)
+    if not marginal_only:
+        return counts
+    projected = {}
+    for outcome, mult in counts.items():
+        key = tuple(outcome[m] for m in modes)
+        projected[key] = projected.get(key, 0) + mult
+    return projected
+
+
 def get_counts(samples):
     counts = {}
     for s in samples:
