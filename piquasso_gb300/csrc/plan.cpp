@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <functional>
 #include <thread>
 
@@ -51,15 +52,27 @@ void parallel_ranges(int64_t n, int nt, const std::function<void(int, int64_t, i
         fn(0, 0, n);
         return;
     }
+    // A worker's exception (std::bad_alloc) is rethrown on the calling
+    // thread after every worker has joined, as the one-thread path would.
+    std::vector<std::exception_ptr> errs(static_cast<size_t>(nt));
+    auto run = [&](int w, int64_t lo, int64_t hi) {
+        try {
+            fn(w, lo, hi);
+        } catch (...) {
+            errs[static_cast<size_t>(w)] = std::current_exception();
+        }
+    };
     std::vector<std::thread> pool;
     pool.reserve(static_cast<size_t>(nt - 1));
     const int64_t per = (n + nt - 1) / nt;
     for (int w = 1; w < nt; ++w) {
         const int64_t lo = std::min<int64_t>(n, w * per), hi = std::min<int64_t>(n, lo + per);
-        pool.emplace_back(fn, w, lo, hi);
+        pool.emplace_back(run, w, lo, hi);
     }
-    fn(0, 0, std::min<int64_t>(n, per));
+    run(0, 0, std::min<int64_t>(n, per));
     for (auto &t : pool) t.join();
+    for (auto &e : errs)
+        if (e) std::rethrow_exception(e);
 }
 
 double algorithmic_flops(const PendingProblem &p, Form form) {
