@@ -295,3 +295,55 @@ def generate_lossy_samples(input_state, shots, matrix, seed, postselect):
         E = E.astype(np.complex64)
     state = np.concatenate([inp, np.zeros(d, dtype=int)])
     return [s[:d] for s in generate_samples(state, shots, E, seed, postselect)]
+
+
+def _round_seed(seed, r):
+    """An independent 63-bit seed for round r of a rejection loop."""
+    return int(np.random.SeedSequence([int(seed), int(r)]).generate_state(1, dtype=np.uint64)[0] >> np.uint64(1))
+
+
+def generate_samples_batched(input_state, shots, interferometer, seed, postselect, transmission=None,
+                             particle_overlap=None, lossy=False, batch_size=2048):
+    """Postselected samples at throughput: rounds of unconditioned samples
+    from ``sampling.generate_samples_batched`` (one fused Laplace + pmf + draw
+    launch per photon step for all shots of a batch), keeping the samples
+    whose postselected modes hold exactly the requested counts.  Those follow
+    the conditional distribution that the reference's retry loop samples, but
+    not its per-seed sequence.  ``lossy``: non-uniform loss, sampled on the
+    2d-mode dilation and trimmed as the reference trims it (postselected
+    modes deleted, then the first d entries).  Raises ``InvalidSimulation``
+    after (maximum trials) x shots samples without enough matches.  Returns
+    an int array (shots, remaining modes)."""
+    from . import sampling
+
+    modes, counts = tuple(int(m) for m in postselect[0]), np.array([int(c) for c in postselect[1]], dtype=int)
+    max_trials = int(postselect[2]) if len(postselect) > 2 else DEFAULT_MAX_TRIALS
+    M = np.asarray(interferometer)
+    inp = np.asarray(input_state).astype(int)
+    d = len(inp)
+    if lossy:
+        E = expanded_interferometer(M)
+        if M.dtype == np.complex64:
+            E = E.astype(np.complex64)
+        M, inp = E, np.concatenate([inp, np.zeros(d, dtype=int)])
+    D = len(inp)
+    if len(modes) != len(counts) or len(set(modes)) != len(modes) or any(m < 0 or m >= D for m in modes) \
+            or np.any(counts < 0):
+        raise ValueError("postselect needs one nonnegative photon count per distinct mode in 0..d-1")
+    kept, have, drawn, r = [], 0, 0, 0
+    while have < shots:
+        if drawn >= max_trials * shots:
+            raise _trial_limit(max_trials)
+        rate = max(have / drawn, 1.0 / max_trials) if drawn else 1.0
+        k = int(min(max(batch_size, np.ceil(1.2 * (shots - have) / rate)), max_trials * shots - drawn, 1 << 20))
+        S = sampling.generate_samples_batched(inp, k, M, _round_seed(seed, r), batch_size=batch_size,
+                                              transmission=transmission, particle_overlap=particle_overlap)
+        drawn += k
+        r += 1
+        ok = np.all(S[:, list(modes)] == counts, axis=1)
+        out = np.delete(S[ok], list(modes), axis=1)
+        kept.append(out[:, :d] if lossy else out)
+        have += len(out)
+    if not kept:
+        return np.zeros((0, min(d, D - len(modes)) if lossy else D - len(modes)), dtype=int)
+    return np.concatenate(kept)[:shots]

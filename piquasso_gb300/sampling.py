@@ -210,8 +210,9 @@ def sample(input_state, shots, interferometer, seed, particle_overlap=None, batc
 
     ``postselect``: (modes, photon counts[, maximum trials per shot]), the
     reference's ``PostSelectPhotons`` before the measurement.  Samples then
-    come from ``piquasso_gb300.postselect``: the reference's per-seed sequence,
-    with the shots' photon steps batched, whatever ``batched`` says."""
+    come from ``piquasso_gb300.postselect``: the reference's per-seed sequence
+    with the shots' photon steps batched, or with ``batched`` rejection
+    rounds of the throughput sampler (an int array)."""
     M = np.asarray(interferometer)
     sv = np.linalg.svd(M.astype(np.complex128), compute_uv=False)
     if postselect is not None:
@@ -219,10 +220,16 @@ def sample(input_state, shots, interferometer, seed, particle_overlap=None, batc
 
         if np.all(np.isclose(sv, sv[0])):
             T = None if np.isclose(sv[0], 1.0) else float(sv[0] ** 2)
+            if batched:
+                return ps.generate_samples_batched(input_state, shots, M, seed, postselect, transmission=T,
+                                                   particle_overlap=particle_overlap, batch_size=batch_size)
             return ps.generate_samples(input_state, shots, M, seed, postselect, transmission=T,
                                        particle_overlap=particle_overlap)
         if particle_overlap is not None:
             raise NotImplementedError("non-uniform loss with partially distinguishable photons (loop hafnians)")
+        if batched:
+            return ps.generate_samples_batched(input_state, shots, M, seed, postselect, lossy=True,
+                                               batch_size=batch_size)
         return ps.generate_lossy_samples(input_state, shots, M, seed, postselect)
     if np.all(np.isclose(sv, sv[0])):
         T = None if np.isclose(sv[0], 1.0) else float(sv[0] ** 2)
@@ -295,7 +302,7 @@ def measure(input_state, shots, interferometer, seed, modes=None, postselect=Non
                                                       postselected_photons=post_counts)
         return get_counts(samples)
     samples = sample(inp, shots, M, seed, particle_overlap=particle_overlap, batched=batched, postselect=postselect)
-    if batched and postselect is None:
+    if batched:
         samples = [tuple(int(x) for x in row) for row in samples]
     counts = get_counts(samples)
     if not marginal_only:

@@ -147,3 +147,43 @@ def test_trial_limit_on_gpu():
         sampling.sample(np.array(t["input"]), 1, _matrix(t["matrix"]), 0,
                         postselect=(t["modes"], t["photons"], t["max_trials"]))
     assert str(e.value) == t["message"]
+
+
+@pytest.fixture
+def batched_on_cpu(monkeypatch):
+    from piquasso_gb300 import sampling
+    from test_sampling_host_cpu import _numpy_step
+
+    monkeypatch.setattr(sampling, "sampler_step_batch", _numpy_step)
+    return sampling
+
+
+def test_batched_rejection_distribution(batched_on_cpu):
+    U = haar_unitary(4, 21)
+    inp = [1, 1, 1, 0]
+    modes, counts = (1,), (1,)
+    exact = _conditional(U, inp, modes, counts)
+    S = batched_on_cpu.sample(np.array(inp), 2500, U, 99, postselect=(modes, counts), batched=True)
+    assert S.shape == (2500, 3) and np.all(S.sum(axis=1) == 2)
+    emp = {}
+    for s in map(tuple, S):
+        emp[s] = emp.get(s, 0) + 1.0 / len(S)
+    tvd = 0.5 * sum(abs(emp.get(k, 0.0) - exact.get(k, 0.0)) for k in set(emp) | set(exact))
+    assert tvd < 0.05
+
+
+def test_batched_rejection_lossy_trim_and_limits(batched_on_cpu):
+    U = haar_unitary(5, 32) @ np.diag([0.9, 0.8, 0.95, 0.7, 0.85]) @ haar_unitary(5, 33)
+    inp = np.array([1, 1, 1, 0, 0])
+    S = batched_on_cpu.sample(inp, 200, U, 4, postselect=((2,), (1,)), batched=True)
+    assert S.shape == (200, 5)  # postselected mode deleted from the 10 dilated modes, first 5 kept
+    assert np.all(S[:, :4].sum(axis=1) <= 2)
+    a = batched_on_cpu.sample(inp, 50, U, 6, postselect=((2,), (1,)), batched=True)
+    b = batched_on_cpu.sample(inp, 50, U, 6, postselect=((2,), (1,)), batched=True)
+    assert np.array_equal(a, b)
+    from piquasso_gb300 import postselect
+
+    with pytest.raises(postselect.InvalidSimulation):
+        batched_on_cpu.sample(np.array([2, 0, 2, 0]), 3, haar_unitary(4, 16), 0, postselect=((0,), (5,), 4),
+                              batched=True)
+    assert batched_on_cpu.sample(inp, 0, haar_unitary(5, 2), 1, postselect=((0,), (1,)), batched=True).shape == (0, 4)
