@@ -187,3 +187,18 @@ def test_batched_rejection_lossy_trim_and_limits(batched_on_cpu):
         batched_on_cpu.sample(np.array([2, 0, 2, 0]), 3, haar_unitary(4, 16), 0, postselect=((0,), (5,), 4),
                               batched=True)
     assert batched_on_cpu.sample(inp, 0, haar_unitary(5, 2), 1, postselect=((0,), (1,)), batched=True).shape == (0, 4)
+
+
+@pytest.mark.gpu
+def test_batched_rejection_on_gpu():
+    from piquasso_gb300 import sampling
+
+    U = haar_unitary(4, 21)
+    inp = [1, 1, 1, 0]
+    exact = _conditional(U, inp, (1,), (1,))
+    S = sampling.sample(np.array(inp), 4000, U, 99, postselect=((1,), (1,)), batched=True)
+    assert S.shape == (4000, 3) and np.all(S.sum(axis=1) == 2)
+    emp = {}
+    for s in map(tuple, S):
+        emp[s] = emp.get(s, 0) + 1.0 / len(S)
+    assert 0.5 * sum(abs(emp.get(k, 0.0) - exact.get(k, 0.0)) for k in set(emp) | set(exact)) < 0.05
