@@ -683,7 +683,8 @@ int time_fma(Context &C, double target_ms, double *tflops) {
 // and a CUDA graph of its device pipeline, so that repeated executions cost
 // one graph launch (no planning, no copies).
 struct PlanHandle {
-    Planner pl{Precision::C128, Form::PLAIN, PlanConfig{}};
+    PlanHandle(Precision prec, Form form, const PlanConfig &cfg) : pl(prec, form, cfg) {}
+    Planner pl;
     PlanLayout L;
     DeviceBuffers B;
     cudaStream_t stream = nullptr;
@@ -888,8 +889,7 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     std::lock_guard<std::mutex> lock(C.mu);
     const Form fm = form == 1 ? Form::LAPLACE : Form::PLAIN;
     const Precision prec = dtype == 1 ? Precision::C64 : c128_precision(mode);
-    PlanHandle *h = new PlanHandle();
-    h->pl = Planner(prec, fm, C.cfg);
+    PlanHandle *h = new PlanHandle(prec, fm, C.cfg);
     h->single = dtype == 1;
     h->n_cols = n_cols;
     h->pl.set_matrix(m, n_rows, n_cols);

@@ -86,6 +86,55 @@ double algorithmic_flops(const PendingProblem &p, Form form) {
     return p.S * (4.0 * nc + 12.0 * sum_cm + 6.0 * nc + 4.0 * p.n_out);
 }
 
+namespace {
+
+// One pool per host thread: the buffers of the last planner destroyed on the
+// thread (up to a cap), handed to the next planner created on it.  A planner
+// created while the pool is empty (another planner on the thread holds its
+// buffers) allocates as usual.
+struct PlannerPool {
+    std::vector<PendingProblem> pending;
+    std::vector<PqgProblem> probs;
+    std::vector<unsigned char> arena;
+    std::vector<int32_t> idx_rows;
+};
+thread_local PlannerPool t_pool;
+
+constexpr size_t kPoolCapBytes = size_t(64) << 20;
+
+template <typename T>
+size_t capacity_bytes(const std::vector<T> &v) {
+    return v.capacity() * sizeof(T);
+}
+
+}  // namespace
+
+Planner::Planner(Precision prec, Form form, const PlanConfig &cfg) : prec_(prec), form_(form), cfg_(cfg) {
+    PlannerPool &P = t_pool;
+    pending.swap(P.pending);
+    probs.swap(P.probs);
+    arena.swap(P.arena);
+    idx_rows_.swap(P.idx_rows);
+    pending.clear();
+    probs.clear();
+    arena.clear();
+    idx_rows_.clear();
+}
+
+Planner::~Planner() {
+    PlannerPool &P = t_pool;  // the destroying thread's pool (a plan handle may die on another thread)
+    const size_t mine = capacity_bytes(pending) + capacity_bytes(probs) + capacity_bytes(arena) +
+                        capacity_bytes(idx_rows_);
+    const size_t pooled = capacity_bytes(P.pending) + capacity_bytes(P.probs) + capacity_bytes(P.arena) +
+                          capacity_bytes(P.idx_rows);
+    if (mine <= kPoolCapBytes && mine > pooled) {
+        P.pending.swap(pending);
+        P.probs.swap(probs);
+        P.arena.swap(arena);
+        P.idx_rows.swap(idx_rows_);
+    }
+}
+
 void Planner::set_matrix(const double *a, int64_t nr, int64_t nc) {
     a_ = a;
     int_nr_ = nr;
@@ -476,7 +525,8 @@ void Planner::finish() {
     // the device-built data and the prefix tables).  The plan is the same
     // whatever the thread count.
     constexpr int IDX_STRIDE = 1 + PQG_MAX_OUTER + PQG_MAX_COLS;
-    std::vector<int32_t> idxv(np * IDX_STRIDE);
+    std::vector<int32_t> &idxv = idx_rows_;
+    idxv.resize(np * IDX_STRIDE);  // reused capacity: every row's first n_idx entries are written below
     std::vector<int32_t> n_idx(np, 0);
     std::vector<std::pair<uint64_t, uint64_t>> tkey(np);
     std::vector<char> lap_too_wide(np, 0);

@@ -9,7 +9,9 @@
 // of nr row multiplicities followed by nc column multiplicities.
 // prec: 0 = C128, 1 = C64, 2 = C128DF; form: 0 = plain, 1 = Laplace.
 #include <cstdint>
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -32,6 +34,20 @@ int main() {
     }
     PlanConfig cfg;
     if (form == Form::LAPLACE) cfg.p_max = 512;
+    if (std::getenv("PLAN_DUMP_WARM")) {
+        // plan the problems in reverse order first and drop that plan: the
+        // plan printed below then reuses its pooled (dirty) buffers
+        std::vector<int32_t> rr(rows.size()), cr(cols.size());
+        for (long long b = 0; b < batch; ++b) {
+            std::copy(rows.begin() + b * nr, rows.begin() + (b + 1) * nr, rr.begin() + (batch - 1 - b) * nr);
+            std::copy(cols.begin() + b * nc, cols.begin() + (b + 1) * nc, cr.begin() + (batch - 1 - b) * nc);
+        }
+        Planner warm(prec, form, cfg);
+        warm.set_matrix(a.data(), nr, nc);
+        std::string werr;
+        int64_t wbad = -1;
+        if (warm.add_batch(rr.data(), cr.data(), batch, werr, &wbad) == 0) warm.finish();
+    }
     Planner pl(prec, form, cfg);
     pl.set_matrix(a.data(), nr, nc);
     std::string err;

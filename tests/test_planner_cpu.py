@@ -166,6 +166,22 @@ def test_threaded_planning_is_deterministic(planner, monkeypatch, prec, form):
     assert one == four
 
 
+@pytest.mark.parametrize("prec,form", [(C64, 0), (DF, 1)])
+def test_pooled_buffers_give_the_same_plan(planner, monkeypatch, prec, form):
+    """A planner reuses the buffers of the last planner destroyed on its
+    thread; a plan made after another (different) plan on dirty buffers is
+    byte for byte the plan of a fresh process."""
+    rng = np.random.default_rng(50 + prec + form)
+    d, n = 30, 10
+    R = [np.bincount(rng.integers(0, d, n), minlength=d) for _ in range(300)]
+    C = [np.bincount(rng.integers(0, d, n), minlength=d) for _ in range(300)]
+    fresh = planner(prec, form, R, C)
+    monkeypatch.setenv("PLAN_DUMP_WARM", "1")
+    warm = planner(prec, form, R, C)
+    assert "error" not in fresh, fresh
+    assert fresh == warm
+
+
 def test_threaded_planning_reports_the_first_bad_problem(planner, monkeypatch):
     d = 6
     R = [[1, 1, 0, 0, 0, 0]] * 3000
