@@ -31,28 +31,33 @@ def to_first_quantized(occupation_numbers):
 
 def _pmf_batch(U, current_input, samples, laplace):
     """pmf[s, idx] of sampling.py:723-749 for every shot, with the reference's
-    summation order (over the nonzero input modes in increasing order, then the
-    normalisation over idx in increasing order)."""
+    summation order: the terms over the nonzero input modes in increasing
+    order, then the normalisation over idx in increasing order (``cumsum``
+    adds left to right, as the reference's loop does).  Vectorised over shots
+    with the same elementwise operations; a shot with fewer terms keeps its
+    amplitude unchanged at the steps it does not take."""
     shots, d = samples.shape
-    pmf = np.empty((shots, d), dtype=np.float64)
-    for s in range(shots):
-        nz = np.nonzero(current_input[s] > 0)[0]
-        if samples[s].sum() == 0:
-            # empty output: the reference's Laplace vector is [1] (one entry)
-            part = {nz[0]: 1.0 + 0.0j}
-            terms = 1
-        else:
-            part = laplace[s]
-            terms = len(nz)
-        amp = np.zeros(d, dtype=np.complex128)
-        for j in range(terms):
-            amp = amp + (current_input[s, nz[j]] * part[nz[j]]) * U[:, nz[j]]
-        p = np.abs(amp) ** 2
-        norm = 0.0
-        for idx in range(d):
-            norm += p[idx]
-        pmf[s] = p / norm
-    return pmf
+    current_input = np.asarray(current_input)
+    nzmask = current_input > 0
+    terms = nzmask.sum(axis=1)
+    # the nonzero input modes of every shot first, in increasing order
+    order = np.argsort(~nzmask, axis=1, kind="stable")
+    # empty output: the reference's Laplace vector is [1] (one entry), so one term
+    empty = samples.sum(axis=1) == 0
+    terms = np.where(empty, 1, terms)
+    lap = np.asarray(laplace, dtype=np.complex128)
+    Ut = np.ascontiguousarray(np.asarray(U).T)
+    at = np.arange(shots)
+    amp = np.zeros((shots, d), dtype=np.complex128)
+    for t in range(int(terms.max(initial=0))):
+        j = order[:, t]
+        part = np.where(empty, 1.0 + 0.0j, lap[at, j])
+        coef = current_input[at, j] * part
+        stepped = amp + coef[:, None] * Ut[j]
+        amp = np.where((t < terms)[:, None], stepped, amp)
+    p = np.abs(amp) ** 2
+    norm = np.cumsum(p, axis=1)[:, -1]
+    return p / norm[:, None]
 
 
 def _separate_particles(input_occupation, overlap, rng):
@@ -99,7 +104,7 @@ def _lockstep(U, U128, samples, photons, rngs, rejects):
     output mode.  ``samples`` (shots x d) is updated in place."""
     nb, d = samples.shape
     current = np.zeros((nb, d), dtype=int)
-    to_shrink = [np.copy(p) for p in photons]
+    to_shrink = [list(p) for p in photons]
     steps = max((len(p) for p in photons), default=0)
     for k in range(steps):
         act = [s for s in range(nb) if k < len(photons[s]) and not rejects[s][k]]
@@ -107,8 +112,7 @@ def _lockstep(U, U128, samples, photons, rngs, rejects):
             continue
         for s in act:
             i = rngs[s].choice(len(to_shrink[s]))
-            current[s, to_shrink[s][i]] += 1
-            to_shrink[s] = np.delete(to_shrink[s], i)
+            current[s, to_shrink[s].pop(i)] += 1
         idx = np.asarray(act)
         lap = permanent_laplace_batch(U, samples[idx], current[idx]).astype(np.complex128)
         pmf = _pmf_batch(U128, current[idx], samples[idx], lap)

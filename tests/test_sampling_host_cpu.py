@@ -97,3 +97,81 @@ def test_same_seed_same_samples(sampling_on_cpu):
     a = sampling_on_cpu.generate_samples_batched(inp, 200, U, seed=11, batch_size=64, workers=1)
     b = sampling_on_cpu.generate_samples_batched(inp, 200, U, seed=11, batch_size=64, workers=3)
     assert np.array_equal(a, b)  # per-batch generators: the thread count does not matter
+
+
+# --- the reference-RNG sampler's host logic (generate_samples: the lockstep
+# photon steps and the vectorised pmf) against the reference's seeded goldens,
+# its batched Laplace call answered by the oracle
+
+
+@pytest.fixture
+def rng_mode_on_cpu(monkeypatch):
+    from piquasso_gb300 import sampling
+    from test_postselect import _oracle_laplace_batch
+
+    monkeypatch.setattr(sampling, "permanent_laplace_batch", _oracle_laplace_batch)
+    return sampling
+
+
+def test_seeded_golden_on_cpu(rng_mode_on_cpu):
+    from conftest import as_matrix, load_golden
+
+    g = load_golden("sampler_seeded.json")
+    samples = rng_mode_on_cpu.generate_samples(g["input"], g["shots"], as_matrix(g["U"]), g["seed"], batch_size=7)
+    assert [list(s) for s in samples] == g["generated_samples"]
+    assert [list(s) for s in rng_mode_on_cpu.result_samples(samples, g["seed"])] == g["expected_samples"]
+
+
+def test_seeded_lossy_goldens_on_cpu(rng_mode_on_cpu):
+    from conftest import as_matrix, load_golden
+
+    for c in load_golden("sampler_lossy_seeded.json")["cases"]:
+        M = as_matrix(c["matrix"]).astype(np.complex128)
+        got = rng_mode_on_cpu.sample(np.array(c["input"]), c["shots"], M, c["seed"])
+        assert [list(s) for s in got] == c["generated_samples"], c["kind"]
+
+
+def test_overlap_and_loss_match_restatement_on_cpu(rng_mode_on_cpu):
+    from oracle import sampler as osampler
+
+    U = haar_unitary(4, 8) * np.sqrt(0.8)
+    inp = np.array([2, 1, 1, 0])
+    got = rng_mode_on_cpu.generate_samples(inp, 40, U, 5, transmission=0.8, particle_overlap=0.6)
+    want = osampler.generate_samples(inp, 40, oracle.permanent_laplace_dd, U, 5, transmission=0.8, overlap=0.6)
+    assert got == want
+
+
+def test_vectorised_pmf_matches_the_reference_loop():
+    """sampling._pmf_batch against the oracle's per-shot restatement of the
+    reference's _calculate_pmf (sampling.py:723-749; Python loops over modes
+    on numpy scalars) for shots with different numbers of terms, repeated
+    input modes and an empty output.  Array and scalar complex arithmetic in
+    numpy differ in the last bits (6e-16 here), which the seeded goldens
+    above never notice; the terms' order is the reference's."""
+    from oracle import sampler as osampler
+    from piquasso_gb300 import sampling
+
+    d = 7
+    U = haar_unitary(d, 12)
+    rng = np.random.default_rng(3)
+    cur, out = [], []
+    for k in range(1, 8):
+        c = np.bincount(rng.integers(0, d, k), minlength=d)
+        o = np.bincount(rng.integers(0, d, k - 1), minlength=d)
+        cur.append(c)
+        out.append(o)
+    cur, out = np.array(cur), np.array(out)
+    lap = np.zeros((len(cur), d), dtype=np.complex128)
+    want = []
+    for s in range(len(cur)):
+        if out[s].sum() > 0:
+            lap[s] = oracle.permanent_laplace_dd(U, out[s], cur[s])[:d]
+        nz = np.nonzero(cur[s])[0]
+
+        def laplace(matrix, rows, cols, s=s, nz=nz):
+            return np.array([1.0 + 0.0j]) if rows.sum() == 0 else lap[s][nz]
+
+        want.append(osampler.calculate_pmf(cur[s], out[s], laplace, U))
+    got = sampling._pmf_batch(U, cur, out, lap)
+    want = np.array(want)
+    assert np.max(np.abs(got - want) / want) < 1e-14
