@@ -60,6 +60,18 @@ def _pmf_batch(U, current_input, samples, laplace):
     return p / norm[:, None]
 
 
+def _draw_from_pmf(pmf, u):
+    """``rng.choice(np.arange(d), p=pmf[s])`` of every shot s, from one
+    ``rng.random()`` per shot (u[s]), which is all the draw takes from the
+    generator: numpy's Generator.choice with p and no size normalises the
+    cumulative sum by its last entry and returns searchsorted(cdf, u,
+    'right'), the number of entries <= u (sampling.py:752-753 of the
+    reference makes that call)."""
+    cdf = np.cumsum(pmf, axis=1)
+    cdf /= cdf[:, -1:]
+    return (cdf <= u[:, None]).sum(axis=1)
+
+
 def _separate_particles(input_occupation, overlap, rng):
     """sampling.py:371-400 of the reference: per occupied input mode j, the
     number K of indistinguishable photons, drawn with weights
@@ -116,8 +128,8 @@ def _lockstep(U, U128, samples, photons, rngs, rejects):
         idx = np.asarray(act)
         lap = permanent_laplace_batch(U, samples[idx], current[idx]).astype(np.complex128)
         pmf = _pmf_batch(U128, current[idx], samples[idx], lap)
-        for r, s in enumerate(act):
-            samples[s, rngs[s].choice(np.arange(d), p=pmf[r])] += 1
+        u = np.array([rngs[s].random() for s in act])
+        samples[idx, _draw_from_pmf(pmf, u)] += 1
 
 
 def generate_samples(input_state, shots, interferometer, seed, batch_size=4096, transmission=None,

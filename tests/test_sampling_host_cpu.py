@@ -175,3 +175,25 @@ def test_vectorised_pmf_matches_the_reference_loop():
     got = sampling._pmf_batch(U, cur, out, lap)
     want = np.array(want)
     assert np.max(np.abs(got - want) / want) < 1e-14
+
+
+def test_draw_from_pmf_is_generator_choice():
+    """One rng.random() per shot and a count over the normalised cumulative
+    sum give what rng.choice(np.arange(d), p=pmf) gives, and leave every
+    generator in the same state."""
+    import copy
+
+    from piquasso_gb300 import sampling
+
+    master = np.random.default_rng(123)
+    for trial in range(300):
+        d = int(master.integers(2, 60))
+        pmf = master.random((4, d)) ** 3 + 1e-300
+        pmf[0, master.integers(0, d)] = 0.0
+        pmf /= pmf.sum(axis=1, keepdims=True)
+        gens = [np.random.default_rng(trial * 4 + s) for s in range(4)]
+        twins = [copy.deepcopy(g) for g in gens]
+        want = [g.choice(np.arange(d), p=pmf[s]) for s, g in enumerate(gens)]
+        got = sampling._draw_from_pmf(pmf, np.array([g.random() for g in twins]))
+        assert list(got) == want
+        assert all(a.random() == b.random() for a, b in zip(gens, twins))
