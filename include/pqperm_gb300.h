@@ -42,6 +42,10 @@ extern "C" {
 #define PQG_MODE_DF 2   /* FP64 seeds and double-double sums; updates and products in
                            double-float (FP32 pairs, ~2^-48 relative per operation) */
 
+/* Host planning: a call with 2048 or more problems is planned on up to 8
+ * host threads (the environment variable PQG_HOST_THREADS caps the count; 1
+ * plans on the calling thread).  The plan does not depend on the count. */
+
 /* Message describing the calling thread's last failure ("" if none). */
 const char *pqg_last_error(void);
 
