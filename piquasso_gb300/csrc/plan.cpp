@@ -92,11 +92,14 @@ namespace {
 // thread (up to a cap), handed to the next planner created on it.  A planner
 // created while the pool is empty (another planner on the thread holds its
 // buffers) allocates as usual.
+thread_local bool t_pool_gone = false;  // trivially destructible: readable while the thread tears down
+
 struct PlannerPool {
     std::vector<PendingProblem> pending;
     std::vector<PqgProblem> probs;
     std::vector<unsigned char> arena;
     std::vector<int32_t> idx_rows;
+    ~PlannerPool() { t_pool_gone = true; }
 };
 thread_local PlannerPool t_pool;
 
@@ -110,6 +113,7 @@ size_t capacity_bytes(const std::vector<T> &v) {
 }  // namespace
 
 Planner::Planner(Precision prec, Form form, const PlanConfig &cfg) : prec_(prec), form_(form), cfg_(cfg) {
+    if (t_pool_gone) return;
     PlannerPool &P = t_pool;
     pending.swap(P.pending);
     probs.swap(P.probs);
@@ -122,6 +126,7 @@ Planner::Planner(Precision prec, Form form, const PlanConfig &cfg) : prec_(prec)
 }
 
 Planner::~Planner() {
+    if (t_pool_gone) return;  // a planner destroyed while its thread tears down: plain frees
     PlannerPool &P = t_pool;  // the destroying thread's pool (a plan handle may die on another thread)
     const size_t mine = capacity_bytes(pending) + capacity_bytes(probs) + capacity_bytes(arena) +
                         capacity_bytes(idx_rows_);
