@@ -34,6 +34,7 @@ extern "C" {
 #define PQG_ERR_TOO_LARGE 3    /* > 32 distinct nonzero columns or > 2^50 Gray-code steps */
 #define PQG_ERR_CUDA 4         /* a CUDA runtime call failed */
 #define PQG_ERR_NO_DEVICE 5    /* no CUDA device visible */
+#define PQG_ERR_HOST 6         /* host-side failure, e.g. out of host memory (no C++ exception leaves the library) */
 
 /* precision modes for the complex128 entry points */
 #define PQG_MODE_AUTO 0 /* default: PQG_MODE_DF where valid (<= 32 particles), else FP64;

@@ -18,6 +18,7 @@ PQG_ERR_INVALID = 2
 PQG_ERR_TOO_LARGE = 3
 PQG_ERR_CUDA = 4
 PQG_ERR_NO_DEVICE = 5
+PQG_ERR_HOST = 6
 
 MODE_AUTO = 0
 MODE_FP64 = 1

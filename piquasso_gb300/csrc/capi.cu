@@ -7,6 +7,8 @@
 // work-queue head, the persistent walk kernel, the level-1 and level-2
 // double-double reductions, one D2H copy of the results.  Device and pinned
 // host buffers are cached per process and grow on demand.
+#include <exception>
+#include <new>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -37,6 +39,22 @@ std::atomic<uint64_t> g_launches{0};
 int fail(int code, const std::string &msg) {
     g_err = msg;
     return code;
+}
+
+// No C++ exception crosses the C ABI: every int entry point is a function-try-
+// block whose handler turns the exception in flight (std::bad_alloc from
+// the planner's host buffers, in practice) into PQG_ERR_HOST.
+int host_failure() {
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        g_err = "out of host memory";
+    } catch (const std::exception &e) {
+        g_err = e.what();
+    } catch (...) {
+        g_err = "host-side failure";
+    }
+    return PQG_ERR_HOST;
 }
 
 #define PQG_CUDA(call)                                                                      \
@@ -756,81 +774,105 @@ const char *pqg_version(void) { return "pqperm_gb300 0.1.0 (sm_103a)"; }
 uint64_t pqg_kernel_launches(void) { return g_launches.load(); }
 
 int pqg_permanent_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
-                       int32_t mode, double *out, double *out_lo) {
+                       int32_t mode, double *out, double *out_lo) try {
     return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, 1, c128_precision(mode), out, out_lo);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
-                      float *out) {
+                      float *out) try {
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return plain_batch<float>(m.data(), n_rows, n_cols, rows, cols, 1, Precision::C64, out, nullptr);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                             const int32_t *cols, int64_t batch, int32_t mode, double *out) {
+                             const int32_t *cols, int64_t batch, int32_t mode, double *out) try {
     return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(mode), out, nullptr);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                            const int32_t *cols, int64_t batch, float *out) {
+                            const int32_t *cols, int64_t batch, float *out) try {
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return plain_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out, nullptr);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_laplace_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                               const int32_t *cols, double *out, int64_t *n_out) {
+                               const int32_t *cols, double *out, int64_t *n_out) try {
     return laplace_one<double>(matrix, n_rows, n_cols, rows, cols, c128_precision(PQG_MODE_AUTO), out, n_out);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_laplace_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                              const int32_t *cols, float *out, int64_t *n_out) {
+                              const int32_t *cols, float *out, int64_t *n_out) try {
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return laplace_one<float>(m.data(), n_rows, n_cols, rows, cols, Precision::C64, out, n_out);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_laplace_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                                     const int32_t *cols, int64_t batch, double *out, int64_t *n_out) {
+                                     const int32_t *cols, int64_t batch, double *out, int64_t *n_out) try {
     return laplace_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(PQG_MODE_AUTO), out,
                                  n_out);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_laplace_batch_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                                    const int32_t *cols, int64_t batch, float *out, int64_t *n_out) {
+                                    const int32_t *cols, int64_t batch, float *out, int64_t *n_out) try {
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return laplace_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out, n_out);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_sampler_step_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                          const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) {
+                          const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) try {
     return sampler_step<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(PQG_MODE_AUTO), uniforms,
                                 modes);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_sampler_step_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                         const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) {
+                         const int32_t *cols, int64_t batch, const double *uniforms, int32_t *modes) try {
     if (n_rows < 0 || n_cols < 0) return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrix, 2 * n_rows * n_cols);
     return sampler_step<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, uniforms, modes);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_grad_c128(const double *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                            const int32_t *cols, int64_t batch, double *out) {
+                            const int32_t *cols, int64_t batch, double *out) try {
     return grad_batch<double>(matrices, n_rows, n_cols, rows, cols, batch, c128_precision(PQG_MODE_AUTO), out);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_permanent_grad_c64(const float *matrices, int64_t n_rows, int64_t n_cols, const int32_t *rows,
-                           const int32_t *cols, int64_t batch, float *out) {
+                           const int32_t *cols, int64_t batch, float *out) try {
     if (n_rows < 0 || n_cols < 0 || batch < 0 || (batch * n_rows * n_cols > 0 && !matrices))
         return fail(PQG_ERR_INVALID, "invalid arguments");
     std::vector<double> m = widen(matrices, 2 * batch * n_rows * n_cols);
     return grad_batch<float>(m.data(), n_rows, n_cols, rows, cols, batch, Precision::C64, out);
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) {
+int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) try {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
     if (items_per_smsp < 0 || p_max < 0 || p_max > 32768 || seed_steps < 0)
@@ -841,18 +883,22 @@ int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) {
     C.cfg.p_max_user = p_max != 0;
     C.cfg.seed_steps = seed_steps;
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_get_tuning(int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps) {
+int pqg_get_tuning(int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps) try {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
     if (items_per_smsp) *items_per_smsp = C.cfg.items_per_smsp;
     if (p_max) *p_max = C.cfg.p_max;
     if (seed_steps) *seed_steps = C.cfg.seed_steps;
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_measure_vector_peaks(double ms, double *out2) {
+int pqg_measure_vector_peaks(double ms, double *out2) try {
     if (!out2) return fail(PQG_ERR_INVALID, "null output");
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
@@ -861,10 +907,12 @@ int pqg_measure_vector_peaks(double ms, double *out2) {
     st = time_fma<double, 8>(C, ms, &out2[0]);
     if (st) return st;
     return time_fma<float, 16>(C, ms, &out2[1]);
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *flops, double *h2d_bytes,
-                    double *d2h_bytes) {
+                    double *d2h_bytes) try {
     if (h2d_bytes) *h2d_bytes = g_h2d;
     if (d2h_bytes) *d2h_bytes = g_d2h;
     if (walk_ms) *walk_ms = g_walk_ms;
@@ -872,10 +920,12 @@ int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *f
     if (steps) *steps = g_walk_steps;
     if (flops) *flops = g_walk_flops;
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
 int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
-                    int64_t batch, int32_t dtype, int32_t form, int32_t mode, pqg_plan_t **out_plan) {
+                    int64_t batch, int32_t dtype, int32_t form, int32_t mode, pqg_plan_t **out_plan) try {
     if (!out_plan || batch < 0 || n_rows < 0 || n_cols < 0 || (dtype != 0 && dtype != 1) || (form != 0 && form != 1))
         return fail(PQG_ERR_INVALID, "invalid arguments");
     *out_plan = nullptr;
@@ -922,9 +972,11 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     }
     *out_plan = reinterpret_cast<pqg_plan_t *>(h);
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_plan_launch(pqg_plan_t *plan) {
+int pqg_plan_launch(pqg_plan_t *plan) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h) return fail(PQG_ERR_INVALID, "null plan");
     PQG_CUDA(cudaEventRecord(h->e0, h->stream));
@@ -933,9 +985,11 @@ int pqg_plan_launch(pqg_plan_t *plan) {
     g_launches += pipeline_launches(h->pl);
     h->launched = true;
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms) {
+int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h) return fail(PQG_ERR_INVALID, "null plan");
     PQG_CUDA(cudaStreamSynchronize(h->stream));
@@ -945,9 +999,11 @@ int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms) {
         *device_ms = ms;
     }
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) {
+int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h || !out) return fail(PQG_ERR_INVALID, "null argument");
     std::vector<unsigned char> tmp(h->L.out_bytes);
@@ -980,9 +1036,11 @@ int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) {
     }
     if (n_values) *n_values = static_cast<int64_t>(h->pl.pending.size()) * stride;
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_plan_info(pqg_plan_t *plan, double *steps, double *flops, int64_t *work_items, int64_t *h2d_bytes) {
+int pqg_plan_info(pqg_plan_t *plan, double *steps, double *flops, int64_t *work_items, int64_t *h2d_bytes) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h) return fail(PQG_ERR_INVALID, "null plan");
     if (steps) *steps = h->pl.total_steps;
@@ -990,15 +1048,19 @@ int pqg_plan_info(pqg_plan_t *plan, double *steps, double *flops, int64_t *work_
     if (work_items) *work_items = h->pl.total_items;
     if (h2d_bytes) *h2d_bytes = static_cast<int64_t>(h->L.total);
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
-int pqg_plan_destroy(pqg_plan_t *plan) {
+int pqg_plan_destroy(pqg_plan_t *plan) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (h) {
         cudaStreamSynchronize(h->stream);
         delete h;
     }
     return PQG_OK;
+} catch (...) {
+    return host_failure();
 }
 
 }  // extern "C"

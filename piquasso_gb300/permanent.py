@@ -47,6 +47,8 @@ def _raise_for(status):
         raise PermanentTooLarge(msg)
     if status == _lib.PQG_ERR_NO_DEVICE:
         raise _lib.EngineUnavailable(msg or "no CUDA device visible")
+    if status == _lib.PQG_ERR_HOST:
+        raise MemoryError(msg)
     raise RuntimeError("piquasso_gb300 engine error %d: %s" % (status, msg))
 
 

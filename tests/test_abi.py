@@ -88,3 +88,21 @@ def test_no_cpu_fallback_without_gpu(engine):
         engine.permanent(np.eye(3), [1, 1, 1], [1, 1, 1])
     with pytest.raises(engine.EngineUnavailable):
         engine.permanent_laplace(np.eye(3)[:, :2], [1, 0, 0], [1, 1])
+
+
+def test_status_codes_match_the_header():
+    """Every PQG_ERR_* status of include/pqperm_gb300.h has the same value in
+    the Python binding (PQG_ERR_HOST: a host-side failure such as running out
+    of host memory, which the entry points return instead of letting a C++
+    exception cross the C ABI)."""
+    import os
+    import re
+
+    from piquasso_gb300 import _lib
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    header = open(os.path.join(os.path.dirname(here), "include", "pqperm_gb300.h")).read()
+    codes = dict(re.findall(r"#define (PQG_ERR_\w+) (\d+)", header))
+    assert "PQG_ERR_HOST" in codes
+    for name, value in codes.items():
+        assert getattr(_lib, name) == int(value), name
