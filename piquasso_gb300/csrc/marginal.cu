@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <new>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -202,7 +203,7 @@ int64_t rank_of(const int *c, int k, int deg) {
 extern "C" {
 
 int pqg_binomial_moments_c128(const double *U, int64_t d, const int32_t *input, const int32_t *modes, int32_t k,
-                              int32_t n_sets, double *moments, int64_t max_device_bytes) {
+                              int32_t n_sets, double *moments, int64_t max_device_bytes) try {
     if (!U || !input || !modes || !moments || d <= 0 || k <= 0 || k > 8 || n_sets <= 0)
         return fail(PQG_ERR_INVALID, "pqg_binomial_moments_c128: invalid arguments");
     int64_t n = 0;
@@ -366,6 +367,10 @@ int pqg_binomial_moments_c128(const double *U, int64_t d, const int32_t *input, 
                 moments[s * per + at] = f * diag[static_cast<size_t>(s) * L.soff[n + 1] + L.soff[deg] + i];
             }
     return PQG_OK;
+} catch (const std::bad_alloc &) {
+    return fail(PQG_ERR_HOST, "out of host memory");
+} catch (...) {  // no C++ exception crosses the C ABI
+    return fail(PQG_ERR_HOST, "host-side failure");
 }
 
 }  // extern "C"
