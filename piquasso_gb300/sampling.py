@@ -67,6 +67,8 @@ def _draw_from_pmf(pmf, u):
     cumulative sum by its last entry and returns searchsorted(cdf, u,
     'right'), the number of entries <= u (sampling.py:752-753 of the
     reference makes that call)."""
+    if np.isnan(pmf).any() or (pmf < 0).any():  # rng.choice refuses these; so does this draw
+        raise ValueError("probabilities contain NaN or negative values")
     cdf = np.cumsum(pmf, axis=1)
     cdf /= cdf[:, -1:]
     return (cdf <= u[:, None]).sum(axis=1)
