@@ -20,7 +20,7 @@ Each shot follows the reference's random-number sequence exactly, with its own
 ``np.random.default_rng(seed + idx)`` and the shared configuration generator
 for uniform loss, so a seed reproduces the reference's samples.  Each shot is
 written as a generator. Its photon steps yield (input so far, output so far)
-and receive the step's pmf. The driver answers every shot waiting on a step
+and receive the step's pmf. ``_drive`` answers every shot waiting on a step
 with one batched Laplace-permanent launch (``permanent_laplace_batch``).
 Shots run side by side unless a uniform-loss reject condition draws from
 the shared generator. Then they run one after another, because the number of

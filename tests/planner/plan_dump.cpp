@@ -1,4 +1,4 @@
-// Test driver for the host planner (compiled with g++ by tests/test_planner_cpu.py;
+// Test program for the host planner (compiled with g++ by tests/test_planner_cpu.py;
 // no CUDA): reads problems from stdin, plans them, prints the plan as JSON.
 //
 // The problems go through Planner::add_batch, which plans on several host

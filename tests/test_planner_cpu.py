@@ -1,5 +1,5 @@
 """The host planner's invariants, on CPU: plan.cpp compiled with g++ beside a
-small driver (tests/planner/plan_dump.cpp) that prints a plan as JSON.
+small program (tests/planner/plan_dump.cpp) that prints a plan as JSON.
 
 * outputs stay in the caller's order although problems are laid out longest
   item first (PqgProblem::index / out_of);
