@@ -35,7 +35,7 @@ kept as they are.
 import numpy as np
 
 from .permanent import permanent_laplace_batch
-from .sampling import _pmf_batch, _separate_particles, expanded_interferometer, to_first_quantized
+from .sampling import _draw_from_pmf, _pmf_batch, _separate_particles, expanded_interferometer, to_first_quantized
 
 
 class InvalidSimulation(RuntimeError):
@@ -56,8 +56,9 @@ def _trial_limit(limit):
 
 
 def _shot(d, n, photons, rng, reject, modes, counts, max_trials, track_needed=True):
-    """One shot of sampling.py:239-326 as a generator (yields (input, output)
-    for each photon step, receives the pmf).  Returns the output with the
+    """One shot of sampling.py:239-326 as a generator: for each photon step it
+    yields (input, output, its generator) and receives the mode drawn from the
+    step's pmf with that generator.  Returns the output with the
     postselected modes deleted, or the whole output when ``track_needed`` is
     False (the partially distinguishable sampler's inner call)."""
     modes = tuple(int(m) for m in modes)
@@ -73,16 +74,14 @@ def _shot(d, n, photons, rng, reject, modes, counts, max_trials, track_needed=Tr
         sample[:] = 0
         needed = needed0
         left = np.array(counts, dtype=int)  # photons each postselected mode may still take
-        pool = np.copy(photons)
+        pool = list(photons)
         complete = True
         for k in range(1, n + 1):
             if reject():
                 continue
             i = rng.choice(len(pool))
-            current[pool[i]] += 1
-            pool = np.delete(pool, i)
-            pmf = yield current, sample
-            mode = rng.choice(np.arange(d), p=pmf)
+            current[pool.pop(i)] += 1
+            mode = yield current, sample, rng
             sample[mode] += 1
             if mode in modes:
                 needed -= 1
@@ -215,8 +214,10 @@ def _overlap_shot(d, U, inp, rng, reject, modes, counts, max_trials, overlap):
 def _drive(U, shots, side_by_side):
     """Runs the shot generators.  Every shot waiting on a photon step gets its
     pmf from one batched Laplace launch over all of them (the pmf as the
-    reference's _calculate_pmf forms it, sampling.py:723-749).  With
-    ``side_by_side`` False the shots run one after another."""
+    reference's _calculate_pmf forms it, sampling.py:723-749) and its mode
+    from one ``random()`` of its own generator (what ``rng.choice`` with p
+    draws, sampling.py:752-753).  With ``side_by_side`` False the shots run
+    one after another."""
     U128 = U.astype(np.complex128)
     results = [None] * len(shots)
     groups = [list(range(len(shots)))] if side_by_side else [[i] for i in range(len(shots))]
@@ -235,11 +236,13 @@ def _drive(U, shots, side_by_side):
             idx = list(waiting)
             cols = np.stack([waiting[i][0] for i in idx])
             rows = np.stack([waiting[i][1] for i in idx])
+            gens = [waiting[i][2] for i in idx]
             waiting.clear()
             lap = permanent_laplace_batch(U, rows, cols).astype(np.complex128)
             pmf = _pmf_batch(U128, cols, rows, lap)
+            modes = _draw_from_pmf(pmf, np.array([g.random() for g in gens]))
             for r, i in enumerate(idx):
-                advance(i, pmf[r])
+                advance(i, int(modes[r]))
     return results
 
 
