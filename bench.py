@@ -42,6 +42,12 @@ def haar_unitary(d, seed):
     return Q * (np.diag(R) / np.abs(np.diag(R)))
 
 
+# DRAM traffic of one n=28 double-float walk launch (bytes, read + write),
+# recorded from an ncu capture of the headline workload on a GB300
+TRAFFIC_N28_DF = 528128
+TRAFFIC_N28_DF_DATE = "2026-12-04"
+
+
 def flops_all_ones(n):
     return 2.0 ** (n - 1) * (10 * n + 4)
 
@@ -150,19 +156,73 @@ def allreduce_max_sum(pg, vals_max, vals_sum):
     return t.tolist(), s.tolist()
 
 
+def cpu_info():
+    """Host cores this process may use and the CPU model (lscpu's "Model name",
+    else /proc/cpuinfo's first model line, else the machine type)."""
+    import platform
+
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        cores = os.cpu_count()
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu model")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"cores": cores, "cpu_count": os.cpu_count(), "model": model or platform.machine(),
+            "reference_threads": 4 * (os.cpu_count() or 1),
+            "threading": "the reference method starts 4 x std::thread::hardware_concurrency() OpenMP threads, "
+                         "whatever the affinity mask"}
+
+
 def cpu_reference_rate(U, ones, reps):
     """The reference's CPU method (oracle port: std::complex<double>, 4 x
-    hardware threads, OpenMP) on the same input; returns (perm/s, threads)."""
+    hardware threads, OpenMP) on the same input; returns (perm/s, cores, the
+    method's value on this input)."""
     import oracle
 
     oracle.build.build(with_reference=False)
     oracle.port_permanent(U[:20, :20].copy(), ones[:20], ones[:20])  # warm the thread pool
     times = []
+    val = None
     for _ in range(reps):
         t0 = time.perf_counter()
-        oracle.port_permanent(U, ones, ones)
+        val = oracle.port_permanent(U, ones, ones)
         times.append(time.perf_counter() - t0)
-    return 1.0 / statistics.median(times), os.cpu_count()
+    return 1.0 / statistics.median(times), cpu_info()["cores"], complex(val)
+
+
+def parity_record(got, want, pabs, against, single=False):
+    """|gpu - want| against the contract's tolerance: max(1e-10 |perm|,
+    1e-14 perm(|A|)) for complex128, max(1e-5 |perm|, 2^-23 perm(|A|)) for
+    complex64."""
+    rel, absf = (1e-5, 2.0 ** -23) if single else (1e-10, 1e-14)
+    err = abs(complex(got) - complex(want))
+    tol = max(rel * abs(want), absf * pabs)
+    return {"against": against, "value": [float(np.real(want)), float(np.imag(want))], "abs_err": err,
+            "rel_err": err / abs(want) if want else None, "tol": tol, "err_over_tol": err / tol,
+            "pass": bool(err <= tol), "perm_abs": pabs}
+
+
+def headline_config(n, dtype, world):
+    """The config dict both arms print (identical for the same workload)."""
+    return {"workload": "permanent n=%d %s, leading block of seeded %dx%d Haar unitary (seed 0), unit "
+                        "multiplicities, one permanent per step" % (n, "complex128" if dtype == "c128" else
+                                                                    "complex64", 2 * n, 2 * n),
+            "n": n, "dtype": dtype, "parallelism": "replicas" if world > 1 else "1gpu"}
 
 
 def run_reference(args, world, rank, pg):
@@ -181,7 +241,7 @@ def run_reference(args, world, rank, pg):
         oracle.port_permanent(U, ones, ones)
     dt = time.perf_counter() - t0
     value = args.steps / dt
-    cores = os.cpu_count()
+    info = cpu_info()
     line = {
         "impl": "reference",
         "metric": "permanents_per_second_n%d_complex128" % n,
@@ -196,9 +256,9 @@ def run_reference(args, world, rank, pg):
         "vs_baseline": None,
         "dtype": "c128",
         "data": "synthetic (seeded Haar unitary)",
-        "config": {"workload": "permanent n=%d complex128, leading block of seeded %dx%d Haar unitary, "
-                               "unit multiplicities" % (n, 2 * n, 2 * n), "n": n},
-        "cpu_baseline": {"value": value, "unit": "perm/s", "cores": cores, "kind": "port",
+        "config": headline_config(n, "c128", world),
+        "cpu_baseline": {"value": value, "unit": "perm/s", "cores": info["cores"], "kind": "port",
+                         "model": info["model"], "threads": info["reference_threads"],
                          "sample": "%d full n=%d permanents, reference method (4 x hw threads)" % (args.steps, n)},
         "e2e": {"value": value, "unit": "perm/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -231,6 +291,77 @@ def time_calls(pg_engine, torch, flush, U, ones, steps, mode):
         dev.append(tm["device_ms"])
         walk.append(tm["walk_ms"])
     return dev, walk, e2e, tm, res
+
+
+def bench_config2(pg_engine, torch, flush, peaks, cpu=True):
+    """Single large permanents, n = 24, 26, 28, 30: the leading n x n block of
+    a seeded 2n x 2n Haar unitary (seed 0), unit multiplicities, one
+    permanent per launch over all SMs, in the three arithmetics -- the
+    double-float walk (the complex128 default), the FP64 walk and the
+    complex64 walk.  Per entry: perm/s (device time of the pipeline, L2
+    flushed before each call), the walk's fraction of the measured FP32 or
+    FP64 peak, and the result's error against the double-double oracle
+    (n = 24) or the reference's CPU method (n >= 26), with the contract's
+    tolerance; the reference method's perm/s on the host cores beside it."""
+    import oracle
+
+    oracle.build.build(with_reference=False)
+    out = {"workload": "leading n x n block of Haar(2n) seed 0, unit multiplicities, one permanent per launch",
+           "entries": {}}
+    reps = {24: 8, 26: 5, 28: 3, 30: 2}
+    all_pass = True
+    for n in (24, 26, 28, 30):
+        U = haar_unitary(2 * n, 0)[:n, :n].copy()
+        ones = np.ones(n, dtype=int)
+        U64 = U.astype(np.complex64)
+        F = flops_all_ones(n)
+        row = {}
+        if cpu:
+            t0 = time.perf_counter()
+            port_val = complex(oracle.port_permanent(U, ones, ones))
+            cpu_s = time.perf_counter() - t0
+            pabs = float(abs(oracle.port_permanent(np.abs(U).astype(np.complex128), ones, ones)))
+            if n <= 24:
+                against = "double-double oracle"
+                ref = oracle.permanent(U, ones, ones)
+                ref64 = oracle.permanent(U64.astype(np.complex128), ones, ones)
+            else:
+                against = "reference CPU method (oracle port)"
+                ref = port_val
+                ref64 = complex(oracle.port_permanent(U64.astype(np.complex128), ones, ones))
+            row["cpu_reference"] = {"value": 1.0 / cpu_s, "unit": "perm/s", "cores": cpu_info()["cores"],
+                                    "kind": "port", "sample": "one full n=%d complex128 permanent" % n}
+        for arith in ("df", "fp64", "c64"):
+            A = U64 if arith == "c64" else U
+            mode = "api" if arith == "c64" else arith
+            time_calls(pg_engine, torch, flush, A, ones, 1, mode)  # first use of the instantiation
+            dev, walk, _, _, res = time_calls(pg_engine, torch, flush, A, ones, reps[n], mode)
+            w = statistics.mean(walk) / 1e3
+            rec = {"value": len(dev) / (sum(dev) / 1e3), "unit": "perm/s", "walk_ms": 1e3 * w}
+            if arith == "df":
+                rec["achieved_tflops"] = 2.0 ** (n - 1) * df_flops_per_step(n) / w / 1e12
+                rec["peak_tflops"] = peaks["fp32_tflops"]
+                rec["basis"] = "FP32 flops executed by the double-float walk, 2^(n-1)(72n+38), vs measured FP32 peak"
+                rec["complex128_algorithmic_tflops"] = F / w / 1e12
+            elif arith == "fp64":
+                rec["achieved_tflops"] = F / w / 1e12
+                rec["peak_tflops"] = peaks["fp64_tflops"]
+                rec["basis"] = "algorithmic 2^(n-1)(10n+4) vs measured FP64 peak"
+            else:
+                rec["achieved_tflops"] = F / w / 1e12
+                rec["peak_tflops"] = peaks["fp32_tflops"]
+                rec["basis"] = "algorithmic 2^(n-1)(10n+4) vs measured FP32 peak"
+            rec["frac"] = rec["achieved_tflops"] / rec["peak_tflops"]
+            if cpu:
+                rec["parity"] = parity_record(res, ref64 if arith == "c64" else ref, pabs, against,
+                                              single=arith == "c64")
+                all_pass = all_pass and rec["parity"]["pass"]
+                rec["speedup_vs_cpu"] = rec["value"] / row["cpu_reference"]["value"]
+            row["complex64" if arith == "c64" else ("complex128_df" if arith == "df" else "complex128_fp64")] = rec
+        out["entries"]["n%d" % n] = row
+    if cpu:
+        out["all_within_tolerance"] = all_pass
+    return out
 
 
 def batch_workload():
@@ -280,7 +411,7 @@ def bench_batch(pg_engine, torch, flush, args, cpu=True):
         for p in pats[:k]:
             oracle.port_permanent(U, p, inp)
         dt = time.perf_counter() - t0
-        out["cpu_baseline"] = {"value": k / dt, "unit": "perm/s", "cores": os.cpu_count(), "kind": "port",
+        out["cpu_baseline"] = {"value": k / dt, "unit": "perm/s", "cores": cpu_info()["cores"], "kind": "port",
                                "sample": "first %d of the 4096 patterns, one reference-method call each" % k}
     return out
 
@@ -412,7 +543,7 @@ def bench_next_rows(args, cpu=True):
             v = oracle.port_permanent(A, r2, c2)
             assert abs(v - G[0, j]) <= 1e-9 * abs(G).max()
         per = (time.perf_counter() - t0) / k
-        g["cpu_baseline"] = {"ms": 1e3 * per * n * n, "unit": "ms per gradient", "cores": os.cpu_count(),
+        g["cpu_baseline"] = {"ms": 1e3 * per * n * n, "unit": "ms per gradient", "cores": cpu_info()["cores"],
                              "kind": "port", "sample": "%d of the %d minors (reference method), scaled" % (k, n * n)}
         g["speedup_vs_cpu"] = g["cpu_baseline"]["ms"] / g["ms"]
     out["gradient_n20"] = g
@@ -485,11 +616,15 @@ def run_ours(args, world, rank, local, pg):
                 "flops_basis": "FP32 flops of the double-float walk, 2^(n-1)(72n+38) (FMA = 2)",
                 "complex128_algorithmic_tflops": F / mean_walk_s / 1e12}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    # DRAM bytes (read + write) of one headline launch, from one ncu capture
-    # of the same workload (profiles/walk_plain_df_n28_dram.md)
+    # DRAM bytes (read + write) of one headline launch: a recorded constant
+    # from one ncu capture of this workload (the walk reads the 12.5 KB
+    # matrix's prefix tables, seeds and weight tables, and writes its
+    # partials); a bench run cannot read DRAM counters itself
     if n == 28 and args.dtype == "c128":
-        roof["traffic"] = 528128
-        roof["traffic_source"] = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one n=28 launch"
+        roof["traffic"] = TRAFFIC_N28_DF
+        roof["traffic_source"] = ("recorded constant, not measured by this run: ncu dram__bytes_read.sum + "
+                                  "dram__bytes_write.sum of one n=28 double-float walk launch, captured %s"
+                                  % TRAFFIC_N28_DF_DATE)
     else:
         roof["traffic"] = None
     roof["peak_source"] = "measured: engine FMA-chain microkernel (pqg_measure_vector_peaks)"
@@ -508,11 +643,8 @@ def run_ours(args, world, rank, local, pg):
         "vs_baseline": None,
         "dtype": args.dtype,
         "data": "synthetic (seeded Haar unitary)",
-        "config": {"workload": "permanent n=%d %s, leading block of seeded %dx%d Haar unitary, unit "
-                               "multiplicities, one permanent per launch over all SMs"
-                               % (n, "complex128" if args.dtype == "c128" else "complex64", 2 * n, 2 * n),
-                   "n": n, "l2": "flushed between steps (256 MB write)",
-                   "parallelism": "replicas" if world > 1 else "1gpu",
+        "config": headline_config(n, args.dtype, world),
+        "timing": {"l2": "flushed between steps (256 MB write)",
                    "c128_arithmetic": "auto (double-float walk, FP64 seeds and double-double sums)"},
         "e2e": {"value": e2e, "unit": "perm/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": roof,
@@ -553,11 +685,28 @@ def run_ours(args, world, rank, local, pg):
         line["sampling_n24_d48"] = section(bench_sampling, args)
         line["training_mlp"] = section(bench_training, args)
         line["next_rows"] = section(bench_next_rows, args, cpu=(rank == 0 and not args.no_cpu_baseline))
+    if rank == 0 and not args.no_variants:
+        line["config2"] = section(bench_config2, pg_engine, torch, flush, peaks, cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_cpu_baseline:
-        rate, cores = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
+        rate, cores, ref_val = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
+        info = cpu_info()
         line["cpu_baseline"] = {"value": rate, "unit": "perm/s", "cores": cores, "kind": "port",
+                                "model": info["model"], "threads": info["reference_threads"],
                                 "sample": "median of %d full n=%d complex128 permanents, reference method, "
                                           "4 x hw threads" % (args.cpu_reps, n)}
+        if args.dtype == "c128":
+            import oracle
+
+            pabs = float(abs(oracle.port_permanent(np.abs(U128).astype(np.complex128), ones, ones)))
+            par = {"reference_method": parity_record(result, ref_val, pabs, "reference CPU method (oracle port)")}
+            if not args.no_dd_oracle:
+                t0 = time.perf_counter()
+                par["dd_oracle"] = parity_record(result, oracle.permanent(U128, ones, ones), pabs,
+                                                 "double-double oracle")
+                par["dd_oracle"]["oracle_s"] = time.perf_counter() - t0
+            par["pass"] = all(v["pass"] for v in par.values() if isinstance(v, dict))
+            par["tolerance"] = "max(1e-10 |perm|, 1e-14 perm(|A|)); perm(|A|) by the reference method"
+            line["parity"] = par
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -674,6 +823,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-sampling", action="store_true")
+    ap.add_argument("--no-dd-oracle", action="store_true", help="skip the double-double check of the headline")
     ap.add_argument("--mcmc-steps", type=int, default=600)
     ap.add_argument("--exact-samples", type=int, default=32768)
     ap.add_argument("--profile-case", default=None, help="run one small named case for ncu and exit")

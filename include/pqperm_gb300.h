@@ -194,6 +194,25 @@ int pqg_measure_vector_peaks(double ms, double *out2);
 int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *flops, double *h2d_bytes,
                     double *d2h_bytes);
 
+/* Walk kernel of the calling thread's last plain/Laplace/batch/sampler call
+ * (no counterpart in the reference, whose CPU loop has one form): `table`
+ * receives one of PQG_WALK_* (-1 when the call needed no walk) and `n_cols`
+ * the exact column count of the instantiation (1..32).  Every (table, column
+ * count) pair is a separately compiled kernel; tests use this to show that
+ * each one has run against the oracle.  Either pointer may be null. */
+#define PQG_WALK_PLAIN_FP64 0        /* FP64 walk, repeated columns */
+#define PQG_WALK_PLAIN_C64 1         /* complex64 walk, repeated columns */
+#define PQG_WALK_LAPLACE_FP64 2      /* FP64 Laplace walk */
+#define PQG_WALK_LAPLACE_C64 3       /* complex64 Laplace walk, repeated columns */
+#define PQG_WALK_PLAIN_DF 4          /* double-float walk, repeated columns */
+#define PQG_WALK_LAPLACE_C64_UNIT 5  /* complex64 Laplace walk, unit columns */
+#define PQG_WALK_PLAIN_FP64_UNIT 6   /* FP64 walk, unit columns */
+#define PQG_WALK_PLAIN_C64_UNIT 7    /* complex64 walk, unit columns */
+#define PQG_WALK_PLAIN_DF_UNIT 8     /* double-float walk, unit columns */
+#define PQG_WALK_LAPLACE_DF_UNIT 9   /* double-float Laplace walk, unit columns (<= 25) */
+#define PQG_WALK_LAPLACE_DF 10       /* double-float Laplace walk, any columns */
+int pqg_last_walk_kernel(int32_t *table, int32_t *n_cols);
+
 /* Learned proposal (no counterpart in the reference): kernels of the
  * autoregressive MLP over output occupations used as the independence
  * proposal of the Metropolis boson sampler.  All pointers are DEVICE pointers;
@@ -272,9 +291,14 @@ int pqg_proposal_step_tc(int32_t j, int32_t B, int32_t d, int32_t n, const float
  *
  * It allocates no device memory: all intermediate data lives in one
  * file-scope device array of PQG_NOALLOC_SCRATCH_BYTES, held by every GPU that
- * loads the library until the process exits.  The first call on a device looks
- * that array's address up (cudaGetSymbolAddress) with the device current; make
- * that first call before any stream capture.  Every call on a device shares
+ * loads the library until the process exits.  With CUDA's lazy module loading
+ * (the default) the array comes into being when the library's device code is
+ * first loaded on a device, at the latest in the first call of this entry
+ * point there: that first call looks the array's address up
+ * (cudaGetSymbolAddress) with the device current, and it is the one call that
+ * can need device memory.  Make it before your own allocator reserves the
+ * device, and before any stream capture; later calls allocate nothing.  Every
+ * call on a device shares
  * the array, so calls whose executions overlap on the GPU (different streams,
  * or threads) race and give wrong results: order them on one stream.
  * n must be between 1 and PQG_NOALLOC_MAX_N; larger sizes are rejected with

@@ -11,8 +11,10 @@
 # Flags follow the reference's Release build: -O3 -std=c++17 -fopenmp.
 set -euo pipefail
 
-REF="${PQ_REFERENCE_DIR:-/root/reference}"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+# the reference checkout: PQ_REFERENCE_DIR, else a directory named "reference"
+# beside this repository
+REF="${PQ_REFERENCE_DIR:-$(dirname "$(dirname "$HERE")")/reference}"
 OUT="$HERE/_ref"
 
 if [ ! -f "$REF/src/permanent.cpp" ]; then

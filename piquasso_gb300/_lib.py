@@ -79,6 +79,14 @@ SIGNATURES = {
     "pqg_get_tuning": ([_i64, _i64, _i64], ctypes.c_int),
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),
     "pqg_last_timing": ([_d, _d, _d, _d, _d, _d], ctypes.c_int),
+    "pqg_last_walk_kernel": ([_i32, _i32], ctypes.c_int),
+}
+
+# walk kernel tables (PQG_WALK_* in the header), as pqg_last_walk_kernel reports them
+WALK_TABLES = {
+    0: "plain_fp64", 1: "plain_c64", 2: "laplace_fp64", 3: "laplace_c64", 4: "plain_df",
+    5: "laplace_c64_unit", 6: "plain_fp64_unit", 7: "plain_c64_unit", 8: "plain_df_unit",
+    9: "laplace_df_unit", 10: "laplace_df",
 }
 
 _lib = None
@@ -125,6 +133,14 @@ def last_timing():
     load().pqg_last_timing(*[ctypes.byref(x) for x in v])
     keys = ("walk_ms", "device_ms", "steps", "flops", "h2d_bytes", "d2h_bytes")
     return {k: x.value for k, x in zip(keys, v)}
+
+
+def last_walk_kernel():
+    """(table name, exact column count) of the walk kernel this thread's last
+    call launched, or (None, 0) when it needed no walk."""
+    t, n = ctypes.c_int32(0), ctypes.c_int32(0)
+    load().pqg_last_walk_kernel(ctypes.byref(t), ctypes.byref(n))
+    return (WALK_TABLES.get(t.value), n.value) if t.value >= 0 else (None, 0)
 
 
 def check_tc_status():

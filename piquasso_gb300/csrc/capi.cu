@@ -34,6 +34,9 @@ namespace {
 thread_local std::string g_err;
 thread_local double g_walk_ms = 0.0, g_dev_ms = 0.0, g_walk_steps = 0.0, g_walk_flops = 0.0;
 thread_local double g_h2d = 0.0, g_d2h = 0.0;
+// walk instantiation of the calling thread's last plan run: kernel table
+// (PQG_WALK_* in the header) and exact column count; -1 / 0 when no walk ran
+thread_local int g_last_table = -1, g_last_nc = 0;
 std::atomic<uint64_t> g_launches{0};
 
 int fail(int code, const std::string &msg) {
@@ -343,9 +346,13 @@ int run_plan(Context &C, Planner &pl, T *out, double *out_lo, const DrawRequest 
     PQG_CUDA(C.h_out.ensure(align256(L.out_bytes) + L.lo_bytes));
     const KernelInfo *k = nullptr;
     int64_t blocks = 1;
+    g_last_table = -1;
+    g_last_nc = 0;
     if (pl.total_items > 0) {
         st = walk_launch_config(C, pl, &k, &blocks);
         if (st) return st;
+        kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, &g_last_table);
+        g_last_nc = pl.max_nc;
     }
     cudaStream_t s = C.stream;
     PQG_CUDA(cudaMemcpyAsync(C.bufs.plan.p, C.h_plan.p, L.total, cudaMemcpyHostToDevice, s));
@@ -919,6 +926,14 @@ int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *f
     if (device_ms) *device_ms = g_dev_ms;
     if (steps) *steps = g_walk_steps;
     if (flops) *flops = g_walk_flops;
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
+int pqg_last_walk_kernel(int32_t *table, int32_t *n_cols) try {
+    if (table) *table = g_last_table;
+    if (n_cols) *n_cols = g_last_nc;
     return PQG_OK;
 } catch (...) {
     return host_failure();

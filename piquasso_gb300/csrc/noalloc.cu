@@ -185,25 +185,35 @@ __global__ void unit_finish(UnitPlan p, const unsigned char *__restrict__ scratc
     }
 }
 
-// Device address of the scratch, looked up once per device with that device
-// current (cudaGetSymbolAddress; the array's host-side name is not a device
-// address).
+// Per-device state, looked up once per device with that device current: the
+// scratch's device address (cudaGetSymbolAddress; the array's host-side name
+// is not a device address) and the SM count the split and the grid are sized
+// for.
+struct DeviceScratch {
+    void *ptr = nullptr;
+    int num_sms = 0;
+};
 std::mutex g_scratch_mu;
-void *g_scratch_ptr[64] = {nullptr};
+DeviceScratch g_scratch[64];
 
-cudaError_t scratch_address(void **ptr) {
+cudaError_t scratch_for_device(DeviceScratch *out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
+    DeviceScratch &d = g_scratch[dev];
+    if (!d.ptr) {
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = p;
+        d.num_sms = sms > 0 ? sms : 1;
+        d.ptr = p;
     }
-    *ptr = g_scratch_ptr[dev];
+    *out = d;
     return cudaSuccess;
 }
 
@@ -224,14 +234,17 @@ using namespace pqg;
 
 extern "C" {
 
-int pqg_permanent_unit_c128_noalloc(const double *d_matrix, int64_t n, double *d_out, void *stream) {
+// A function-try-block like every other entry point: no C++ exception (the
+// mutex, the error message) crosses the C ABI.
+int pqg_permanent_unit_c128_noalloc(const double *d_matrix, int64_t n, double *d_out, void *stream) try {
     if (!d_matrix || !d_out) return noalloc_fail(PQG_ERR_INVALID, "null device pointer");
     if (n < 1 || n > kNoallocMaxN)
         return noalloc_fail(PQG_ERR_TOO_LARGE, "matrix order must be between 1 and PQG_NOALLOC_MAX_N (32)");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    void *scratch = nullptr;
-    cudaError_t e = scratch_address(&scratch);
+    DeviceScratch dev{};
+    cudaError_t e = scratch_for_device(&dev);
     if (e != cudaSuccess) return noalloc_fail(PQG_ERR_CUDA, "scratch address", e);
+    void *scratch = dev.ptr;
 
     // implicit plan: up to 256 inner codes, up to 64 outer positions per lane,
     // at least ~16 warps of work per SM sub-partition when the space allows
@@ -241,7 +254,7 @@ int pqg_permanent_unit_c128_noalloc(const double *d_matrix, int64_t n, double *d
     p.K = digits < 8 ? digits : 8;
     p.n_outer = digits - p.K;
     const int64_t Q = int64_t(1) << p.n_outer;
-    int64_t R = Q / (32 * 4 * 152 * 16);
+    int64_t R = Q / (int64_t(32) * 4 * dev.num_sms * 16);
     R = R < 1 ? 1 : (R > 64 ? 64 : R);
     p.R = static_cast<int>(R);
     const int64_t lanes = (Q + R - 1) / R;
@@ -259,11 +272,17 @@ int pqg_permanent_unit_c128_noalloc(const double *d_matrix, int64_t n, double *d
     if (e != cudaSuccess) return noalloc_fail(PQG_ERR_CUDA, "queue reset", e);
     const double2 *a = reinterpret_cast<const double2 *>(d_matrix);
     unit_build_delta<<<64, 256, 0, s>>>(a, p, sc);
-    unit_walk<<<152 * 4, PQG_WALK_THREADS, 0, s>>>(a, p, sc);
+    unit_walk<<<dev.num_sms * 4, PQG_WALK_THREADS, 0, s>>>(a, p, sc);
     unit_finish<<<1, 1024, 0, s>>>(p, sc, d_out);
     e = cudaGetLastError();
     if (e != cudaSuccess) return noalloc_fail(PQG_ERR_CUDA, "launch", e);
     return PQG_OK;
+} catch (...) {
+    try {
+        set_last_error("host-side failure");
+    } catch (...) {
+    }
+    return PQG_ERR_HOST;
 }
 
 }  // extern "C"

@@ -65,11 +65,24 @@ void parallel_ranges(int64_t n, int nt, const std::function<void(int, int64_t, i
     std::vector<std::thread> pool;
     pool.reserve(static_cast<size_t>(nt - 1));
     const int64_t per = (n + nt - 1) / nt;
+    // A worker that cannot be started (std::system_error: no thread
+    // resources) leaves its range, and every later one, to the calling
+    // thread; the threads already started are always joined.
+    int started = 1;
     for (int w = 1; w < nt; ++w) {
         const int64_t lo = std::min<int64_t>(n, w * per), hi = std::min<int64_t>(n, lo + per);
-        pool.emplace_back(run, w, lo, hi);
+        try {
+            pool.emplace_back(run, w, lo, hi);
+        } catch (...) {
+            break;
+        }
+        started = w + 1;
     }
     run(0, 0, std::min<int64_t>(n, per));
+    for (int w = started; w < nt; ++w) {
+        const int64_t lo = std::min<int64_t>(n, w * per), hi = std::min<int64_t>(n, lo + per);
+        run(w, lo, hi);
+    }
     for (auto &t : pool) t.join();
     for (auto &e : errs)
         if (e) std::rethrow_exception(e);

@@ -254,10 +254,50 @@ def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, s
     return out
 
 
+def integrated_autocorrelation(series, c=5.0):
+    """Integrated autocorrelation time of a scalar statistic recorded on
+    several chains, ``series`` of shape (steps, chains): the normalised
+    autocovariance rho_k averaged over the chains (about the overall mean),
+    tau = 1 + 2 sum_{k=1}^{M} rho_k with Sokal's automatic window (the
+    smallest M >= c tau(M)).  tau is 1 for independent draws; a chain of
+    length T then holds about T / tau effective samples.  A constant
+    statistic gives tau = 1."""
+    x = np.asarray(series, dtype=np.float64)
+    T = x.shape[0]
+    x = x - x.mean()
+    var = float(np.mean(x * x))
+    if T < 2 or var == 0.0:
+        return 1.0
+    nfft = 1 << int(np.ceil(np.log2(2 * T)))
+    f = np.fft.rfft(x, n=nfft, axis=0)
+    acov = np.fft.irfft(f * np.conj(f), n=nfft, axis=0)[:T].sum(axis=1)
+    acov /= (T - np.arange(T)) * x.shape[1]  # unbiased per lag, averaged over chains
+    rho = acov / acov[0]
+    tau = 1.0
+    for m in range(1, T):
+        tau += 2.0 * rho[m]
+        if m >= c * tau:
+            break
+    return max(tau, 1.0)
+
+
+def chain_autocorrelation(samples, chains):
+    """tau of every mode's occupation, from recorded chain states in step-
+    major order ((steps * chains, d), as run_chains records them); returns
+    (max over modes, mean over modes)."""
+    S = np.asarray(samples)
+    steps = S.shape[0] // chains
+    S = S[: steps * chains].reshape(steps, chains, -1)
+    taus = [integrated_autocorrelation(S[:, :, j]) for j in range(S.shape[2])]
+    return float(np.max(taus)), float(np.mean(taus))
+
+
 def evaluate(U, input_photons, mlp=None, chains=1024, steps=300, burn_in=30, seed=0, baseline=False, pairs=None,
              pair_seed=0, n_pairs=16, block=8):
-    """Samples/s, acceptance and two-mode-marginal TVD (mean and max over
-    `pairs`, default `n_pairs` random mode pairs) of one Metropolis run."""
+    """Samples/s, acceptance, two-mode-marginal TVD (mean and max over
+    `pairs`, default `n_pairs` random mode pairs) and the chains' integrated
+    autocorrelation time (mode occupations; the largest over the modes gives
+    the effective samples per second) of one Metropolis run."""
     from .marginals import tvd_two_mode
 
     d = len(input_photons)
@@ -267,7 +307,10 @@ def evaluate(U, input_photons, mlp=None, chains=1024, steps=300, burn_in=30, see
         pairs = [allp[i] for i in rng.choice(len(allp), size=min(n_pairs, len(allp)), replace=False)]
     out = run_chains(U, input_photons, mlp=mlp, chains=chains, steps=steps, burn_in=burn_in, seed=seed,
                      baseline=baseline, block=block)
-    tv = tvd_two_mode(out.pop("samples"), input_photons, U, pairs)
+    S = out.pop("samples")
+    tv = tvd_two_mode(S, input_photons, U, pairs)
+    tau_max, tau_mean = chain_autocorrelation(S, chains)
     out.update({"tvd_mean": float(tv.mean()), "tvd_max": float(tv.max()), "pairs": [list(p) for p in pairs],
-                "kept_samples": chains * max(0, steps - burn_in)})
+                "kept_samples": chains * max(0, steps - burn_in), "tau_max": tau_max, "tau_mean": tau_mean,
+                "effective_samples_per_s": out["samples_per_s"] / tau_max})
     return out

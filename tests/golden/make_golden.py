@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Runs only where the reference source tree is present (default
-/root/reference, override with PQ_REFERENCE_DIR) and its permanent module has
+Runs only where the reference source tree is present (PQ_REFERENCE_DIR, else
+a directory named ``reference`` beside this repository) and its permanent module has
 been compiled by oracle/build_ref.sh.  Outputs (JSON, complex numbers as
 [re, im] pairs):
 
@@ -48,7 +48,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PQ_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("PQ_REFERENCE_DIR") or os.path.join(os.path.dirname(REPO), "reference")
 sys.path.insert(0, REPO)
 
 import oracle  # noqa: E402

@@ -20,8 +20,8 @@ The samplers are driven by the reference's compiled ``permanent_laplace``
 ``config`` carries ``seed_sequence``, ``rng = default_rng(seed_sequence)``
 (piquasso/api/config.py:159) and ``use_dask = False``.
 
-Runs only where the reference source tree is present (default
-/root/reference, override with PQ_REFERENCE_DIR).
+Runs only where the reference source tree is present (PQ_REFERENCE_DIR, else
+a directory named ``reference`` beside this repository).
 
 Usage: python tests/golden/make_postselect_golden.py
 """
@@ -36,7 +36,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PQ_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("PQ_REFERENCE_DIR") or os.path.join(os.path.dirname(REPO), "reference")
 sys.path.insert(0, REPO)
 
 import oracle  # noqa: E402
