@@ -364,6 +364,41 @@ def bench_config2(pg_engine, torch, flush, peaks, cpu=True):
     return out
 
 
+def bench_tuning(reps=5):
+    """Tuned against default on the benchmarked shapes: the n = 28 headline
+    permanent, the 4096-pattern batch (one graph-captured plan), a Metropolis
+    block of 8192 complex64 target permanents, and the exact sampler's last
+    photon step.  Each is timed (median device time of `reps` graph
+    executions) with the engine's tuning table emptied (the defaults) and
+    with the table the package loaded (the autotuner's cache for this GPU and
+    library version)."""
+    from piquasso_gb300 import _lib, autotune
+
+    lib = _lib.load()
+    key = autotune.cache_key(lib)
+    entries = autotune.cached_entries(key)
+    out = {"cache_key": key, "cache_entries": len(entries),
+           "how": "median device ms of %d executions of one graph-captured plan per setting" % reps}
+    names = ("single_n28_df", "batch_4096_d40_n20", "target_8192_n24_d48", "sampler_last_step_2048_n24_d48")
+    ws = {w.name: w for w in autotune.standard_workloads()}
+    for name in names:
+        w = ws[name]
+        lib.pqg_tuning_clear()
+        d_ms, _ = autotune.time_workload(w, autotune.DEFAULT_SETTINGS, reps)
+        autotune.install(entries, lib)
+        t_ms, _ = autotune.time_workload(w, autotune.DEFAULT_SETTINGS, reps)
+        with w.plan() as p:
+            import ctypes
+
+            v = [ctypes.c_int64(0) for _ in range(3)]
+            b = ctypes.c_int32(0)
+            lib.pqg_plan_config(p._h, *[ctypes.byref(x) for x in v], ctypes.byref(b))
+        out[name] = {"default_ms": d_ms, "tuned_ms": t_ms, "speedup": d_ms / t_ms,
+                     "tuned_settings": {"items_per_smsp": v[0].value, "p_max": v[1].value,
+                                        "seed_steps": v[2].value, "blocks_per_sm": b.value}}
+    return out
+
+
 def batch_workload():
     """4096 output patterns drawn uniformly from the compositions of 20 photons
     into 40 modes with at most 4 per mode; seeded 40x40 Haar unitary; one
@@ -687,6 +722,7 @@ def run_ours(args, world, rank, local, pg):
         line["next_rows"] = section(bench_next_rows, args, cpu=(rank == 0 and not args.no_cpu_baseline))
     if rank == 0 and not args.no_variants:
         line["config2"] = section(bench_config2, pg_engine, torch, flush, peaks, cpu=not args.no_cpu_baseline)
+        line["tuning"] = section(bench_tuning)
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores, ref_val = cpu_reference_rate(U128, ones, reps=args.cpu_reps)
         info = cpu_info()

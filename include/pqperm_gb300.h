@@ -174,9 +174,38 @@ int pqg_plan_destroy(pqg_plan_t *plan);
  * items_per_smsp — warps of work per SM sub-partition the split aims for
  * (default 16); p_max — longest inner walk, i.e. step-table length (default
  * 2048, at most 32768); seed_steps — Gray-code steps per lane that amortise
- * one seed (default depends on the arithmetic).  The autotuner sets these. */
+ * one seed (default depends on the arithmetic).  The reference fixes its
+ * split at 4 x hardware_concurrency contiguous segments
+ * (src/permanent.cpp:144-155); these knobs replace it.  A knob set here
+ * (nonzero) overrides the autotuned table below for every workload; the
+ * autotuner (piquasso_gb300.autotune) sets them while it times candidates.
+ * pqg_set_blocks_per_sm caps the walk's resident blocks per SM the same way
+ * (0: as many as fit, or the autotuned value). */
 int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps);
 int pqg_get_tuning(int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps);
+int pqg_set_blocks_per_sm(int32_t blocks);
+
+/* Autotuned settings (no counterpart in the reference).  Each entry gives the
+ * planner knobs (0: keep the default) for the workloads of one form (0 plain,
+ * 1 Laplace) and arithmetic (0 FP64, 1 double-float, 2 complex64) whose
+ * largest column count lies in [nc_lo, nc_hi], total Gray-code steps in
+ * [steps_lo, steps_hi) and walk problems in [probs_lo, probs_hi].  Every
+ * call's planner takes the first matching entry for each knob that
+ * pqg_set_tuning leaves at 0.  The Python package fills this table at load
+ * time from the tuning cache that piquasso_gb300.autotune writes (a JSON file
+ * keyed by GPU name and library version); C callers add entries themselves.
+ * pqg_plan_config reports the knobs a plan handle was planned with. */
+int pqg_tuning_add(int32_t form, int32_t arith, int32_t nc_lo, int32_t nc_hi, double steps_lo, double steps_hi,
+                   int64_t probs_lo, int64_t probs_hi, int64_t items_per_smsp, int64_t p_max, int64_t seed_steps,
+                   int32_t blocks_per_sm);
+int pqg_tuning_clear(void);
+int pqg_tuning_count(int64_t *count);
+int pqg_plan_config(pqg_plan_t *plan, int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps,
+                    int32_t *blocks_per_sm);
+
+/* Name (NUL-terminated, at most name_len bytes with the NUL) and SM count of
+ * the device the engine runs on. */
+int pqg_device_info(char *name, int64_t name_len, int32_t *num_sms);
 
 /* Measured FP64 / FP32 fused-multiply-add throughput of device 0 in TFLOP/s
  * (2 flops per FMA), from dependent-chain microkernels run over all SMs for

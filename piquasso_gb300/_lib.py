@@ -80,6 +80,13 @@ SIGNATURES = {
     "pqg_measure_vector_peaks": ([ctypes.c_double, _d], ctypes.c_int),
     "pqg_last_timing": ([_d, _d, _d, _d, _d, _d], ctypes.c_int),
     "pqg_last_walk_kernel": ([_i32, _i32], ctypes.c_int),
+    "pqg_set_blocks_per_sm": ([_I32], ctypes.c_int),
+    "pqg_tuning_add": ([_I32, _I32, _I32, _I32, ctypes.c_double, ctypes.c_double, _I64, _I64, _I64, _I64, _I64,
+                        _I32], ctypes.c_int),
+    "pqg_tuning_clear": ([], ctypes.c_int),
+    "pqg_tuning_count": ([_i64], ctypes.c_int),
+    "pqg_plan_config": ([ctypes.c_void_p, _i64, _i64, _i64, _i32], ctypes.c_int),
+    "pqg_device_info": ([ctypes.c_char_p, _I64, _i32], ctypes.c_int),
 }
 
 # walk kernel tables (PQG_WALK_* in the header), as pqg_last_walk_kernel reports them
@@ -114,7 +121,22 @@ def load():
                 fn.argtypes = args
                 fn.restype = res
             _lib = lib
+            _apply_tuning_cache()
     return _lib
+
+
+def _apply_tuning_cache():
+    """Fills the engine's autotuned-settings table from the tuning cache of
+    this GPU and library version (piquasso_gb300.autotune), if there is one;
+    without a visible GPU, or with PQG_TUNING=off, nothing is loaded."""
+    if os.environ.get("PQG_TUNING", "").lower() in ("off", "0", "none"):
+        return
+    try:
+        from . import autotune
+
+        autotune.apply_cache(_lib)
+    except Exception:  # noqa: BLE001  (a missing or unreadable cache leaves the defaults)
+        pass
 
 
 def last_error() -> str:
@@ -160,6 +182,30 @@ def set_tuning(items_per_smsp=0, p_max=0, seed_steps=0):
     st = load().pqg_set_tuning(int(items_per_smsp), int(p_max), int(seed_steps))
     if st:
         raise ValueError(last_error())
+
+
+def set_blocks_per_sm(blocks=0):
+    """Process-wide cap on the walk's resident blocks per SM (0: as many as
+    fit, or the autotuned value)."""
+    st = load().pqg_set_blocks_per_sm(int(blocks))
+    if st:
+        raise ValueError(last_error())
+
+
+def tuning_count():
+    n = ctypes.c_int64(0)
+    load().pqg_tuning_count(ctypes.byref(n))
+    return n.value
+
+
+def device_info():
+    """(device name, SM count) of the engine's GPU; raises without one."""
+    buf = ctypes.create_string_buffer(256)
+    sms = ctypes.c_int32(0)
+    st = load().pqg_device_info(buf, 256, ctypes.byref(sms))
+    if st:
+        raise EngineUnavailable(last_error())
+    return buf.value.decode(errors="replace"), sms.value
 
 
 def get_tuning():

@@ -102,6 +102,18 @@ struct DeviceBuffers {
     DevBuf plan, partials, chunk_out, out, counter, delta, draw;
 };
 
+// One autotuned setting: the planner knobs for the workloads of one form and
+// arithmetic whose largest column count, total Gray-code steps and problem
+// count fall in the given ranges (pqg_tuning_add).
+struct TuneEntry {
+    int32_t form, arith;        // 0 plain / 1 Laplace; 0 FP64, 1 double-float, 2 complex64
+    int32_t nc_lo, nc_hi;       // largest column count, inclusive
+    double steps_lo, steps_hi;  // total Gray-code steps, [lo, hi)
+    int64_t probs_lo, probs_hi; // problems, inclusive
+    int64_t items_per_smsp, p_max, seed_steps;
+    int32_t blocks_per_sm;
+};
+
 struct Context {
     std::mutex mu;
     DeviceBuffers bufs;
@@ -112,7 +124,8 @@ struct Context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, evs = nullptr;
     HostBuf h_plan, h_out;
     PlanConfig cfg;
-    int blocks_per_sm = 0;  // 0: as many as fit (occupancy)
+    int blocks_per_sm = 0;  // process-wide walk blocks per SM (pqg_set_blocks_per_sm); 0: the plan's
+    std::vector<TuneEntry> tune;  // autotuned settings by workload (pqg_tuning_add)
     std::vector<int> occ_cache[11];  // blocks per SM, per kernel table, per column count
 
     int init() {
@@ -137,6 +150,43 @@ struct Context {
 Context &ctx() {
     static Context c;
     return c;
+}
+
+int arith_code(Precision p) { return p == Precision::C128 ? 0 : (p == Precision::C128DF ? 1 : 2); }
+
+// The planner configuration of a plan whose problems are added: the
+// process-wide knobs (pqg_set_tuning), and for every knob left at its default
+// there, the first autotuned entry matching the plan's form, arithmetic,
+// largest column count, total steps and problem count.  Caller holds C.mu.
+PlanConfig tuned_config(const Context &C, const Planner &pl, Precision prec) {
+    PlanConfig cfg = C.cfg;
+    if (pl.form() == Form::LAPLACE) cfg.p_max = std::min<int64_t>(cfg.p_max, 512);  // Laplace tables
+    if (C.tune.empty()) return cfg;
+    int ncmax = 0;
+    double steps = 0.0;
+    int64_t probs = 0;
+    for (const PendingProblem &p : pl.pending)
+        if (p.kind == PQG_KIND_WALK) {
+            ncmax = std::max(ncmax, p.nc);
+            steps += p.S;
+            ++probs;
+        }
+    if (probs == 0) return cfg;
+    const int form = pl.form() == Form::LAPLACE ? 1 : 0, arith = arith_code(prec);
+    for (const TuneEntry &t : C.tune) {
+        if (t.form != form || t.arith != arith || ncmax < t.nc_lo || ncmax > t.nc_hi || steps < t.steps_lo ||
+            steps >= t.steps_hi || probs < t.probs_lo || probs > t.probs_hi)
+            continue;
+        if (cfg.items_per_smsp == 0 && t.items_per_smsp > 0) cfg.items_per_smsp = t.items_per_smsp;
+        if (!cfg.p_max_user && t.p_max > 0) {
+            cfg.p_max = form == 1 ? std::min<int64_t>(t.p_max, 512) : t.p_max;
+            cfg.p_max_user = true;
+        }
+        if (cfg.seed_steps == 0 && t.seed_steps > 0) cfg.seed_steps = t.seed_steps;
+        if (t.blocks_per_sm > 0) cfg.blocks_per_sm = t.blocks_per_sm;
+        break;
+    }
+    return cfg;
 }
 
 // walk kernel for (form, precision, exact column count); `which` indexes the
@@ -271,7 +321,8 @@ int walk_launch_config(Context &C, const Planner &pl, const KernelInfo **k, int6
         occ = std::max(1, b);
     }
     const int64_t warps_per_block = PQG_WALK_THREADS / 32;
-    int64_t nb = static_cast<int64_t>(C.num_sms) * std::min(occ, C.blocks_per_sm > 0 ? C.blocks_per_sm : occ);
+    const int bps = C.blocks_per_sm > 0 ? C.blocks_per_sm : pl.config().blocks_per_sm;
+    int64_t nb = static_cast<int64_t>(C.num_sms) * std::min(occ, bps > 0 ? bps : occ);
     nb = std::min<int64_t>(nb, (pl.total_items + warps_per_block - 1) / warps_per_block);
     *k = &kk;
     *blocks = std::max<int64_t>(1, nb);
@@ -451,18 +502,20 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
         int st = pl.add_batch(rows, cols, batch, err, &bad);
         if (st) return fail(st, batch > 1 ? "problem " + std::to_string(bad) + ": " + err : err);
     }
-    PlanConfig cfg;
+    PlanConfig cfg, cfg64;
     {
         std::lock_guard<std::mutex> lock(C.mu);
         int st = C.init();
         if (st) return st;
-        cfg = C.cfg;
+        cfg = tuned_config(C, pl, prec);
+        cfg64 = tuned_config(C, pl, Precision::C128);
     }
     pl.set_config(cfg);
     pl.finish();
     if (prec == Precision::C128DF && !pl.df_ok) {
         // outside the double-float domain: the FP64 walk
         pl.set_precision(Precision::C128);
+        pl.set_config(cfg64);
         pl.finish();
     }
     std::lock_guard<std::mutex> lock(C.mu);
@@ -471,9 +524,10 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
 
 // The double-float Laplace walk serves plans in the double-float domain; any
 // other complex128 Laplace plan is redone for the FP64 walk.
-void laplace_precision_fallback(Planner &pl) {
+void laplace_precision_fallback(Planner &pl, const PlanConfig &cfg64) {
     if (pl.precision() == Precision::C128DF && !pl.df_ok) {
         pl.set_precision(Precision::C128);
+        pl.set_config(cfg64);
         pl.finish();
     }
 }
@@ -489,17 +543,17 @@ int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int6
         int st = pl.add_batch(rows, cols, batch, err, &bad);
         if (st) return fail(st, batch > 1 ? "problem " + std::to_string(bad) + ": " + err : err);
     }
-    PlanConfig cfg;
+    PlanConfig cfg, cfg64;
     {
         std::lock_guard<std::mutex> lock(C.mu);
         int st = C.init();
         if (st) return st;
-        cfg = C.cfg;
+        cfg = tuned_config(C, pl, pl.precision());
+        cfg64 = tuned_config(C, pl, Precision::C128);
     }
-    cfg.p_max = std::min<int64_t>(cfg.p_max, 512);
     pl.set_config(cfg);
     pl.finish();
-    laplace_precision_fallback(pl);
+    laplace_precision_fallback(pl, cfg64);
     return PQG_OK;
 }
 
@@ -630,10 +684,9 @@ int grad_batch(const double *mats, int64_t nr, int64_t nc, const int32_t *rows, 
     if (minors.empty()) return PQG_OK;
     int st = C.init();
     if (st) return st;
-    cfg.num_sms = C.cfg.num_sms;
-    pl.set_config(cfg);
+    pl.set_config(tuned_config(C, pl, pl.precision()));
     pl.finish();
-    laplace_precision_fallback(pl);
+    laplace_precision_fallback(pl, tuned_config(C, pl, Precision::C128));
     std::vector<T> res(2 * static_cast<size_t>(std::max<int64_t>(1, pl.total_outputs)));
     st = run_plan<T>(C, pl, res.data(), nullptr);
     if (st) return st;
@@ -905,6 +958,82 @@ int pqg_get_tuning(int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps)
     return host_failure();
 }
 
+int pqg_set_blocks_per_sm(int32_t blocks) try {
+    if (blocks < 0 || blocks > 32) return fail(PQG_ERR_INVALID, "blocks per SM must be between 0 and 32");
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    C.blocks_per_sm = blocks;
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
+int pqg_tuning_add(int32_t form, int32_t arith, int32_t nc_lo, int32_t nc_hi, double steps_lo, double steps_hi,
+                   int64_t probs_lo, int64_t probs_hi, int64_t items_per_smsp, int64_t p_max, int64_t seed_steps,
+                   int32_t blocks_per_sm) try {
+    if (form < 0 || form > 1 || arith < 0 || arith > 2 || nc_lo > nc_hi || !(steps_lo < steps_hi) ||
+        probs_lo > probs_hi || items_per_smsp < 0 || p_max < 0 || p_max > 32768 || seed_steps < 0 ||
+        blocks_per_sm < 0 || blocks_per_sm > 32)
+        return fail(PQG_ERR_INVALID, "invalid tuning entry");
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    C.tune.push_back(TuneEntry{form, arith, nc_lo, nc_hi, steps_lo, steps_hi, probs_lo, probs_hi, items_per_smsp,
+                               p_max, seed_steps, blocks_per_sm});
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
+int pqg_tuning_clear(void) try {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    C.tune.clear();
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
+int pqg_tuning_count(int64_t *count) try {
+    if (!count) return fail(PQG_ERR_INVALID, "null output");
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    *count = static_cast<int64_t>(C.tune.size());
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
+int pqg_plan_config(pqg_plan_t *plan, int64_t *items_per_smsp, int64_t *p_max, int64_t *seed_steps,
+                    int32_t *blocks_per_sm) try {
+    PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
+    if (!h) return fail(PQG_ERR_INVALID, "null plan");
+    const PlanConfig &c = h->pl.config();
+    if (items_per_smsp) *items_per_smsp = c.items_per_smsp;
+    if (p_max) *p_max = c.p_max;
+    if (seed_steps) *seed_steps = c.seed_steps;
+    if (blocks_per_sm) *blocks_per_sm = c.blocks_per_sm;
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
+int pqg_device_info(char *name, int64_t name_len, int32_t *num_sms) try {
+    Context &C = ctx();
+    std::lock_guard<std::mutex> lock(C.mu);
+    int st = C.init();
+    if (st) return st;
+    cudaDeviceProp prop;
+    PQG_CUDA(cudaGetDeviceProperties(&prop, C.device));
+    if (name && name_len > 0) {
+        std::strncpy(name, prop.name, static_cast<size_t>(name_len - 1));
+        name[name_len - 1] = '\0';
+    }
+    if (num_sms) *num_sms = C.num_sms;
+    return PQG_OK;
+} catch (...) {
+    return host_failure();
+}
+
 int pqg_measure_vector_peaks(double ms, double *out2) try {
     if (!out2) return fail(PQG_ERR_INVALID, "null output");
     Context &C = ctx();
@@ -972,12 +1101,13 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
         delete h;
         return st;
     }
-    h->pl.set_config(C.cfg);
+    h->pl.set_config(tuned_config(C, h->pl, prec));
     h->pl.finish();
     if (fm == Form::LAPLACE) {
-        laplace_precision_fallback(h->pl);
+        laplace_precision_fallback(h->pl, tuned_config(C, h->pl, Precision::C128));
     } else if (prec == Precision::C128DF && !h->pl.df_ok) {
         h->pl.set_precision(Precision::C128);
+        h->pl.set_config(tuned_config(C, h->pl, Precision::C128));
         h->pl.finish();
     }
     st = h->single ? plan_build<float>(C, h) : plan_build<double>(C, h);

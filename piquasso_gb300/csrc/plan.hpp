@@ -28,6 +28,7 @@ struct PlanConfig {
     int64_t p_max = 2048;         // longest inner walk (table length)
     bool p_max_user = false;      // p_max was set explicitly (overrides the per-arithmetic cap)
     int64_t seed_steps = 0;       // steps per lane that amortise a seed; 0: per-precision default
+    int blocks_per_sm = 0;        // walk blocks per SM; 0: as many as fit (occupancy)
 };
 
 // One reduced problem before its inner/outer split is fixed.  Fixed-size
@@ -89,6 +90,7 @@ class Planner {
     void finish();
 
     void set_config(const PlanConfig &cfg) { cfg_ = cfg; }
+    const PlanConfig &config() const { return cfg_; }
 
     std::vector<PendingProblem> pending;
     std::vector<PqgProblem> probs;     // in work order (PqgProblem::index: the pending problem)
