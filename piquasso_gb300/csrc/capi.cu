@@ -152,6 +152,24 @@ Context &ctx() {
     return c;
 }
 
+// The engine's buffers, stream and events belong to the device that was
+// current at its first call.  Every entry point that touches them makes that
+// device current for the call and gives the caller's back afterwards, so a
+// thread that has switched to another device neither fails nor leaks work
+// onto the wrong one.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard &) = delete;
+    DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
+
 int arith_code(Precision p) { return p == Precision::C128 ? 0 : (p == Precision::C128DF ? 1 : 2); }
 
 // The planner configuration of a plan whose problems are added: the
@@ -191,7 +209,7 @@ PlanConfig tuned_config(const Context &C, const Planner &pl, Precision prec) {
 
 // walk kernel for (form, precision, exact column count); `which` indexes the
 // occupancy cache
-const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_ones, int *which) {
+const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_ones, bool pairs, int *which) {
     if (form == Form::PLAIN) {
         if (prec == Precision::C128DF) {
             *which = all_ones ? 8 : 4;
@@ -206,7 +224,7 @@ const KernelInfo &kernel_for_plan(Form form, Precision prec, int nc, bool all_on
         return all_ones ? kernel_for(k_plain_c64o_0, k_plain_c64o_1, nc) : kernel_for(k_plain_c64_0, k_plain_c64_1, nc);
     }
     if (prec == Precision::C64) {
-        if (all_ones) {
+        if (pairs) {  // unit columns, two codes per iteration from a code-pair table
             *which = 5;
             return kernel_for(k_laplace_c64o_0, k_laplace_c64o_1, nc);
         }
@@ -287,7 +305,7 @@ int enqueue_prep(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayo
     A.mat_cols = pl.mat_cols;
     A.n_probs = static_cast<int32_t>(L.n_probs);
     A.dup = (pl.precision() == Precision::C64 && pl.form() == Form::PLAIN) ? 1 : 0;
-    A.pad = 0;
+    A.pairs = pl.pairs ? 1 : 0;
     // enough blocks for every SM: several slices per problem for small batches
     const int64_t want = int64_t(C.num_sms) * 4;
     A.slices = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(64, want / std::max<int64_t>(1, L.n_probs))));
@@ -310,7 +328,7 @@ int enqueue_prep(Context &C, DeviceBuffers &B, const Planner &pl, const PlanLayo
 // Walk kernel of a plan, its dynamic shared memory set up, and its grid size.
 int walk_launch_config(Context &C, const Planner &pl, const KernelInfo **k, int64_t *blocks) {
     int which = 0;
-    const KernelInfo &kk = kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, &which);
+    const KernelInfo &kk = kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, pl.pairs, &which);
     int &occ = C.occ_cache[which][pl.max_nc];
     if (occ < 0) {
         if (kk.smem_bytes > 0)
@@ -389,6 +407,7 @@ struct DrawRequest {
 template <typename T>
 int run_plan(Context &C, Planner &pl, T *out, double *out_lo, const DrawRequest *draw = nullptr) {
     if (pl.probs.empty()) return PQG_OK;
+    DeviceGuard dg(C.device);
     const PlanLayout L = layout_of(pl, sizeof(T));
     PQG_CUDA(C.h_plan.ensure(L.total));
     pack_plan(pl, L, static_cast<unsigned char *>(C.h_plan.p));
@@ -402,7 +421,7 @@ int run_plan(Context &C, Planner &pl, T *out, double *out_lo, const DrawRequest 
     if (pl.total_items > 0) {
         st = walk_launch_config(C, pl, &k, &blocks);
         if (st) return st;
-        kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, &g_last_table);
+        kernel_for_plan(pl.form(), pl.precision(), pl.max_nc, pl.all_ones, pl.pairs, &g_last_table);
         g_last_nc = pl.max_nc;
     }
     cudaStream_t s = C.stream;
@@ -771,8 +790,12 @@ struct PlanHandle {
     cudaGraphExec_t exec = nullptr;
     bool single = false;      // complex64 outputs
     bool launched = false;
+    int device = 0;           // the engine's device, where the handle's buffers live
+    bool on_device = false;   // plan_build ran: device resources to free
     int64_t n_cols = 0;       // Laplace: outputs per problem in the caller's layout
     ~PlanHandle() {
+        if (!on_device) return;
+        DeviceGuard dg(device);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (e0) cudaEventDestroy(e0);
@@ -785,6 +808,9 @@ struct PlanHandle {
 
 template <typename T>
 int plan_build(Context &C, PlanHandle *h) {
+    h->device = C.device;
+    h->on_device = true;
+    DeviceGuard dg(C.device);
     h->L = layout_of(h->pl, sizeof(T));
     int st = ensure_buffers(h->B, h->pl, h->L);
     if (st) return st;
@@ -1040,6 +1066,7 @@ int pqg_measure_vector_peaks(double ms, double *out2) try {
     std::lock_guard<std::mutex> lock(C.mu);
     int st = C.init();
     if (st) return st;
+    DeviceGuard dg(C.device);
     st = time_fma<double, 8>(C, ms, &out2[0]);
     if (st) return st;
     return time_fma<float, 16>(C, ms, &out2[1]);
@@ -1124,6 +1151,7 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
 int pqg_plan_launch(pqg_plan_t *plan) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h) return fail(PQG_ERR_INVALID, "null plan");
+    DeviceGuard dg(h->device);
     PQG_CUDA(cudaEventRecord(h->e0, h->stream));
     PQG_CUDA(cudaGraphLaunch(h->exec, h->stream));
     PQG_CUDA(cudaEventRecord(h->e1, h->stream));
@@ -1137,6 +1165,7 @@ int pqg_plan_launch(pqg_plan_t *plan) try {
 int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h) return fail(PQG_ERR_INVALID, "null plan");
+    DeviceGuard dg(h->device);
     PQG_CUDA(cudaStreamSynchronize(h->stream));
     if (device_ms) {
         float ms = 0.0f;
@@ -1151,6 +1180,7 @@ int pqg_plan_synchronize(pqg_plan_t *plan, double *device_ms) try {
 int pqg_plan_read(pqg_plan_t *plan, void *out, int64_t *n_values) try {
     PlanHandle *h = reinterpret_cast<PlanHandle *>(plan);
     if (!h || !out) return fail(PQG_ERR_INVALID, "null argument");
+    DeviceGuard dg(h->device);
     std::vector<unsigned char> tmp(h->L.out_bytes);
     if (h->L.out_bytes) {
         PQG_CUDA(cudaMemcpyAsync(tmp.data(), h->B.out.p, h->L.out_bytes, cudaMemcpyDeviceToHost, h->stream));

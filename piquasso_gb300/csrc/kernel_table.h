@@ -29,7 +29,7 @@ extern const KernelInfo k_laplace_c128_0[16];
 extern const KernelInfo k_laplace_c128_1[16];
 extern const KernelInfo k_laplace_c64_0[16];
 extern const KernelInfo k_laplace_c64_1[16];
-extern const KernelInfo k_laplace_c64o_0[16];  // every column of multiplicity 1
+extern const KernelInfo k_laplace_c64o_0[16];  // unit columns, code pairs (2..24 columns)
 extern const KernelInfo k_laplace_c64o_1[16];
 extern const KernelInfo k_laplace_dfo_0[16];  // double-float, every column of multiplicity 1
 extern const KernelInfo k_laplace_dfo_1[16];

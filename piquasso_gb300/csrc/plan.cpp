@@ -516,6 +516,18 @@ void Planner::finish() {
     // L1; its problems then come in whole groups of items
     const int64_t group = (prec_ == Precision::C64 && form_ == Form::PLAIN) ? PQG_ITEM_GROUP : 1;
     item_group = static_cast<int>(group);
+    // complex64 Laplace plans whose every walk problem has unit columns (the
+    // exact sampler's) store their prefix tables as code pairs for the
+    // two-code walk: each problem's table holds an even number of codes
+    pairs = false;
+    if (prec_ == Precision::C64 && laplace && any_walk && ncmax >= 2 && ncmax <= PQG_PAIRS_MAX_NC) {
+        pairs = true;
+        for (const auto &p : pending) {
+            if (p.kind != PQG_KIND_WALK) continue;
+            for (int k = 0; k < p.nc && pairs; ++k) pairs = p.cm[k] == 1;
+            if (!pairs) break;
+        }
+    }
 
     // Outputs stay in the caller's order; the work runs longest items first.
     // The device queue hands out items in problem order, so the problems are
@@ -683,7 +695,7 @@ void Planner::finish() {
             if (no) q.off_outer_df = pdata(16 * int64_t(no) * p.nc);
         }
         if (no) q.off_D = pdata(d_elem * 2 * int64_t(no) * p.nc);
-        total_delta += static_cast<int64_t>(q.P) * p.nc;
+        total_delta += static_cast<int64_t>(pairs ? (q.P + 1) & ~1 : q.P) * p.nc;
 
         auto it = table_cache_.find(tkey[ip]);
         if (it != table_cache_.end()) {

@@ -108,6 +108,8 @@ class Planner {
     int max_nc = 0;
     int item_group = 1;                // items a walk block takes at once (total_items is a multiple)
     bool all_ones = true;              // every walk problem's columns have multiplicity 1
+    bool pairs = false;                // complex64 Laplace, unit columns, <= PQG_PAIRS_MAX_NC columns:
+                                       // prefix tables stored as code pairs (an even count per problem)
     double total_steps = 0.0;          // sum over problems of the Gray-code space
     double total_flops = 0.0;          // algorithmic flop count, see algorithmic_flops()
 

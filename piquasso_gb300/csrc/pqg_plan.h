@@ -33,6 +33,9 @@
 #define PQG_SMEM_TABLE_NC_MIN 17
 #define PQG_SMEM_TABLE_NC_MAX 24
 #define PQG_SMEM_TABLE_P 256
+// complex64 Laplace walks of unit columns up to this count take two inner
+// codes per iteration, from prefix tables stored as code pairs
+#define PQG_PAIRS_MAX_NC 24
 
 enum PqgProblemKind : int32_t {
     PQG_KIND_WALK = 0,      // Gray-code walk on the device

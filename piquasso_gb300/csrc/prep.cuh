@@ -40,8 +40,9 @@ struct PrepArgs {
     int64_t mat_cols;
     int32_t n_probs;
     int32_t slices;
-    int32_t dup;   // PREP_F32 only: table entries {re, re, im, im} (the packed two-seed walk)
-    int32_t pad;
+    int32_t dup;    // PREP_F32 only: table entries {re, re, im, im} (the packed two-seed walk)
+    int32_t pairs;  // PREP_F32 only: code pairs, float4 {re_2u, re_2u+1, im_2u, im_2u+1} per column
+                    // (an odd P gets a zero pad code)
 };
 
 __device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
@@ -286,10 +287,22 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                     reinterpret_cast<double2 *>(A.delta)[at] = make_double2(re, im);
                 } else if constexpr (FMT == PREP_F32) {
                     const float fr = __double2float_rn(re), fi = __double2float_rn(im);
-                    if (A.dup)
+                    if (A.dup) {
                         reinterpret_cast<float4 *>(A.delta)[at] = make_float4(fr, fr, fi, fi);
-                    else
+                    } else if (A.pairs) {
+                        // code t of column j: pair t/2, lane t&1 (delta_begin counts float2 slots)
+                        const int t = t0 + tl;
+                        float *f = reinterpret_cast<float *>(A.delta) + 2 * pr->delta_begin +
+                                   (static_cast<int64_t>(t >> 1) * nc + j) * 4 + (t & 1);
+                        f[0] = fr;
+                        f[2] = fi;
+                        if ((P & 1) && t == P - 1) {  // the zero pad code P beside the last one
+                            f[1] = 0.0f;
+                            f[3] = 0.0f;
+                        }
+                    } else {
                         reinterpret_cast<float2 *>(A.delta)[at] = make_float2(fr, fi);
+                    }
                 } else {
                     float4 v;
                     split_df(re, v.x, v.y);

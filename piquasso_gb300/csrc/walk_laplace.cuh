@@ -392,6 +392,223 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
     }
 }
 
+// Complex64 Laplace walk for unit columns (the exact sampler's case), two
+// inner codes per iteration.  Codes a = 2u and b = 2u + 1 of the same outer
+// position ride in the two lanes of Blackwell's packed FP32x2 instructions
+// (__fadd2_rn, __fmul2_rn, __ffma2_rn; each lane rounded as the scalar
+// instruction).  The plan stores the prefix table as code pairs, one float4
+// {re_a, re_b, im_a, im_b} per column (prep.cuh, `pairs`; an odd P gets a
+// zero pad code of weight 0), so one load feeds both codes, and the seeds
+// stay scalar: each column sum is two scalar adds into adjacent registers.
+// The columns are split into two halves, each with its own prefix chain and
+// suffix chain, so every pass runs two independent dependency chains of
+// packed multiplies.  The step weight of each code times the lane's outer
+// weight starts the suffix chains (an exact FP32 integer: the sampler's
+// weights stay below 2^24), so both codes add into one FP32 partial sum per
+// output (re_a + re_b, then into the sum), folded into the per-lane FP64
+// sums every 16 code pairs.  Prefix products of both codes sit in one float4
+// per column in registers; the per-output FP32 partial sums and the FP64
+// sums in column-major slices of shared memory (a partial sum is read and
+// written once per output per code pair, where shared prefix products would
+// cost a store and a load of a float4 per column).
+template <int NC>
+struct LaplaceC64PCfg {
+    static constexpr size_t smem_bytes = size_t(NC + 1) * PQG_WALK_THREADS * sizeof(float2) +
+                                         size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2);
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+constexpr int LAP64P_G = 8;
+
+template <int NC>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArgs A) {
+    static_assert(NC >= 2, "unit-column Laplace walks have at least two columns");
+    extern __shared__ double2 lap_smem64p[];
+    const int lane = threadIdx.x & 31;
+    LaneArray<double2, NC + 1, true> acc64;  // per-lane FP64 sums of every output
+    acc64.init(lap_smem64p, threadIdx.x);
+    LaneArray<float2, NC + 1, true> part;  // per-lane FP32 partial sums {re, im} of every output
+    part.init(reinterpret_cast<float2 *>(lap_smem64p + (NC + 1) * PQG_WALK_THREADS), threadIdx.x);
+    LaneArray<float4, NC, false> pre;  // prefix products {re_a, re_b, im_a, im_b}, registers
+    pre.init(nullptr, threadIdx.x);
+
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t R = pr->R;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
+        const int n_out = pr->n_out;
+        const bool full = n_out > NC;
+        const bool active = r0 < pr->Q;
+        if (active) {
+            float sr0[NC], si0[NC];  // seed of the current outer position (double-float, rounded)
+            OuterState st;
+            outer_decode(pr, r0, st);
+            {
+                ArF32::cs_t s[NC];
+                seed_lane<ArF32, NC>(pr, A.arena, st, s);
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+                    sr0[j] = s[j].r;
+                    si0[j] = s[j].i;
+                }
+            }
+            float wout = static_cast<float>(outer_weight(pr, st));
+            const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
+            const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            // code-pair rows (delta_begin is even: every problem's table holds an even count)
+            const float4 *delta = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin / 2;
+            const int P = pr->P;
+            const int pairs = (P + 1) >> 1;
+#pragma unroll
+            for (int l = 0; l <= NC; ++l) {
+                part.set(l, make_float2(0.0f, 0.0f));
+                acc64.set(l, make_double2(0.0, 0.0));
+            }
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+                for (int u = 0; u < pairs; ++u) {
+                    const int ta = 2 * u, tb = ta + 1;
+                    // step weights times the outer weight (the pad code weighs 0)
+                    const float2 w2 = f2(__fmul_rn(__ldg(&tab[ta].wf), wout),
+                                         tb < P ? __fmul_rn(__ldg(&tab[tb].wf), wout) : 0.0f);
+                    const float4 *d = delta + static_cast<int64_t>(u) * NC;
+                    // (plain loads, which the compiler barriers below order: the suffix
+                    // pass reloads its rows rather than keeping the prefix pass's live)
+                    auto col = [&](int j, float2 &cr, float2 &ci) {
+                        const float4 v = d[j];
+                        cr = f2(__fadd_rn(sr0[j], v.x), __fadd_rn(sr0[j], v.y));
+                        ci = f2(__fadd_rn(si0[j], v.z), __fadd_rn(si0[j], v.w));
+                    };
+                    // Halves: low 0..H-1 and high H..NC-1.  Prefix pass: pre_l =
+                    // prod_{k<l} c_k within the low half (l = 1..H-1) and
+                    // prod_{H<=k<l} c_k within the high half (l = H+1..NC-1); the
+                    // chains end at P_lo and P_hi, the halves' products.  Suffix pass:
+                    // the high chain starts at w P_lo, the low one at w P_hi, so
+                    // out_l = pre_l * (chain after the columns above l in its half)
+                    // = w prod_{k != l} c_k.  (A compiler barrier every LAP64P_G steps
+                    // keeps at most that many table rows in flight.)
+                    constexpr int H = NC / 2;
+                    float2 xlr, xli, xhr, xhi;
+#pragma unroll
+                    for (int i = 0; i < NC - H; ++i) {
+                        if (i % LAP64P_G == 0) asm volatile("" ::: "memory");
+                        if (i < H) {
+                            float2 cr, ci;
+                            col(i, cr, ci);
+                            if (i == 0) {
+                                xlr = cr;
+                                xli = ci;
+                            } else {
+                                cmul2(xlr, xli, cr, ci);
+                            }
+                            if (i + 1 < H) pre.set(i + 1, make_float4(xlr.x, xlr.y, xli.x, xli.y));
+                        }
+                        {
+                            const int j = H + i;
+                            float2 cr, ci;
+                            col(j, cr, ci);
+                            if (i == 0) {
+                                xhr = cr;
+                                xhi = ci;
+                            } else {
+                                cmul2(xhr, xhi, cr, ci);
+                            }
+                            if (j + 1 < NC) pre.set(j + 1, make_float4(xhr.x, xhr.y, xhi.x, xhi.y));
+                        }
+                    }
+                    float2 shr = __fmul2_rn(w2, xlr), shi = __fmul2_rn(w2, xli);  // w P_lo
+                    float2 slr = __fmul2_rn(w2, xhr), sli = __fmul2_rn(w2, xhi);  // w P_hi
+#pragma unroll
+                    for (int i = 0; i < NC - H; ++i) {
+                        if (i % LAP64P_G == 0) asm volatile("" ::: "memory");
+                        {
+                            const int l = NC - 1 - i;  // high half, from the top
+                            float2 cr, ci;
+                            col(l, cr, ci);
+                            float2 tr = shr, ti = shi;
+                            if (l > H) {
+                                const float4 p = pre.get(l);
+                                tr = f2(p.x, p.y);
+                                ti = f2(p.z, p.w);
+                                cmul2(tr, ti, shr, shi);
+                            }
+                            float2 q = part.get(l);
+                            q.x = __fadd_rn(q.x, __fadd_rn(tr.x, tr.y));
+                            q.y = __fadd_rn(q.y, __fadd_rn(ti.x, ti.y));
+                            part.set(l, q);
+                            if (l > H || full) cmul2(shr, shi, cr, ci);  // at l = H: w prod of every column
+                        }
+                        if (i < H) {
+                            const int l = H - 1 - i;  // low half, from the top
+                            float2 cr, ci;
+                            col(l, cr, ci);
+                            float2 tr = slr, ti = sli;
+                            if (l > 0) {
+                                const float4 p = pre.get(l);
+                                tr = f2(p.x, p.y);
+                                ti = f2(p.z, p.w);
+                                cmul2(tr, ti, slr, sli);
+                            }
+                            float2 q = part.get(l);
+                            q.x = __fadd_rn(q.x, __fadd_rn(tr.x, tr.y));
+                            q.y = __fadd_rn(q.y, __fadd_rn(ti.x, ti.y));
+                            part.set(l, q);
+                            if (l > 0) cmul2(slr, sli, cr, ci);
+                        }
+                    }
+                    if (full) {
+                        float2 q = part.get(NC);
+                        q.x = __fadd_rn(q.x, __fadd_rn(shr.x, shr.y));
+                        q.y = __fadd_rn(q.y, __fadd_rn(shi.x, shi.y));
+                        part.set(NC, q);
+                    }
+                    if ((u & 15) == 15 || u == pairs - 1) {
+#pragma unroll
+                        for (int l = 0; l <= NC; ++l) {
+                            if (l == NC && !full) continue;
+                            double2 a = acc64.get(l);
+                            const float2 q = part.get(l);
+                            a.x = __dadd_rn(a.x, static_cast<double>(q.x));
+                            a.y = __dadd_rn(a.y, static_cast<double>(q.y));
+                            acc64.set(l, a);
+                            part.set(l, make_float2(0.0f, 0.0f));
+                        }
+                    }
+                }
+                if (seg + 1 < my_R) {  // one-digit step to the next outer position
+                    bool up = false;
+                    const int k = outer_next(pr, st, &up);
+                    const float2 *dd = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) {
+                        sr0[j] = __fadd_rn(sr0[j], dd[j].x);
+                        si0[j] = __fadd_rn(si0[j], dd[j].y);
+                    }
+                    wout = static_cast<float>(outer_weight(pr, st));
+                }
+            }
+        }
+        for (int l = 0; l < n_out; ++l) {
+            double r = 0.0, i = 0.0;
+            if (active) {
+                const double2 a = acc64.get(l);
+                r = a.x;
+                i = a.y;
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                r += __shfl_down_sync(PQG_FULL_MASK, r, off);
+                i += __shfl_down_sync(PQG_FULL_MASK, i, off);
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, ddv{r, 0.0}, ddv{i, 0.0});
+        }
+    }
+}
+
 template <int NC>
 struct LaplaceDfCfg {
     static constexpr size_t smem_bytes = size_t(2 * NC + 1) * PQG_WALK_THREADS * sizeof(float4);

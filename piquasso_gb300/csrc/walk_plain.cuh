@@ -703,4 +703,139 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
     }
 }
 
+// --------------------------------- double-float walk, seeds in shared memory
+// The double-float walk is bound by FP32 instruction issue at two blocks per
+// SM: its seeds take four registers per column (112 at 28 columns).  This
+// variant keeps each lane's seeds in a column-major slice of dynamic shared
+// memory (one float4 {re_hi, re_lo, im_hi, im_lo} per column, stride = the
+// block's threads, so a warp's loads are conflict-free), read once per column
+// and code next to the broadcast prefix-table row, so that more blocks fit an
+// SM: up to 24 columns, four (125 registers, at most 48 KB each), where it
+// measured 489 -> 462 us at n = 24 (FMA pipe 57 -> 65 %).  From 25 columns
+// only three fit the shared memory and it measured no faster than the
+// register-seeded walk, which those tables keep.  Seeding, the one-digit
+// outer updates, the products and the accumulation are the operations of
+// walk_plain<ArDF> in the same order, so the results are bit-identical.
+constexpr int DFS_G = 8;
+template <int NC>
+struct PlainDfsCfg {
+    static constexpr size_t smem_bytes = size_t(NC) * PQG_WALK_THREADS * sizeof(float4);
+};
+
+template <int NC, bool ONES>
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 3) walk_plain_dfs(WalkArgs A) {
+    using Ar = ArDF;
+    using cs_t = Ar::cs_t;
+    extern __shared__ float4 dfs_seed_smem[];
+    float4 *seed = dfs_seed_smem + threadIdx.x;  // column j at seed[j * PQG_WALK_THREADS]
+    const int lane = threadIdx.x & 31;
+    auto seed_get = [&](int j) -> cs_t {
+        const float4 v = seed[j * PQG_WALK_THREADS];
+        return cs_t{dfl{v.x, v.y}, dfl{v.z, v.w}};
+    };
+    for (;;) {
+        const int64_t item = next_item(A.counter, lane);
+        if (item >= A.total_items) return;
+        const int ip = find_problem(A.item_begin, A.n_probs, item);
+        const PqgProblem *pr = A.probs + ip;
+        const int64_t local = item - pr->item_begin;
+        const int64_t R = pr->R;
+        const int64_t Q = pr->Q;
+        const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
+        ddv sr{0.0, 0.0}, si{0.0, 0.0};
+        if (r0 < Q) {
+            OuterState st;
+            outer_decode(pr, r0, st);
+            {
+                // seed_lane<ArDF> column by column (the same additions per column, in order)
+                const float4 *base = reinterpret_cast<const float4 *>(A.arena + pr->off_base_df);
+                const float4 *orow = reinterpret_cast<const float4 *>(A.arena + pr->off_outer_df);
+                for (int j = 0; j < NC; ++j) {
+                    const float4 v = __ldg(base + j);
+                    dfl r{v.x, v.y}, i{v.z, v.w};
+                    for (int o = 0; o < pr->n_outer; ++o) {
+                        const int g = st.g[o];
+                        if (!g) continue;
+                        const float f = -2.0f * static_cast<float>(g);
+                        const float4 w = __ldg(orow + static_cast<int64_t>(o) * NC + j);
+                        r = df_add(r, df_scale(dfl{w.x, w.y}, f));
+                        i = df_add(i, df_scale(dfl{w.z, w.w}, f));
+                    }
+                    seed[j * PQG_WALK_THREADS] = make_float4(r.hi, r.lo, i.hi, i.lo);
+                }
+            }
+            double wout = outer_weight(pr, st);
+            const uint8_t *cm = pr->cm;
+            const bool ones = ONES || pr->cm_max == 1;
+            const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
+            const float4 *D = reinterpret_cast<const float4 *>(A.arena + pr->off_D);
+            const float4 *delta = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin;
+            const int P = pr->P;
+            const int64_t my_R = (Q - r0 < R) ? (Q - r0) : R;
+            for (int64_t seg = 0; seg < my_R; ++seg) {
+                Ar::acc_t acc = Ar::zero();
+                const bool back = (seg & 1) != 0;
+                for (int s = 0; s < P; ++s) {
+                    const int t = back ? P - 1 - s : s;
+                    const float4 *d = delta + static_cast<int64_t>(t) * NC;
+                    // row_product<ArDF>: even and odd columns in two chains
+                    constexpr bool two = NC >= 4;
+                    const cs_t c0 = Ar::sum(seed_get(0), d[0]);
+                    cs_t x = c0, y;
+                    if constexpr (two) y = Ar::sum(seed_get(1), d[1]);
+                    if (ones) {
+#pragma unroll
+                        for (int j = two ? 2 : 1; j < NC; ++j) {
+                            // (a compiler barrier every DFS_G columns bounds the loads in flight)
+                            if (j % DFS_G == 0) asm volatile("" ::: "memory");
+                            const cs_t c = Ar::sum(seed_get(j), d[j]);
+                            if (two && (j & 1))
+                                Ar::mul(y, c);
+                            else
+                                Ar::mul(x, c);
+                        }
+                    } else {
+                        for (int r = 1; r < cm[0]; ++r) Ar::mul(x, c0);
+                        if constexpr (two) {
+                            const cs_t c1 = y;
+                            for (int r = 1; r < cm[1]; ++r) Ar::mul(y, c1);
+                        }
+#pragma unroll
+                        for (int j = two ? 2 : 1; j < NC; ++j) {
+                            const cs_t c = Ar::sum(seed_get(j), d[j]);
+                            for (int r = 0; r < cm[j]; ++r) {
+                                if (two && (j & 1))
+                                    Ar::mul(y, c);
+                                else
+                                    Ar::mul(x, c);
+                            }
+                        }
+                    }
+                    if constexpr (two) Ar::mul(x, y);
+                    Ar::accumulate(acc, x, tab[t]);
+                }
+                Ar::fold(sr, si, acc, wout);
+                if (seg + 1 < my_R) {
+                    bool up = false;
+                    const int k = outer_next(pr, st, &up);
+                    const float4 *dk = D + (2 * k + (up ? 0 : 1)) * NC;
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) {
+                        cs_t c = seed_get(j);
+                        Ar::update(c, dk[j]);
+                        seed[j * PQG_WALK_THREADS] = make_float4(c.r.hi, c.r.lo, c.i.hi, c.i.lo);
+                    }
+                    wout = outer_weight(pr, st);
+                }
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            sr = dd_add(sr, dd_shfl_down(sr, off));
+            si = dd_add(si, dd_shfl_down(si, off));
+        }
+        if (lane == 0) store_partial(A.partials, pr->part_begin + local, sr, si);
+    }
+}
+
 }  // namespace pqg

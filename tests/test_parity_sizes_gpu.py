@@ -75,7 +75,8 @@ def _expected_table(form, arith, unit, nc):
         return "laplace_fp64"
     if arith == "df":
         return "laplace_df_unit" if unit and nc <= 25 else "laplace_df"
-    return "laplace_c64_unit" if unit else "laplace_c64"
+    # unit columns up to 24: the two-code walk over code-pair tables; wider: the general walk
+    return "laplace_c64_unit" if unit and nc <= 24 else "laplace_c64"
 
 
 def _column_counts(form, arith, unit):
