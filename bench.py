@@ -48,6 +48,15 @@ TRAFFIC_N28_DF = 528128
 TRAFFIC_N28_DF_DATE = "2026-12-04"
 
 
+def hbm_gbs():
+    """Measured HBM copy bandwidth of the GB300s (GB/s), or None."""
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def flops_all_ones(n):
     return 2.0 ** (n - 1) * (10 * n + 4)
 
@@ -526,7 +535,9 @@ def bench_training(args):
     fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))  # noqa: E731
     vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     times = []
-    for _ in range(6):
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > L2 (129 MB): cold operands
+    for _ in range(8):
+        flush.zero_()
         e0.record()
         st = L.pqg_mlp_gemm_tc(vp(A), 256, vp(mlp.WbT[1]), 256, rows, 256, 256, 1, fp(C), vp(Cb), fp(mlp.b[1]),
                                None, None, 0, None)
@@ -534,13 +545,16 @@ def bench_training(args):
         torch.cuda.synchronize()
         assert st == 0
         times.append(e0.elapsed_time(e1))
-    gms = float(np.median(times[2:]))
+    gms = float(np.median(times[3:]))
     flops = 2.0 * rows * 256 * 256
     moved = rows * 256 * 2 + 256 * 256 * 2 + rows * 256 * (4 + 2)
     return {"workload": "Adam steps on 65536-row batches of the 16->256->256->256->8 MLP (BF16, FP32 accumulation)",
             "step_ms": step_ms, "rows_per_s": rows / (step_ms * 1e-3),
             "forward_gemm": {"shape": [rows, 256, 256], "ms": gms, "tflops": flops / (gms * 1e-3) / 1e12,
                              "gb_per_s": moved / (gms * 1e-3) / 1e9,
+                             "hbm_frac": moved / (gms * 1e-3) / 1e9 / hbm_gbs() if hbm_gbs() else None,
+                             "l2": "flushed before each launch (256 MB write)",
+                             "kernel": "persistent (65536 rows >= 2 x SMs tiles): B resident, two TMEM accumulators",
                              "note": "memory-bound at this shape: 64 flop/byte of operands and outputs"}}
 
 
@@ -750,7 +764,9 @@ def run_ours(args, world, rank, local, pg):
 def profile_case(name):
     """Small named cases for ncu captures (no JSON line): each runs its kernel
     a few times after building the engine.
-      gemm16k    — the tcgen05 forward GEMM, 16384 x 256 x 256, bias + GELU, 6 launches;
+      gemm16k    — the tcgen05 forward GEMM, 16384 x 256 x 256, bias + GELU, 6 launches
+                   (one 128-row tile per CTA);
+      gemm65k    — the same at 65536 rows, the benchmarked shape (the persistent kernel);
       target1024 — 1024 complex64 permanents of learned-proposal patterns at
                    n=24, d=48 (one Metropolis block's targets), 3 calls;
       laplace24  — 1024 complex64 Laplace permanents shaped like the exact
@@ -773,9 +789,9 @@ def profile_case(name):
     import piquasso_gb300 as pge
     from piquasso_gb300 import _lib, metropolis, proposal, workloads
 
-    if name == "gemm16k":
+    if name in ("gemm16k", "gemm65k"):
         L = _lib.load()
-        rows = 16384
+        rows = 16384 if name == "gemm16k" else 65536
         g = torch.Generator(device="cuda").manual_seed(0)
         A = torch.randn(rows, 256, device="cuda", generator=g).to(torch.bfloat16)
         B = torch.randn(256, 256, device="cuda", generator=g).to(torch.bfloat16)

@@ -83,6 +83,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 // Bounded wait for the phase with the given parity; false when it ran out.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     for (long long i = 0; i < TC_WAIT_LIMIT; ++i) {
@@ -173,6 +177,90 @@ __device__ __forceinline__ float gelu_grad(float x) {
     const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
     const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
     return cdf + x * pdf;
+}
+
+// One group of 32 (or a last 16) accumulator columns of a warp's 32 rows
+// (row `lane` of the group in v): through the padded 32 x 33 `tile` so that
+// the stores write whole row segments, then the fused epilogue.  rows_base:
+// the global row of the warp's first row; col0: the group's first column.
+__device__ __forceinline__ void epilogue_group(const TcArgs &g, float *tile, const float (&v)[32], int ncol,
+                                               int64_t rows_base, int64_t col0, float *cbase, bool vec_ok,
+                                               int lane) {
+    for (int q = 0; q < ncol; ++q) tile[lane * 33 + q] = v[q];
+    __syncwarp();
+    if (ncol == 32 && vec_ok && rows_base + 32 <= g.M && col0 + 32 <= g.N) {
+        // a whole 32 x 32 group: lane takes column quad q = lane % 8 of rows
+        // lane / 8, + 4, ..., + 28 (the same operations per element as below,
+        // with the column, its bias and the row stride fixed per lane)
+        const int q = lane & 7, r0 = lane >> 3;
+        const int64_t col = col0 + 4 * q;
+        float4 bb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) bb = *reinterpret_cast<const float4 *>(g.bias + col);
+        int64_t at = (rows_base + r0) * g.N + col;
+        const int64_t step = 4 * g.N;
+#pragma unroll 2
+        for (int r = r0; r < 32; r += 4, at += step) {
+            float x[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) x[k] = tile[r * 33 + 4 * q + k];
+            if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) {
+                x[0] += bb.x, x[1] += bb.y, x[2] += bb.z, x[3] += bb.w;
+            } else if (g.epi == TC_EPI_DGELU) {
+                const float4 p = *reinterpret_cast<const float4 *>(g.pre + at);
+                x[0] *= gelu_grad(p.x), x[1] *= gelu_grad(p.y), x[2] *= gelu_grad(p.z), x[3] *= gelu_grad(p.w);
+            }
+            *reinterpret_cast<float4 *>(cbase + at) = make_float4(x[0], x[1], x[2], x[3]);
+            if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_DGELU) {
+                const bool act = g.epi == TC_EPI_BIAS_GELU;
+                __nv_bfloat162 lo2 = __floats2bfloat162_rn(act ? gelu(x[0]) : x[0], act ? gelu(x[1]) : x[1]);
+                __nv_bfloat162 hi2 = __floats2bfloat162_rn(act ? gelu(x[2]) : x[2], act ? gelu(x[3]) : x[3]);
+                uint2 w;
+                w.x = *reinterpret_cast<uint32_t *>(&lo2);
+                w.y = *reinterpret_cast<uint32_t *>(&hi2);
+                *reinterpret_cast<uint2 *>(g.Cb + at) = w;
+            }
+        }
+        return;
+    }
+    const int nquad = ncol / 4;
+    for (int idx = lane; idx < 32 * nquad; idx += 32) {
+        const int r = idx / nquad, q = idx - r * nquad;
+        const int64_t row = rows_base + r;
+        const int64_t col = col0 + 4 * q;
+        if (row >= g.M || col >= g.N) continue;
+        float x[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = tile[r * 33 + 4 * q + k];
+        const int64_t at = row * g.N + col;
+        if (vec_ok && col + 3 < g.N) {
+            if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) {
+                const float4 bb = *reinterpret_cast<const float4 *>(g.bias + col);
+                x[0] += bb.x, x[1] += bb.y, x[2] += bb.z, x[3] += bb.w;
+            } else if (g.epi == TC_EPI_DGELU) {
+                const float4 p = *reinterpret_cast<const float4 *>(g.pre + at);
+                x[0] *= gelu_grad(p.x), x[1] *= gelu_grad(p.y), x[2] *= gelu_grad(p.z), x[3] *= gelu_grad(p.w);
+            }
+            *reinterpret_cast<float4 *>(cbase + at) = make_float4(x[0], x[1], x[2], x[3]);
+            if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_DGELU) {
+                const bool act = g.epi == TC_EPI_BIAS_GELU;
+                __nv_bfloat162 lo2 = __floats2bfloat162_rn(act ? gelu(x[0]) : x[0], act ? gelu(x[1]) : x[1]);
+                __nv_bfloat162 hi2 = __floats2bfloat162_rn(act ? gelu(x[2]) : x[2], act ? gelu(x[3]) : x[3]);
+                uint2 w;
+                w.x = *reinterpret_cast<uint32_t *>(&lo2);
+                w.y = *reinterpret_cast<uint32_t *>(&hi2);
+                *reinterpret_cast<uint2 *>(g.Cb + at) = w;
+            }
+        } else {
+            for (int k = 0; k < 4 && col + k < g.N; ++k) {
+                float y = x[k];
+                if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) y += g.bias[col + k];
+                if (g.epi == TC_EPI_DGELU) y *= gelu_grad(g.pre[at + k]);
+                cbase[at + k] = y;
+                if (g.epi == TC_EPI_BIAS_GELU) g.Cb[at + k] = __float2bfloat16(gelu(y));
+                if (g.epi == TC_EPI_DGELU) g.Cb[at + k] = __float2bfloat16(y);
+            }
+        }
+    }
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -279,47 +367,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                 for (int q = 0; q < 16; ++q) v[q] = h[q];
             }
-            for (int q = 0; q < ncol; ++q) tile[lane * 33 + q] = v[q];
-            __syncwarp();
-            const int nquad = ncol / 4;
-            for (int idx = lane; idx < 32 * nquad; idx += 32) {
-                const int r = idx / nquad, q = idx - r * nquad;
-                const int64_t row = m0 + warp * 32 + r;
-                const int64_t col = n0 + j0 + 4 * q;
-                if (row >= g.M || col >= g.N) continue;
-                float x[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) x[k] = tile[r * 33 + 4 * q + k];
-                const int64_t at = row * g.N + col;
-                if (vec_ok && col + 3 < g.N) {
-                    if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) {
-                        const float4 bb = *reinterpret_cast<const float4 *>(g.bias + col);
-                        x[0] += bb.x, x[1] += bb.y, x[2] += bb.z, x[3] += bb.w;
-                    } else if (g.epi == TC_EPI_DGELU) {
-                        const float4 p = *reinterpret_cast<const float4 *>(g.pre + at);
-                        x[0] *= gelu_grad(p.x), x[1] *= gelu_grad(p.y), x[2] *= gelu_grad(p.z), x[3] *= gelu_grad(p.w);
-                    }
-                    *reinterpret_cast<float4 *>(cbase + at) = make_float4(x[0], x[1], x[2], x[3]);
-                    if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_DGELU) {
-                        const bool act = g.epi == TC_EPI_BIAS_GELU;
-                        __nv_bfloat162 lo2 = __floats2bfloat162_rn(act ? gelu(x[0]) : x[0], act ? gelu(x[1]) : x[1]);
-                        __nv_bfloat162 hi2 = __floats2bfloat162_rn(act ? gelu(x[2]) : x[2], act ? gelu(x[3]) : x[3]);
-                        uint2 w;
-                        w.x = *reinterpret_cast<uint32_t *>(&lo2);
-                        w.y = *reinterpret_cast<uint32_t *>(&hi2);
-                        *reinterpret_cast<uint2 *>(g.Cb + at) = w;
-                    }
-                } else {
-                    for (int k = 0; k < 4 && col + k < g.N; ++k) {
-                        float y = x[k];
-                        if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) y += g.bias[col + k];
-                        if (g.epi == TC_EPI_DGELU) y *= gelu_grad(g.pre[at + k]);
-                        cbase[at + k] = y;
-                        if (g.epi == TC_EPI_BIAS_GELU) g.Cb[at + k] = __float2bfloat16(gelu(y));
-                        if (g.epi == TC_EPI_DGELU) g.Cb[at + k] = __float2bfloat16(y);
-                    }
-                }
-            }
+            epilogue_group(g, tile, v, ncol, m0 + warp * 32, n0 + j0, cbase, vec_ok, lane);
             __syncwarp();  // the tile is rewritten by the next group
         }
     }
@@ -327,6 +375,182 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols) : "memory");
+}
+
+// Persistent form of gemm_tc for the network's hidden-layer shapes: N <= 256
+// (one column tile), K <= 256, and many 128-row tiles.  One CTA per SM walks
+// the row tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The whole B operand
+// (BN x K, at most 128 KB) is loaded once per CTA and stays in shared memory;
+// A streams through a ring of PT_STAGES 16 KB stages.  Warp roles:
+//   warp 0  TMA producer: B once, then A chunk by chunk, each stage refilled
+//           once the MMAs that read it have completed (empty barrier);
+//   warp 1  MMA issuer and TMEM owner: two accumulators of tmem_cols columns
+//           (the whole 512-column TMEM at BN = 256), so that the epilogue of
+//           tile i reads one accumulator while the MMAs of tile i + 1 fill the
+//           other; tcgen05.commit signals a stage's release and an
+//           accumulator's completion;
+//   warps 2-9  epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
+//           lane quarter its position allows), i.e. those rows of the tile;
+//           the two warps of a quarter take alternate 32-column groups.  Each
+//           applies the same epilogue as gemm_tc (epilogue_group) and hands
+//           the accumulator back (one arrival per warp).  Eight warps keep
+//           the stores and the GELU's latencies overlapped.
+// The MMAs of a tile accumulate the K chunks in gemm_tc's order and the
+// epilogue performs the same operations, so the results are identical bit for
+// bit.  Every wait is bounded; a wait that runs out records an error code, the
+// waiting role stops, and the others then run out too; before the CTA frees
+// its TMEM the producer waits for the copies it issued and the issuer for its
+// MMAs.
+constexpr int PT_STAGES = 4;
+constexpr int PT_EPI_WARPS = 8;
+constexpr int PT_THREADS = 32 * (2 + PT_EPI_WARPS);
+
+__global__ void __launch_bounds__(PT_THREADS, 1)
+    gemm_tc_persistent(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                       TcArgs g) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    const uint32_t raw = smem_u32(tc_smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    const int nkc = static_cast<int>((g.K + TC_BK - 1) / TC_BK);  // K chunks (<= 4)
+    const uint32_t b_chunk = static_cast<uint32_t>(g.BN) * TC_BK * 2;
+    const uint32_t sB = base;                                       // nkc chunks of BN x 64
+    const uint32_t sA = sB + static_cast<uint32_t>(nkc) * b_chunk;  // PT_STAGES x 16 KB
+    const uint32_t sT = sA + PT_STAGES * TC_A_BYTES;  // PT_EPI_WARPS x (32 x 33) floats, the epilogue tiles
+    const uint32_t bars = sT + PT_EPI_WARPS * 32 * 33 * 4;
+    // barriers: bfull | full[S] | empty[S] | tfull[2] | tempty[2] | done
+    const uint32_t bfull = bars, full0 = bars + 8, empty0 = full0 + 8 * PT_STAGES, tfull0 = empty0 + 8 * PT_STAGES,
+                   tempty0 = tfull0 + 16, done = tempty0 + 16;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem_raw + (done + 8 - raw));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t n_tiles = (g.M + TC_BM - 1) / TC_BM;
+
+    if (tid == 0) {
+        mbar_init(bfull, 1);
+        for (int s = 0; s < PT_STAGES; ++s) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull0 + 8 * a, 1);
+            mbar_init(tempty0 + 8 * a, PT_EPI_WARPS);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(2 * g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            mbar_expect_tx(bfull, static_cast<uint32_t>(nkc) * b_chunk);
+            for (int kc = 0; kc < nkc; ++kc) tma_load_2d(sB + kc * b_chunk, &map_b, kc * TC_BK, 0, bfull);
+            uint32_t it = 0;
+            bool ok = true;
+            for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+                for (int kc = 0; kc < nkc; ++kc, ++it) {
+                    const uint32_t s = it % PT_STAGES, use = it / PT_STAGES;
+                    if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1)) {
+                        record_error(5);
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(full0 + 8 * s, TC_A_BYTES);
+                    tma_load_2d(sA + s * TC_A_BYTES, &map_a, kc * TC_BK, static_cast<int32_t>(tile * TC_BM),
+                                full0 + 8 * s);
+                }
+            }
+            // every copy issued has landed before the CTA can leave
+            for (uint32_t k = it > PT_STAGES ? it - PT_STAGES : 0; k < it; ++k)
+                if (!mbar_wait(full0 + 8 * (k % PT_STAGES), (k / PT_STAGES) & 1)) record_error(6);
+            if (!mbar_wait(bfull, 0)) record_error(6);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(g.BN);
+            bool ok = mbar_wait(bfull, 0);
+            if (!ok) record_error(7);
+            uint32_t it = 0, tl = 0;
+            for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++tl) {
+                const uint32_t a = tl & 1, use = tl >> 1;
+                if (use > 0 && !mbar_wait(tempty0 + 8 * a, (use - 1) & 1)) {
+                    record_error(8);
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + a * static_cast<uint32_t>(g.tmem_cols);
+                for (int kc = 0; kc < nkc; ++kc, ++it) {
+                    const uint32_t s = it % PT_STAGES;
+                    if (!mbar_wait(full0 + 8 * s, (it / PT_STAGES) & 1)) {
+                        record_error(9);
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t sa = sA + s * TC_A_BYTES, sb = sB + kc * b_chunk;
+                    const int64_t kcols = g.K - static_cast<int64_t>(kc) * TC_BK;
+                    const int nk = kcols >= TC_BK ? TC_BK / 16 : static_cast<int>((kcols + 15) / 16);
+                    for (int kk = 0; kk < nk; ++kk)
+                        umma_bf16(acc, sdesc_sw128(sa + 32u * kk), sdesc_sw128(sb + 32u * kk), idesc,
+                                  (kc > 0 || kk > 0) ? 1 : 0);
+                    umma_commit(empty0 + 8 * s);
+                }
+                if (!ok) break;
+                umma_commit(tfull0 + 8 * a);
+            }
+            umma_commit(done);  // arrives when every MMA issued above has completed
+            if (!mbar_wait(done, 0)) record_error(10);
+        }
+    } else {
+        // epilogue warps: TMEM lane quarter q, rows 32 q .. 32 q + 31 of each
+        // tile; column groups h, h + 2, ... of 32 columns
+        const int q = warp & 3, h = (warp - 2) / 4;
+        float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * 32 * 33;
+        const bool vec_ok = (g.N % 4) == 0;
+        uint32_t tl = 0;
+        for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++tl) {
+            const uint32_t a = tl & 1, use = tl >> 1;
+            // warp-uniform: the TMEM loads below are .sync.aligned
+            const bool have = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, use & 1));
+            if (!have) {
+                if (lane == 0) record_error(11);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t taddr =
+                tmem + a * static_cast<uint32_t>(g.tmem_cols) + (static_cast<uint32_t>(q * 32) << 16);
+            for (int j0 = 32 * h; j0 < g.BN; j0 += 64) {
+                const int ncol = g.BN - j0 >= 32 ? 32 : 16;
+                float v[32];
+                if (ncol == 32) {
+                    tmem_ld32(taddr + static_cast<uint32_t>(j0), v);
+                } else {
+                    float hv[16];
+                    tmem_ld16(taddr + static_cast<uint32_t>(j0), hv);
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) v[k] = hv[k];
+                }
+                epilogue_group(g, tile_f, v, ncol, tile * TC_BM + q * 32, j0, g.C, vec_ok, lane);
+                __syncwarp();  // the tile is rewritten by the next group
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty0 + 8 * a);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * g.tmem_cols)
+                     : "memory");
 }
 
 // dst[c][r] = src[r][c] for BF16 matrices (32 x 32 tiles through shared memory).
@@ -583,6 +807,19 @@ int fail_cuda(cudaError_t e, const char *what) {
     return PQG_ERR_CUDA;
 }
 
+// SM count of the current device (0 if it cannot be read), looked up once.
+int device_sms() {
+    static std::once_flag once;
+    static int sms = 0;
+    std::call_once(once, [] {
+        int dev = 0, n = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            sms = n;
+    });
+    return sms;
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static std::once_flag once;
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -676,6 +913,24 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
     });
     if (attr_err != cudaSuccess) return fail_cuda(attr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // many row tiles of one column tile with the whole B in shared memory:
+    // the persistent kernel, one CTA per SM
+    const int64_t row_tiles = (M + TC_BM - 1) / TC_BM;
+    const int sms = device_sms();
+    if (epilogue != TC_EPI_SPLITK && N <= 256 && K <= 256 && sms > 0 && row_tiles >= 2 * sms) {
+        const size_t psmem = 1024 + static_cast<size_t>((K + TC_BK - 1) / TC_BK) * g.BN * TC_BK * 2 +
+                             PT_STAGES * static_cast<size_t>(TC_A_BYTES) + PT_EPI_WARPS * 32 * 33 * 4 + 128;
+        static std::once_flag pattr_once;
+        static cudaError_t pattr_err = cudaSuccess;
+        std::call_once(pattr_once, [] {
+            pattr_err = cudaFuncSetAttribute(gemm_tc_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             227 * 1024);
+        });
+        if (pattr_err != cudaSuccess) return fail_cuda(pattr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
+        gemm_tc_persistent<<<static_cast<unsigned>(sms), PT_THREADS, psmem, s>>>(ma, mb, g);
+        cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_gemm_tc");
+    }
     dim3 grid(static_cast<unsigned>((N + g.BN - 1) / g.BN), static_cast<unsigned>((M + TC_BM - 1) / TC_BM),
               static_cast<unsigned>(nsplit));
     gemm_tc<<<grid, TC_THREADS, smem, s>>>(ma, mb, g);

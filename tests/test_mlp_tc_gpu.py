@@ -147,3 +147,36 @@ def test_bias_grad(L, M, N):
     assert L.pqg_mlp_bias_grad(_f(d), M, N, _f(db2), _f(part), None) == 0
     torch.cuda.synchronize()
     assert torch.equal(db, db2)  # deterministic
+
+
+@pytest.mark.parametrize("M,N,K", [(65536, 256, 256), (40000, 256, 16), (50001, 48, 200), (39000, 8, 256)])
+@pytest.mark.parametrize("epi", [0, 1, 4])
+def test_persistent_kernel_is_bitwise_the_tile_kernel(L, M, N, K, epi):
+    """From 2 x SMs row tiles on (K <= 256, N <= 256, no split-K) the GEMM runs
+    as the persistent kernel (B resident in shared memory, two TMEM
+    accumulators).  The same rows computed as blocks of 16384 (below that
+    threshold: one tile per CTA) must give the same bits, in every output of
+    the epilogue; and the result against the FP32 reference as above."""
+    import torch
+
+    A, B, ref, scale = _operands(torch, M, N, K, M + 3 * epi)
+    bias = torch.randn(N, device="cuda")
+    pre = torch.randn(M, N, device="cuda")
+    outs = []
+    for blocks in (False, True):
+        C = torch.full((M, N), float("nan"), device="cuda")
+        Cb = torch.zeros(M, N, device="cuda", dtype=torch.bfloat16)
+        step = 16384 if blocks else M
+        for r0 in range(0, M, step):
+            m = min(step, M - r0)
+            a = A[r0:r0 + m]
+            assert L.pqg_mlp_gemm_tc(_v(a), K, _v(B), K, m, N, K, epi, _f(C[r0:r0 + m]),
+                                     _v(Cb[r0:r0 + m]) if epi else None, _f(bias) if epi == 1 else None,
+                                     _f(pre[r0:r0 + m]) if epi == 4 else None, None, 0, None) == 0
+        torch.cuda.synchronize()
+        assert _status(L) == 0
+        outs.append((C, Cb))
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert torch.equal(outs[0][1], outs[1][1])
+    if epi == 0:
+        assert torch.all((outs[0][0] - ref).abs() <= 1e-5 * scale + 1e-6)
