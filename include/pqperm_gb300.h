@@ -251,7 +251,10 @@ int pqg_last_walk_kernel(int32_t *table, int32_t *n_cols);
  * pqg_mlp_gemm_tc: C[M x N] = A[M x K] . B[N x K]^T with BF16 operands, both
  * row-major with K contiguous (row strides lda, ldb >= K, multiples of 8;
  * 16-byte aligned base pointers), FP32 accumulation on the tcgen05 tensor
- * cores (TMA-staged operands, TMEM accumulator).  epilogue 0: C = acc; 1: C =
+ * cores (TMA-staged operands, TMEM accumulator).  With N <= 256, K <= 256,
+ * no split-K and at least two 128-row tiles per SM, a persistent kernel runs
+ * instead (one CTA per SM, B resident in shared memory, two TMEM
+ * accumulators); its results are bit-identical.  epilogue 0: C = acc; 1: C =
  * acc + bias (pre-activation), c_bf16 = GELU(C); 2: split-K over `splits`
  * ranges of K through `splitk_scratch` (splits*M*N floats), then a fixed-order
  * sum into C (weight gradients); 3: C = acc + bias; 4: C = acc * GELU'(pre)

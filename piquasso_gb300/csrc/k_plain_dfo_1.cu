@@ -1,14 +1,14 @@
-// Walk-kernel instantiations (double-float; 17..24 columns keep their seeds in shared memory, four blocks per SM) (all-ones columns), column counts 17..32 (generated list).
+// Walk-kernel instantiations (double-float; 21..24 columns keep their seeds in shared memory, four blocks per SM) (all-ones columns), column counts 17..32 (generated list).
 #include "walk_plain.cuh"
 #include "kernel_table.h"
 
 namespace pqg {
 
 const KernelInfo k_plain_dfo_1[16] = {
-    {reinterpret_cast<const void *>(&walk_plain_dfs<17, true>), PlainDfsCfg<17>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_plain_dfs<18, true>), PlainDfsCfg<18>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_plain_dfs<19, true>), PlainDfsCfg<19>::smem_bytes},
-    {reinterpret_cast<const void *>(&walk_plain_dfs<20, true>), PlainDfsCfg<20>::smem_bytes},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 17, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 18, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 19, true>), 0},
+    {reinterpret_cast<const void *>(&walk_plain<ArDF, 20, true>), 0},
     {reinterpret_cast<const void *>(&walk_plain_dfs<21, true>), PlainDfsCfg<21>::smem_bytes},
     {reinterpret_cast<const void *>(&walk_plain_dfs<22, true>), PlainDfsCfg<22>::smem_bytes},
     {reinterpret_cast<const void *>(&walk_plain_dfs<23, true>), PlainDfsCfg<23>::smem_bytes},

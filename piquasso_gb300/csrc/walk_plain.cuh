@@ -711,9 +711,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
 // block's threads, so a warp's loads are conflict-free), read once per column
 // and code next to the broadcast prefix-table row, so that more blocks fit an
 // SM: up to 24 columns, four (125 registers, at most 48 KB each), where it
-// measured 489 -> 462 us at n = 24 (FMA pipe 57 -> 65 %).  From 25 columns
-// only three fit the shared memory and it measured no faster than the
-// register-seeded walk, which those tables keep.  Seeding, the one-digit
+// measured 489 -> 462 us at n = 24 (FMA pipe 57 -> 65 %).  The tables use it
+// for 21..24 columns: from 25 columns only three blocks fit the shared
+// memory and it measured no faster, and on the 4096-pattern batch of 20
+// columns the register-seeded walk tuned (12.00 ms) beat it tuned (12.63 ms).  Seeding, the one-digit
 // outer updates, the products and the accumulation are the operations of
 // walk_plain<ArDF> in the same order, so the results are bit-identical.
 constexpr int DFS_G = 8;
