@@ -381,8 +381,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // (one column tile), K <= 256, and many 128-row tiles.  One CTA per SM walks
 // the row tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The whole B operand
 // (BN x K, at most 128 KB) is loaded once per CTA and stays in shared memory;
-// A streams through a ring of PT_STAGES 16 KB stages (two: the MMAs are far
-// from the bottleneck, and the epilogue warps' staging tiles need the room).  Warp roles:
+// A streams through PT_STAGES 16 KB stages (one: a tile's four chunk loads
+// take a few microseconds, well inside the epilogue of the other
+// accumulator's tile, and the epilogue warps' staging tiles need the room).  Warp roles:
 //   warp 0  TMA producer: B once, then A chunk by chunk, each stage refilled
 //           once the MMAs that read it have completed (empty barrier);
 //   warp 1  MMA issuer and TMEM owner: two accumulators of tmem_cols columns
@@ -390,11 +391,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //           tile i reads one accumulator while the MMAs of tile i + 1 fill the
 //           other; tcgen05.commit signals a stage's release and an
 //           accumulator's completion;
-//   warps 2-13  epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
+//   warps 2-17  epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
 //           lane quarter its position allows), i.e. those rows of the tile;
-//           the three warps of a quarter take every third 32-column group.
+//           the four warps of a quarter take every fourth 32-column group.
 //           Each applies the same epilogue as gemm_tc (epilogue_group) and
-//           hands the accumulator back (one arrival per warp).  Twelve warps
+//           hands the accumulator back (one arrival per warp).  Sixteen warps
 //           keep the stores and the GELU's latencies overlapped.
 // The MMAs of a tile accumulate the K chunks in gemm_tc's order and the
 // epilogue performs the same operations, so the results are identical bit for
@@ -402,8 +403,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // waiting role stops, and the others then run out too; before the CTA frees
 // its TMEM the producer waits for the copies it issued and the issuer for its
 // MMAs.
-constexpr int PT_STAGES = 2;
-constexpr int PT_EPI_WARPS = 12;
+constexpr int PT_STAGES = 1;
+constexpr int PT_EPI_WARPS = 16;
 constexpr int PT_THREADS = 32 * (2 + PT_EPI_WARPS);
 
 __global__ void __launch_bounds__(PT_THREADS, 1)
