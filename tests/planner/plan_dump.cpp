@@ -65,10 +65,12 @@ int main() {
     const unsigned char *pb = reinterpret_cast<const unsigned char *>(pl.probs.data());
     for (size_t i = 0; i < pl.probs.size() * sizeof(PqgProblem); ++i) hp = (hp ^ pb[i]) * 1099511628211ull;
     printf("{\"total_items\": %lld, \"total_outputs\": %lld, \"item_group\": %d, \"df_ok\": %d, \"all_ones\": %d, "
+           "\"pairs\": %d, \"total_delta\": %lld, "
            "\"max_nc\": %d, \"arena_bytes\": %lld, \"arena_hash\": \"%016llx\", \"probs_hash\": \"%016llx\", \"out_of\": [",
            static_cast<long long>(pl.total_items), static_cast<long long>(pl.total_outputs), pl.item_group,
-           pl.df_ok ? 1 : 0, pl.all_ones ? 1 : 0, pl.max_nc, static_cast<long long>(pl.arena.size()),
-           static_cast<unsigned long long>(h), static_cast<unsigned long long>(hp));
+           pl.df_ok ? 1 : 0, pl.all_ones ? 1 : 0, pl.pairs ? 1 : 0, static_cast<long long>(pl.total_delta), pl.max_nc,
+           static_cast<long long>(pl.arena.size()), static_cast<unsigned long long>(h),
+           static_cast<unsigned long long>(hp));
     for (size_t b = 0; b < pl.out_of.size(); ++b) printf("%s%lld", b ? ", " : "", static_cast<long long>(pl.out_of[b]));
     printf("], \"item_begin\": [");
     for (size_t i = 0; i < pl.item_begin.size(); ++i)
@@ -78,10 +80,11 @@ int main() {
         const PqgProblem &q = pl.probs[i];
         printf("%s{\"index\": %d, \"kind\": %d, \"n_out\": %d, \"out_index\": %lld, \"item_begin\": %lld, "
                "\"n_items\": %lld, \"P\": %d, \"K\": %d, \"n_outer\": %d, \"Q\": %lld, \"R\": %lld, \"nc\": %d, "
-               "\"S\": %.17g}",
+               "\"delta_begin\": %lld, \"S\": %.17g}",
                i ? ", " : "", q.index, q.kind, q.n_out, static_cast<long long>(q.out_index),
                static_cast<long long>(q.item_begin), static_cast<long long>(q.n_items), q.P, q.K, q.n_outer,
-               static_cast<long long>(q.Q), static_cast<long long>(q.R), q.nc, pl.pending[q.index].S);
+               static_cast<long long>(q.Q), static_cast<long long>(q.R), q.nc, static_cast<long long>(q.delta_begin),
+               pl.pending[q.index].S);
     }
     printf("]}\n");
     return 0;

@@ -191,3 +191,36 @@ def test_threaded_planning_reports_the_first_bad_problem(planner, monkeypatch):
     monkeypatch.setenv("PQG_HOST_THREADS", "4")
     bad = planner(C128, 0, R, C)
     assert bad["error"] == 1 and bad["problem"] == 2100
+
+
+def test_code_pair_tables(planner):
+    """complex64 Laplace plans whose walk problems all have unit columns (up
+    to 24 of them) store their prefix tables as code pairs for the two-code
+    walk: each problem's table holds an even number of codes (an odd P gets a
+    pad code), so every table starts at an even slot and the float4 pair
+    rows stay aligned; any other plan keeps P codes per problem."""
+    rng = np.random.default_rng(7)
+    d, n = 30, 12
+    inp = np.array([1] * n + [0] * (d - n))
+    rows = np.stack([np.bincount(rng.integers(0, d, n - 1), minlength=d) for _ in range(40)])
+    plan = planner(C64, 1, rows, inp)
+    assert plan["pairs"] == 1
+    walk = [p for p in plan["probs"] if p["kind"] == 0]
+    assert any(p["P"] % 2 for p in walk)  # odd tables occur and get padded
+    total = 0
+    for p in sorted(walk, key=lambda p: p["delta_begin"]):
+        assert p["delta_begin"] == total and p["delta_begin"] % 2 == 0
+        total += (p["P"] + p["P"] % 2) * p["nc"]
+    assert plan["total_delta"] == total
+    # a repeated column, more than 24 columns, another arithmetic or the plain form: no pairs
+    inp2 = inp.copy()
+    inp2[0] = 2
+    rows2 = rows.copy()
+    rows2[:, 0] += 1
+    assert planner(C64, 1, rows2, inp2)["pairs"] == 0
+    wide = np.array([1] * 26 + [0] * 4)
+    rows3 = np.stack([np.bincount(rng.integers(0, d, 25), minlength=d) for _ in range(4)])
+    assert planner(C64, 1, rows3, wide)["pairs"] == 0
+    assert planner(C128, 1, rows, inp)["pairs"] == 0
+    assert planner(C64, 0, np.stack([np.bincount(rng.integers(0, d, n), minlength=d) for _ in range(4)]),
+                   inp)["pairs"] == 0
