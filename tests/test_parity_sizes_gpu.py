@@ -126,18 +126,26 @@ def _oracle(form, A, rows, cols):
 def test_every_walk_instantiation_matches_oracle(engine, monkeypatch, form, arith, unit):
     from piquasso_gb300 import _lib
 
-    for nc in _column_counts(form, arith, unit):
+    cases = [(nc, False) for nc in _column_counts(form, arith, unit)]
+    if form == "laplace" and unit:
+        # unit columns beside a zero-multiplicity column (the exact sampler's
+        # steps): the walk's extra output shared by the zero columns
+        cases += [(nc, True) for nc in _column_counts(form, arith, unit)]
+    for nc, zero_col in cases:
         A, rows, cols = _case(form, nc, unit, seed=1000 + nc)
+        if zero_col:
+            cols = np.append(cols, 0)
+            A = haar_unitary(len(cols) + len(rows), 2000 + nc)[: len(rows), : len(cols)].copy()
         n_factors = int(cols.sum())
         rel, absf = (1e-5, (n_factors + 2) * 2.0 ** -24) if arith == "c64" else TOL128
         A, got = _run(engine, monkeypatch, form, arith, A, rows, cols)
         table, ran_nc = _lib.last_walk_kernel()
-        assert (table, ran_nc) == (_expected_table(form, arith, unit, nc), nc), (form, arith, unit, nc)
+        assert (table, ran_nc) == (_expected_table(form, arith, unit, nc), nc), (form, arith, unit, nc, zero_col)
         want, scale = _oracle(form, A, rows, cols)
         assert got.shape == want.shape, (nc, got.shape, want.shape)
         tol = np.maximum(rel * np.abs(want), absf * scale)
         err = np.abs(got - want)
-        assert np.all(err <= tol), (form, arith, unit, nc, float(np.max(err / tol)))
+        assert np.all(err <= tol), (form, arith, unit, nc, zero_col, float(np.max(err / tol)))
 
 
 def _leading_block(n):
