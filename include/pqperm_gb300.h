@@ -234,7 +234,7 @@ int pqg_last_timing(double *walk_ms, double *device_ms, double *steps, double *f
 #define PQG_WALK_LAPLACE_FP64 2      /* FP64 Laplace walk */
 #define PQG_WALK_LAPLACE_C64 3       /* complex64 Laplace walk, repeated columns */
 #define PQG_WALK_PLAIN_DF 4          /* double-float walk, repeated columns */
-#define PQG_WALK_LAPLACE_C64_UNIT 5  /* complex64 Laplace walk, unit columns */
+#define PQG_WALK_LAPLACE_C64_UNIT 5  /* complex64 Laplace walk, unit columns (<= 24; two codes per iteration) */
 #define PQG_WALK_PLAIN_FP64_UNIT 6   /* FP64 walk, unit columns */
 #define PQG_WALK_PLAIN_C64_UNIT 7    /* complex64 walk, unit columns */
 #define PQG_WALK_PLAIN_DF_UNIT 8     /* double-float walk, unit columns */
