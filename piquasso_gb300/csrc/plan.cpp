@@ -478,6 +478,19 @@ void Planner::finish() {
         matrix_off = push_bytes_(a_, static_cast<size_t>(2 * int_nr_ * int_nc_) * sizeof(double));
     }
 
+    // complex64 Laplace plans whose every walk problem has unit columns (the
+    // exact sampler's) store their prefix tables as code pairs for the
+    // two-code walk: each problem's table holds an even number of codes
+    pairs = false;
+    if (prec_ == Precision::C64 && laplace && any_walk && ncmax >= 2 && ncmax <= PQG_PAIRS_MAX_NC) {
+        pairs = true;
+        for (const auto &p : pending) {
+            if (p.kind != PQG_KIND_WALK) continue;
+            for (int k = 0; k < p.nc && pairs; ++k) pairs = p.cm[k] == 1;
+            if (!pairs) break;
+        }
+    }
+
     // Steps per lane: about items_per_smsp warps of work per SM sub-partition
     // for balance, but at least enough steps to amortise the seeding.
     double S_tot = 0.0;
@@ -502,6 +515,8 @@ void Planner::finish() {
     // any tuning)
     if (prec_ == Precision::C64 && !laplace && ncmax >= PQG_SMEM_TABLE_NC_MIN && ncmax <= PQG_SMEM_TABLE_NC_MAX)
         p_max = std::min<int64_t>(p_max, PQG_SMEM_TABLE_P);
+    // likewise the two-code Laplace walk's shared-memory table of code pairs
+    if (pairs) p_max = std::min<int64_t>(p_max, PQG_PAIRS_TABLE_P);
     // per-problem device data (built by the prep kernel), by offset from the
     // start of that region; the region follows the uploaded arena
     auto pdata = [&](int64_t bytes) {
@@ -510,24 +525,13 @@ void Planner::finish() {
         return off;
     };
     const int64_t d_elem = prec_ == Precision::C64 ? 8 : 16;  // one D element: float2, else double2 / float4
-    // items a block takes at once: the complex64 plain walk hands out groups
-    // of PQG_ITEM_GROUP consecutive items (one per warp of a block), so a
-    // block's warps walk one problem's prefix table together and share it in
-    // L1; its problems then come in whole groups of items
-    const int64_t group = (prec_ == Precision::C64 && form_ == Form::PLAIN) ? PQG_ITEM_GROUP : 1;
+    // items a block takes at once: the complex64 plain walk and the two-code
+    // Laplace walk hand out groups of PQG_ITEM_GROUP consecutive items (one
+    // per warp of a block), so a block's warps walk one problem's prefix table
+    // together (staged in shared memory or shared in L1); their problems then
+    // come in whole groups of items
+    const int64_t group = (prec_ == Precision::C64 && (form_ == Form::PLAIN || pairs)) ? PQG_ITEM_GROUP : 1;
     item_group = static_cast<int>(group);
-    // complex64 Laplace plans whose every walk problem has unit columns (the
-    // exact sampler's) store their prefix tables as code pairs for the
-    // two-code walk: each problem's table holds an even number of codes
-    pairs = false;
-    if (prec_ == Precision::C64 && laplace && any_walk && ncmax >= 2 && ncmax <= PQG_PAIRS_MAX_NC) {
-        pairs = true;
-        for (const auto &p : pending) {
-            if (p.kind != PQG_KIND_WALK) continue;
-            for (int k = 0; k < p.nc && pairs; ++k) pairs = p.cm[k] == 1;
-            if (!pairs) break;
-        }
-    }
 
     // Outputs stay in the caller's order; the work runs longest items first.
     // The device queue hands out items in problem order, so the problems are

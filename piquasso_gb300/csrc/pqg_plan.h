@@ -36,6 +36,9 @@
 // complex64 Laplace walks of unit columns up to this count take two inner
 // codes per iteration, from prefix tables stored as code pairs
 #define PQG_PAIRS_MAX_NC 24
+// ... whose block stages the problem's table of at most this many codes in
+// shared memory (a block takes PQG_ITEM_GROUP items of one problem)
+#define PQG_PAIRS_TABLE_P 128
 
 enum PqgProblemKind : int32_t {
     PQG_KIND_WALK = 0,      // Gray-code walk on the device

@@ -402,7 +402,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
 // stay scalar: each column sum is two scalar adds into adjacent registers.
 // The columns are split into two halves, each with its own prefix chain and
 // suffix chain, so every pass runs two independent dependency chains of
-// packed multiplies.  The step weight of each code times the lane's outer
+// packed multiplies.  A block takes four consecutive items of one problem
+// (one per warp) and stages that problem's code-pair table in shared memory
+// (the plan caps P at PQG_PAIRS_TABLE_P codes), so the rows are broadcast
+// shared-memory loads.  The step weight of each code times the lane's outer
 // weight starts the suffix chains (an exact FP32 integer: the sampler's
 // weights stay below 2^24), so both codes add into one FP32 partial sum per
 // output (re_a + re_b, then into the sum), folded into the per-lane FP64
@@ -413,8 +416,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
 // cost a store and a load of a float4 per column).
 template <int NC>
 struct LaplaceC64PCfg {
-    static constexpr size_t smem_bytes = size_t(NC + 1) * PQG_WALK_THREADS * sizeof(float2) +
-                                         size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2);
+    static constexpr int TAB_PAIRS = PQG_PAIRS_TABLE_P / 2;  // code pairs the staged table holds
+    static constexpr size_t smem_bytes = size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) +
+                                         size_t(NC + 1) * PQG_WALK_THREADS * sizeof(float2) +
+                                         size_t(TAB_PAIRS) * NC * sizeof(float4);
 };
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
@@ -423,8 +428,15 @@ constexpr int LAP64P_G = 8;
 template <int NC>
 __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArgs A) {
     static_assert(NC >= 2, "unit-column Laplace walks have at least two columns");
+    static_assert(PQG_ITEM_GROUP * 32 == PQG_WALK_THREADS, "one item per warp of a block");
+    using Cfg = LaplaceC64PCfg<NC>;
     extern __shared__ double2 lap_smem64p[];
     const int lane = threadIdx.x & 31;
+    // the block's problem's code-pair table (at most Cfg::TAB_PAIRS pairs: the plan caps P)
+    float4 *s_tab = reinterpret_cast<float4 *>(lap_smem64p + (NC + 1) * PQG_WALK_THREADS) +
+                    (NC + 1) * PQG_WALK_THREADS / 2;
+    __shared__ unsigned long long s_group;
+    int staged = -1;
     LaneArray<double2, NC + 1, true> acc64;  // per-lane FP64 sums of every output
     acc64.init(lap_smem64p, threadIdx.x);
     LaneArray<float2, NC + 1, true> part;  // per-lane FP32 partial sums {re, im} of every output
@@ -433,10 +445,25 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
     pre.init(nullptr, threadIdx.x);
 
     for (;;) {
-        const int64_t item = next_item(A.counter, lane);
+        // a block takes PQG_ITEM_GROUP consecutive items of one problem at once
+        // (one per warp; the plan makes every problem whole groups), so the
+        // exit is uniform over the block
+        __syncthreads();  // every warp has read the previous group and its table
+        if (threadIdx.x == 0) s_group = atomicAdd(A.counter, 1ULL);
+        __syncthreads();
+        const int64_t item = static_cast<int64_t>(s_group) * PQG_ITEM_GROUP + (threadIdx.x >> 5);
         if (item >= A.total_items) return;
         const int ip = find_problem(A.item_begin, A.n_probs, item);
         const PqgProblem *pr = A.probs + ip;
+        if (ip != staged) {
+            // stage the problem's code-pair table once for the block's warps
+            const float4 *src = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin / 2;
+            const int np = (pr->P + 1) >> 1;
+            const int n = (np < Cfg::TAB_PAIRS ? np : Cfg::TAB_PAIRS) * NC;
+            for (int e = threadIdx.x; e < n; e += PQG_WALK_THREADS) s_tab[e] = src[e];
+            staged = ip;
+            __syncthreads();
+        }
         const int64_t local = item - pr->item_begin;
         const int64_t R = pr->R;
         const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
@@ -460,10 +487,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
             const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
             const float2 *D = reinterpret_cast<const float2 *>(A.arena + pr->off_D);
             const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
-            // code-pair rows (delta_begin is even: every problem's table holds an even count)
-            const float4 *delta = reinterpret_cast<const float4 *>(A.delta) + pr->delta_begin / 2;
             const int P = pr->P;
-            const int pairs = (P + 1) >> 1;
+            // (the staged table holds at most Cfg::TAB_PAIRS pairs: the plan guarantees P
+            // fits; the bound keeps every read inside it)
+            const int pairs = ((P + 1) >> 1) < Cfg::TAB_PAIRS ? ((P + 1) >> 1) : Cfg::TAB_PAIRS;
 #pragma unroll
             for (int l = 0; l <= NC; ++l) {
                 part.set(l, make_float2(0.0f, 0.0f));
@@ -475,7 +502,7 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
                     // step weights times the outer weight (the pad code weighs 0)
                     const float2 w2 = f2(__fmul_rn(__ldg(&tab[ta].wf), wout),
                                          tb < P ? __fmul_rn(__ldg(&tab[tb].wf), wout) : 0.0f);
-                    const float4 *d = delta + static_cast<int64_t>(u) * NC;
+                    const float4 *d = s_tab + u * NC;
                     // (plain loads, which the compiler barriers below order: the suffix
                     // pass reloads its rows rather than keeping the prefix pass's live)
                     auto col = [&](int j, float2 &cr, float2 &ci) {
