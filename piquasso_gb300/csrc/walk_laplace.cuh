@@ -408,16 +408,20 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
 // shared-memory loads.  The step weight of each code times the lane's outer
 // weight starts the suffix chains (an exact FP32 integer: the sampler's
 // weights stay below 2^24), so both codes add into one FP32 partial sum per
-// output (re_a + re_b, then into the sum), folded into the per-lane FP64
-// sums every 16 code pairs.  Prefix products of both codes sit in one float4
-// per column in registers; the per-output FP32 partial sums and the FP64
-// sums in column-major slices of shared memory (a partial sum is read and
-// written once per output per code pair, where shared prefix products would
-// cost a store and a load of a float4 per column).
+// output (re_a + re_b, then into the sum), folded every 16 code pairs into
+// per-lane TwoSum-compensated FP32 sums (value and error word), which the
+// warp's lanes then combine the same way.  No FP64 instruction runs in the
+// walk: on GB300 one FP64 warp instruction holds its pipe for tens of
+// cycles, and an FP64 fold stalled the folding warp while its SMSP had one
+// other warp to issue from.  Prefix products of both codes sit in one
+// float4 per column in registers; the per-output FP32 partial sums and the
+// compensated sums in column-major slices of shared memory (a partial sum
+// is read and written once per output per code pair, where shared prefix
+// products would cost a store and a load of a float4 per column).
 template <int NC>
 struct LaplaceC64PCfg {
     static constexpr int TAB_PAIRS = PQG_PAIRS_TABLE_P / 2;  // code pairs the staged table holds
-    static constexpr size_t smem_bytes = size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2) +
+    static constexpr size_t smem_bytes = size_t(NC + 1) * PQG_WALK_THREADS * sizeof(float4) +
                                          size_t(NC + 1) * PQG_WALK_THREADS * sizeof(float2) +
                                          size_t(TAB_PAIRS) * NC * sizeof(float4);
 };
@@ -437,8 +441,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
                     (NC + 1) * PQG_WALK_THREADS / 2;
     __shared__ unsigned long long s_group;
     int staged = -1;
-    LaneArray<double2, NC + 1, true> acc64;  // per-lane FP64 sums of every output
-    acc64.init(lap_smem64p, threadIdx.x);
+    // per-lane compensated FP32 sums of every output, {re, im, re_err, im_err}
+    float4 *const acc_base = reinterpret_cast<float4 *>(lap_smem64p);
+    LaneArray<float4, NC + 1, true> acc;
+    acc.init(acc_base, threadIdx.x);
     LaneArray<float2, NC + 1, true> part;  // per-lane FP32 partial sums {re, im} of every output
     part.init(reinterpret_cast<float2 *>(lap_smem64p + (NC + 1) * PQG_WALK_THREADS), threadIdx.x);
     LaneArray<float4, NC, false> pre;  // prefix products {re_a, re_b, im_a, im_b}, registers
@@ -470,6 +476,11 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
         const int n_out = pr->n_out;
         const bool full = n_out > NC;
         const bool active = r0 < pr->Q;
+#pragma unroll
+        for (int l = 0; l <= NC; ++l) {  // (an idle lane's sums join the lane reduction too)
+            part.set(l, make_float2(0.0f, 0.0f));
+            acc.set(l, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        }
         if (active) {
             float sr0[NC], si0[NC];  // seed of the current outer position (double-float, rounded)
             OuterState st;
@@ -491,11 +502,6 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
             // (the staged table holds at most Cfg::TAB_PAIRS pairs: the plan guarantees P
             // fits; the bound keeps every read inside it)
             const int pairs = ((P + 1) >> 1) < Cfg::TAB_PAIRS ? ((P + 1) >> 1) : Cfg::TAB_PAIRS;
-#pragma unroll
-            for (int l = 0; l <= NC; ++l) {
-                part.set(l, make_float2(0.0f, 0.0f));
-                acc64.set(l, make_double2(0.0, 0.0));
-            }
             for (int64_t seg = 0; seg < my_R; ++seg) {
                 for (int u = 0; u < pairs; ++u) {
                     const int ta = 2 * u, tb = ta + 1;
@@ -597,11 +603,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
 #pragma unroll
                         for (int l = 0; l <= NC; ++l) {
                             if (l == NC && !full) continue;
-                            double2 a = acc64.get(l);
-                            const float2 q = part.get(l);
-                            a.x = __dadd_rn(a.x, static_cast<double>(q.x));
-                            a.y = __dadd_rn(a.y, static_cast<double>(q.y));
-                            acc64.set(l, a);
+                            const float4 a = acc.get(l);
+                            float2 s = f2(a.x, a.y), c = f2(a.z, a.w);
+                            two_sum_acc2(s, c, part.get(l));
+                            acc.set(l, make_float4(s.x, s.y, c.x, c.y));
                             part.set(l, make_float2(0.0f, 0.0f));
                         }
                     }
@@ -619,19 +624,22 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_c64p(WalkArg
                 }
             }
         }
-        for (int l = 0; l < n_out; ++l) {
-            double r = 0.0, i = 0.0;
-            if (active) {
-                const double2 a = acc64.get(l);
-                r = a.x;
-                i = a.y;
+        // lane reduction: lane l sums output l over the warp's 32 lanes,
+        // reading the slices in a rotated order (lane l starts at lane l's
+        // slot), so each quarter-warp's float4 loads hit distinct banks
+        __syncwarp();
+        if (lane < n_out) {
+            const float4 *src = acc_base + lane * PQG_WALK_THREADS + (threadIdx.x & ~31);
+            float2 s = f2(0.0f, 0.0f), c = f2(0.0f, 0.0f);
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                const float4 v = src[(k + lane) & 31];
+                two_sum_acc2(s, c, f2(v.x, v.y));
+                c = __fadd2_rn(c, f2(v.z, v.w));
             }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                r += __shfl_down_sync(PQG_FULL_MASK, r, off);
-                i += __shfl_down_sync(PQG_FULL_MASK, i, off);
-            }
-            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, ddv{r, 0.0}, ddv{i, 0.0});
+            store_partial(A.partials, pr->part_begin + local * n_out + lane,
+                          ddv{static_cast<double>(s.x), static_cast<double>(c.x)},
+                          ddv{static_cast<double>(s.y), static_cast<double>(c.y)});
         }
     }
 }
