@@ -327,6 +327,24 @@ __device__ __forceinline__ void two_sum_acc2(float2 &s, float2 &c, float2 y) {
     c = __fadd2_rn(c, e);
 }
 
+// (s + c) += (a.r + a.cr, a.i + a.ci) * w, {re, im} packed, in FP32 only: the
+// weight (an integer) split as w_hi + w_lo, the leading product's rounding
+// error recovered exactly by an FMA, the sum by TwoSum (two_sum_acc2).  About
+// 2^-44 of the lane's largest partial, far inside the complex64 walk's own
+// rounding; it keeps the fold off GB300's FP64 pipe, where one warp
+// instruction holds the pipe for tens of cycles.
+__device__ __forceinline__ void ff_fold(float2 &s, float2 &c, float r, float cr, float i, float ci, double w) {
+    const float wh = __double2float_rn(w);
+    const float wl = __double2float_rn(w - static_cast<double>(wh));
+    const float2 vh = make_float2(r, i), vl = make_float2(cr, ci);
+    const float2 wh2 = make_float2(wh, wh), wl2 = make_float2(wl, wl);
+    const float2 ph = __fmul2_rn(vh, wh2);
+    const float2 pe = __ffma2_rn(vh, wh2, f2neg(ph));
+    const float2 pl = __fadd2_rn(pe, __ffma2_rn(vh, wl2, __fmul2_rn(vl, wh2)));
+    two_sum_acc2(s, c, ph);
+    c = __fadd2_rn(c, pl);
+}
+
 // Product over the columns of (seed + table row t) for both lanes: even and
 // odd columns in two packed chains (four independent chains in all).
 // With REFILL, software-pipelined table loads: dq holds row t on entry; each
@@ -559,6 +577,9 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
         const int64_t Q = pr->Q;
         const int64_t r0 = (local * PQG_ITEM_LANES + lane) * R;
         ddv sr{0.0, 0.0}, si{0.0, 0.0};
+        // two-seed (complex64) walks: compensated FP32 lane sums {re, im} and
+        // their error words, folded by ff_fold (no FP64 instruction)
+        float2 fs = make_float2(0.0f, 0.0f), fc = fs;
         if (r0 < Q) {
             OuterState st;
             outer_decode(pr, r0, st);
@@ -645,8 +666,8 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
                         two_sum_acc2(accr, accrc, __fmul2_rn(w2, xr));
                         two_sum_acc2(acci, accic, __fmul2_rn(w2, xi));
                     }
-                    Ar::fold(sr, si, typename Ar::acc_t{accr.x, accrc.x, acci.x, accic.x}, wout);
-                    Ar::fold(sr, si, typename Ar::acc_t{accr.y, accrc.y, acci.y, accic.y}, wb);
+                    ff_fold(fs, fc, accr.x, accrc.x, acci.x, accic.x, wout);
+                    ff_fold(fs, fc, accr.y, accrc.y, acci.y, accic.y, wb);
                     if (seg + 2 < my_R) {  // seed moves on to position seg + 2
                         k = outer_next(pr, st, &up);
                         const d_t *d = D + (2 * k + (up ? 0 : 1)) * NC;
@@ -683,7 +704,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
                     const cs_t x = row_product<Ar, NC>(seed, delta + static_cast<int64_t>(t) * NC, cm, ones);
                     Ar::accumulate(acc, x, tab[t]);
                 }
-                Ar::fold(sr, si, acc, wout);
+                if constexpr (Ar::kTwoSeeds)
+                    ff_fold(fs, fc, acc.r, acc.cr, acc.i, acc.ci, wout);
+                else
+                    Ar::fold(sr, si, acc, wout);
                 if (seg + 1 < my_R) {
                     bool up = false;
                     const int k = outer_next(pr, st, &up);
@@ -694,12 +718,28 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks<Ar, NC>()) w
                 }
             }
         }
+        if constexpr (Ar::kTwoSeeds) {
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            sr = dd_add(sr, dd_shfl_down(sr, off));
-            si = dd_add(si, dd_shfl_down(si, off));
+            for (int off = 16; off > 0; off >>= 1) {
+                const float2 os = make_float2(__shfl_down_sync(PQG_FULL_MASK, fs.x, off),
+                                              __shfl_down_sync(PQG_FULL_MASK, fs.y, off));
+                const float2 oc = make_float2(__shfl_down_sync(PQG_FULL_MASK, fc.x, off),
+                                              __shfl_down_sync(PQG_FULL_MASK, fc.y, off));
+                two_sum_acc2(fs, fc, os);
+                fc = __fadd2_rn(fc, oc);
+            }
+            if (lane == 0)
+                store_partial(A.partials, pr->part_begin + local,
+                              ddv{static_cast<double>(fs.x), static_cast<double>(fc.x)},
+                              ddv{static_cast<double>(fs.y), static_cast<double>(fc.y)});
+        } else {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                sr = dd_add(sr, dd_shfl_down(sr, off));
+                si = dd_add(si, dd_shfl_down(si, off));
+            }
+            if (lane == 0) store_partial(A.partials, pr->part_begin + local, sr, si);
         }
-        if (lane == 0) store_partial(A.partials, pr->part_begin + local, sr, si);
     }
 }
 
