@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -114,10 +115,15 @@ struct TuneEntry {
     int32_t blocks_per_sm;
 };
 
+// Locks: `mu` serialises the device work (buffers, stream, events) and is
+// held by a launch until its results are back; `cfg_mu` guards the planner
+// configuration and the tuning table, so that a thread planning its batch
+// reads them without waiting for another thread's launch.  Writers of the
+// configuration take mu, then cfg_mu (readers may hold either).
 struct Context {
-    std::mutex mu;
+    std::mutex mu, cfg_mu;
     DeviceBuffers bufs;
-    bool ready = false;
+    std::atomic<bool> ready{false};  // set once by init(), under mu
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
@@ -128,8 +134,8 @@ struct Context {
     std::vector<TuneEntry> tune;  // autotuned settings by workload (pqg_tuning_add)
     std::vector<int> occ_cache[11];  // blocks per SM, per kernel table, per column count
 
-    int init() {
-        if (ready) return PQG_OK;
+    int init() {  // caller holds mu
+        if (ready.load(std::memory_order_acquire)) return PQG_OK;
         int n = 0;
         cudaError_t e = cudaGetDeviceCount(&n);
         if (e != cudaSuccess || n == 0) return fail(PQG_ERR_NO_DEVICE, "no CUDA device visible");
@@ -140,9 +146,12 @@ struct Context {
         PQG_CUDA(cudaEventCreate(&ev1));
         PQG_CUDA(cudaEventCreate(&ev2));
         PQG_CUDA(cudaEventCreate(&evs));
-        cfg.num_sms = num_sms;
+        {
+            std::lock_guard<std::mutex> lock(cfg_mu);
+            cfg.num_sms = num_sms;
+        }
         for (auto &v : occ_cache) v.assign(PQG_MAX_COLS + 1, -1);
-        ready = true;
+        ready.store(true, std::memory_order_release);
         return PQG_OK;
     }
 };
@@ -175,7 +184,8 @@ int arith_code(Precision p) { return p == Precision::C128 ? 0 : (p == Precision:
 // The planner configuration of a plan whose problems are added: the
 // process-wide knobs (pqg_set_tuning), and for every knob left at its default
 // there, the first autotuned entry matching the plan's form, arithmetic,
-// largest column count, total steps and problem count.  Caller holds C.mu.
+// largest column count, total steps and problem count.  Caller holds C.mu or
+// C.cfg_mu.
 PlanConfig tuned_config(const Context &C, const Planner &pl, Precision prec) {
     PlanConfig cfg = C.cfg;
     if (pl.form() == Form::LAPLACE) cfg.p_max = std::min<int64_t>(cfg.p_max, 512);  // Laplace tables
@@ -205,6 +215,21 @@ PlanConfig tuned_config(const Context &C, const Planner &pl, Precision prec) {
         break;
     }
     return cfg;
+}
+
+// The tuned configurations of a plan whose problems are added: its
+// arithmetic's and the FP64 fallback's.  Initialises the context on first
+// use; otherwise reads only the configuration, under cfg_mu.
+int planning_configs(Context &C, const Planner &pl, Precision prec, PlanConfig &cfg, PlanConfig &cfg64) {
+    if (!C.ready.load(std::memory_order_acquire)) {
+        std::lock_guard<std::mutex> lock(C.mu);
+        const int st = C.init();
+        if (st) return st;
+    }
+    std::lock_guard<std::mutex> lock(C.cfg_mu);
+    cfg = tuned_config(C, pl, prec);
+    cfg64 = tuned_config(C, pl, Precision::C128);
+    return PQG_OK;
 }
 
 // walk kernel for (form, precision, exact column count); `which` indexes the
@@ -523,11 +548,8 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     }
     PlanConfig cfg, cfg64;
     {
-        std::lock_guard<std::mutex> lock(C.mu);
-        int st = C.init();
+        const int st = planning_configs(C, pl, prec, cfg, cfg64);
         if (st) return st;
-        cfg = tuned_config(C, pl, prec);
-        cfg64 = tuned_config(C, pl, Precision::C128);
     }
     pl.set_config(cfg);
     pl.finish();
@@ -551,8 +573,7 @@ void laplace_precision_fallback(Planner &pl, const PlanConfig &cfg64) {
     }
 }
 
-// Plans `batch` Laplace problems over one matrix (outside the context lock;
-// the lock is taken only to read the device's configuration).
+// Plans `batch` Laplace problems over one matrix (outside the context lock).
 int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int64_t nc, const int32_t *rows,
                  const int32_t *cols, int64_t batch) {
     pl.set_matrix(matrix, nr, nc);
@@ -564,11 +585,8 @@ int plan_laplace(Context &C, Planner &pl, const double *matrix, int64_t nr, int6
     }
     PlanConfig cfg, cfg64;
     {
-        std::lock_guard<std::mutex> lock(C.mu);
-        int st = C.init();
+        const int st = planning_configs(C, pl, pl.precision(), cfg, cfg64);
         if (st) return st;
-        cfg = tuned_config(C, pl, pl.precision());
-        cfg64 = tuned_config(C, pl, Precision::C128);
     }
     pl.set_config(cfg);
     pl.finish();
@@ -961,6 +979,7 @@ int pqg_permanent_grad_c64(const float *matrices, int64_t n_rows, int64_t n_cols
 int pqg_set_tuning(int64_t items_per_smsp, int64_t p_max, int64_t seed_steps) try {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
+    std::lock_guard<std::mutex> cfg_lock(C.cfg_mu);
     if (items_per_smsp < 0 || p_max < 0 || p_max > 32768 || seed_steps < 0)
         return fail(PQG_ERR_INVALID, "invalid tuning values");
     PlanConfig d;
@@ -1003,6 +1022,7 @@ int pqg_tuning_add(int32_t form, int32_t arith, int32_t nc_lo, int32_t nc_hi, do
         return fail(PQG_ERR_INVALID, "invalid tuning entry");
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
+    std::lock_guard<std::mutex> cfg_lock(C.cfg_mu);
     C.tune.push_back(TuneEntry{form, arith, nc_lo, nc_hi, steps_lo, steps_hi, probs_lo, probs_hi, items_per_smsp,
                                p_max, seed_steps, blocks_per_sm});
     return PQG_OK;
@@ -1013,6 +1033,7 @@ int pqg_tuning_add(int32_t form, int32_t arith, int32_t nc_lo, int32_t nc_hi, do
 int pqg_tuning_clear(void) try {
     Context &C = ctx();
     std::lock_guard<std::mutex> lock(C.mu);
+    std::lock_guard<std::mutex> cfg_lock(C.cfg_mu);
     C.tune.clear();
     return PQG_OK;
 } catch (...) {

@@ -154,7 +154,7 @@ def log_target(U64, patterns, inp):
 
 
 def run_chains(U, input_photons, mlp=None, chains=1024, steps=200, burn_in=50, seed=0, baseline=False,
-               record=True, block=8):
+               record=True, block=16):
     """Runs `chains` independent chains for `steps` steps; returns a dict with
     the recorded states (after burn-in), acceptance rate and timings.
 
@@ -293,7 +293,7 @@ def chain_autocorrelation(samples, chains):
 
 
 def evaluate(U, input_photons, mlp=None, chains=1024, steps=300, burn_in=30, seed=0, baseline=False, pairs=None,
-             pair_seed=0, n_pairs=16, block=8):
+             pair_seed=0, n_pairs=16, block=16):
     """Samples/s, acceptance, two-mode-marginal TVD (mean and max over
     `pairs`, default `n_pairs` random mode pairs) and the chains' integrated
     autocorrelation time (mode occupations; the largest over the modes gives
