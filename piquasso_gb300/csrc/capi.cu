@@ -530,9 +530,23 @@ Precision c128_precision(int32_t mode) {
     return Precision::C128DF;
 }
 
+// Whether a complex128 plain plan chosen by `auto` (double-float) runs the
+// FP64 walk instead: outside the double-float domain, or so small (at most
+// 2^16 Gray-code steps in all) that the FP64 walk costs microseconds -- it
+// then keeps FP64's accuracy, where the double-float walk rounds each scaled
+// matrix entry to 2^-47 once (relative 1e-14 on a 1 x 1 permanent).
+bool use_fp64_walk(const Planner &pl, int32_t mode) {
+    if (pl.precision() != Precision::C128DF) return false;
+    if (!pl.df_ok) return true;
+    if (mode == PQG_MODE_DF) return false;
+    const char *env = std::getenv("PQG_C128_MODE");
+    if (env && std::strcmp(env, "df") == 0) return false;
+    return pl.total_steps <= 65536.0;
+}
+
 template <typename T>
 int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *rows, const int32_t *cols, int64_t batch,
-                Precision prec, T *out, double *out_lo) {
+                Precision prec, T *out, double *out_lo, int32_t mode = PQG_MODE_AUTO) {
     if (batch < 0 || nr < 0 || nc < 0 || !out) return fail(PQG_ERR_INVALID, "invalid arguments");
     Context &C = ctx();
     // Host planning runs outside the context lock (threads plan concurrently;
@@ -553,8 +567,8 @@ int plain_batch(const double *matrix, int64_t nr, int64_t nc, const int32_t *row
     }
     pl.set_config(cfg);
     pl.finish();
-    if (prec == Precision::C128DF && !pl.df_ok) {
-        // outside the double-float domain: the FP64 walk
+    if (use_fp64_walk(pl, mode)) {
+        // outside the double-float domain, or a small plan: the FP64 walk
         pl.set_precision(Precision::C128);
         pl.set_config(cfg64);
         pl.finish();
@@ -879,7 +893,7 @@ uint64_t pqg_kernel_launches(void) { return g_launches.load(); }
 
 int pqg_permanent_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows, const int32_t *cols,
                        int32_t mode, double *out, double *out_lo) try {
-    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, 1, c128_precision(mode), out, out_lo);
+    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, 1, c128_precision(mode), out, out_lo, mode);
 } catch (...) {
     return host_failure();
 }
@@ -895,7 +909,7 @@ int pqg_permanent_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const
 
 int pqg_permanent_batch_c128(const double *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                              const int32_t *cols, int64_t batch, int32_t mode, double *out) try {
-    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(mode), out, nullptr);
+    return plain_batch<double>(matrix, n_rows, n_cols, rows, cols, batch, c128_precision(mode), out, nullptr, mode);
 } catch (...) {
     return host_failure();
 }
@@ -1153,7 +1167,7 @@ int pqg_plan_create(const void *matrix, int64_t n_rows, int64_t n_cols, const in
     h->pl.finish();
     if (fm == Form::LAPLACE) {
         laplace_precision_fallback(h->pl, tuned_config(C, h->pl, Precision::C128));
-    } else if (prec == Precision::C128DF && !h->pl.df_ok) {
+    } else if (use_fp64_walk(h->pl, mode)) {
         h->pl.set_precision(Precision::C128);
         h->pl.set_config(tuned_config(C, h->pl, Precision::C128));
         h->pl.finish();

@@ -22,7 +22,7 @@
 // share the prefix table's tiles of codes.  The grid loops over (problem,
 // slice).  Launched with 256 threads (one per code of a tile).
 #pragma once
-#include "walk_common.cuh"
+#include "walk_df.cuh"
 
 namespace pqg {
 
@@ -44,6 +44,18 @@ struct PrepArgs {
     int32_t pairs;  // PREP_F32 only: code pairs, float4 {re_2u, re_2u+1, im_2u, im_2u+1} per column
                     // (an odd P gets a zero pad code)
 };
+
+// A scaled matrix entry of the double-float walk rounded to a multiple of
+// 2^-47 (|x| < 1; x * 2^47 and back are exact).  Every seed, update row and
+// prefix-table entry is then a sum of such entries below 2 in magnitude,
+// itself a multiple of 2^-47: its high word on the walk's 2^-23 grid and the
+// rest (at most 2^-24, 23 bits) are exact floats, and the walk's column sums
+// and seed updates are exact (walk_df.cuh).  The one rounding is this one, at
+// most 2^-48 per scaled entry, and it is consistent: the walk sums the
+// permanent of the rounded matrix.
+__device__ __forceinline__ double q47(double x) {
+    return rint(x * 140737488355328.0) * 7.1054273576010019e-15;
+}
 
 __device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
     hi = __double2float_rn(x);
@@ -106,6 +118,19 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
             return make_double2(e[0], e[1]);
         };
         auto mult = [&](int d) -> int { return d < no ? pr->outer_m[d] : pr->inner_m[d - no]; };
+        // a scaled entry as the double-float walk takes it: rounded by q47
+        // (every sum of them below is then exact in FP64: they stay below 2)
+        auto qdf = [&](double x) -> double {
+            if constexpr (FMT == PREP_DF) return q47(x);
+            return x;
+        };
+        // an inner digit's row as the prefix table sums it: scaled and rounded
+        // for the double-float walk (whose table is not scaled afterwards)
+        auto ad_tab = [&](int d, int j) -> double2 {
+            const double2 a = ad(d, j);
+            if constexpr (FMT == PREP_DF) return make_double2(q47(a.x * cscale[j]), q47(a.y * cscale[j]));
+            return a;
+        };
 
         for (int j = threadIdx.x; j < nc; j += blockDim.x) {
             double s = 1.0;
@@ -137,10 +162,10 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                 const int j = c >> 1, part = c & 1;
                 const double sc = cscale[j];
                 const double2 v0 = a0(j);
-                double sum = (part ? v0.y : v0.x) * sc, comp = 0.0;
+                double sum = qdf((part ? v0.y : v0.x) * sc), comp = 0.0;
                 for (int d = 0; d < nd; ++d) {
                     const double2 w = ad(d, j);
-                    const double x = static_cast<double>(mult(d)) * ((part ? w.y : w.x) * sc);
+                    const double x = static_cast<double>(mult(d)) * qdf((part ? w.y : w.x) * sc);
                     const double t = sum + x;
                     const double bb = t - sum;
                     comp += (sum - (t - bb)) + (x - bb);
@@ -160,7 +185,7 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                 const int c = e - o * 2 * nc;
                 const int j = c >> 1, part = c & 1;
                 const double2 w = ad(o, j);
-                const double v = (part ? w.y : w.x) * cscale[j];
+                const double v = qdf((part ? w.y : w.x) * cscale[j]);
                 const int64_t up = static_cast<int64_t>(2 * o) * 2 * nc + c;  // row 2o: -2 a_o
                 const int64_t dn = up + 2 * nc;                                 // row 2o+1: +2 a_o
                 if constexpr (FMT == PREP_F64) {
@@ -172,9 +197,9 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                     float *orow = reinterpret_cast<float *>(A.arena + pr->off_outer_df);
                     split_df(v, orow[2 * e], orow[2 * e + 1]);
                     float *D = reinterpret_cast<float *>(A.arena + pr->off_D);
-                    if constexpr (FMT == PREP_DF) {
-                        split_df(-2.0 * v, D[2 * up], D[2 * up + 1]);
-                        split_df(2.0 * v, D[2 * dn], D[2 * dn + 1]);
+                    if constexpr (FMT == PREP_DF) {  // (high words on the walk's 2^-23 grid)
+                        df_split_grid(-2.0 * v, D[2 * up], D[2 * up + 1]);
+                        df_split_grid(2.0 * v, D[2 * dn], D[2 * dn + 1]);
                     } else {
                         D[up] = __double2float_rn(-2.0 * v);
                         D[dn] = __double2float_rn(2.0 * v);
@@ -224,7 +249,7 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                     rest /= L;
                     if (!g) continue;
                     const double f = -2.0 * g;
-                    const double2 a = ad(no + k, j);
+                    const double2 a = ad_tab(no + k, j);
                     re = __fma_rn(f, a.x, re);
                     im = __fma_rn(f, a.y, im);
                 }
@@ -233,7 +258,7 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
         } else {
             for (int k = threadIdx.x; k < K * nc; k += blockDim.x) {
                 const int kk = k / nc, j = k - kk * nc;
-                inrow[kk][j] = ad(no + kk, j);
+                inrow[kk][j] = ad_tab(no + kk, j);
             }
         }
         for (int tile = slice; tile < n_tiles; tile += A.slices) {
@@ -280,8 +305,10 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                         im = __fma_rn(f, a.y, im);
                     }
                 }
-                re *= cscale[j];
-                im *= cscale[j];
+                if constexpr (FMT != PREP_DF) {  // (the double-float rows are scaled already)
+                    re *= cscale[j];
+                    im *= cscale[j];
+                }
                 const int64_t at = pr->delta_begin + static_cast<int64_t>(t0) * nc + e;
                 if constexpr (FMT == PREP_F64) {
                     reinterpret_cast<double2 *>(A.delta)[at] = make_double2(re, im);
@@ -303,10 +330,10 @@ __global__ void __launch_bounds__(256) prep_problems(PrepArgs A) {
                     } else {
                         reinterpret_cast<float2 *>(A.delta)[at] = make_float2(fr, fi);
                     }
-                } else {
+                } else {  // double-float, high words on the walk's 2^-23 grid
                     float4 v;
-                    split_df(re, v.x, v.y);
-                    split_df(im, v.z, v.w);
+                    df_split_grid(re, v.x, v.y);
+                    df_split_grid(im, v.z, v.w);
                     reinterpret_cast<float4 *>(A.delta)[at] = v;
                 }
             }

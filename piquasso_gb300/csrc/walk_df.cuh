@@ -147,6 +147,65 @@ __device__ __forceinline__ dfl df_scale(dfl x, float w) {
     return {h, __fsub_rn(l, __fsub_rn(h, p))};
 }
 
+// ------------------------------------------------ column sums on a grid
+// Every value that enters a column sum of the double-float walk is below 2 in
+// magnitude: the planner's power-of-two column scale makes every column sum
+// (and so every seed) smaller than 1, a prefix-table entry or a one-digit
+// update row is a difference of two of them.  The walk keeps the high word of
+// each such value on the grid of multiples of 2^-23 (the spacing of floats in
+// [1, 2)).  Two high words on that grid add exactly in FP32 -- their sum is a
+// multiple of 2^-23 below 2 in magnitude, which a float represents -- so a
+// column sum seed + Delta(t) is hi + hi and lo + lo, two adds instead of a
+// TwoSum's eight.  The low word (at most 2^-24 in magnitude, rounded once per
+// add) carries the rest to about 2^-48 absolute: the same order as the TwoSum
+// sum of two double-floats of magnitude up to 1, so the grid costs the walk
+// at most a few times the error of a column sum near zero.
+constexpr float DF_GRID = 1.1920928955078125e-7f;  // 2^-23
+constexpr float DF_GRID_INV = 8388608.0f;          // 2^23
+
+// x on the grid: the nearest multiple of 2^-23 (x * 2^23 and back are exact)
+__device__ __forceinline__ float df_grid_round(float x) {
+    return __fmul_rn(rintf(__fmul_rn(x, DF_GRID_INV)), DF_GRID);
+}
+
+// A double-float of magnitude below 1 with its high word moved onto the grid:
+// hi - t is exact (both are multiples of the smaller one's spacing and the
+// difference is the smaller), so only the new low word rounds.
+__device__ __forceinline__ dfl df_to_grid(dfl a) {
+    const float t = df_grid_round(a.hi);
+    return {t, __fadd_rn(__fsub_rn(a.hi, t), a.lo)};
+}
+
+// a + b for a, b with high words on the grid and |a + b| < 1: the high words
+// add exactly; the low words' grid part moves into the high word ((x + 1.5) -
+// 1.5 rounds |x| < 0.5 to the grid), so the result is on the grid again with
+// a low word of at most 2^-24 (the outer one-digit update of a seed).
+__device__ __forceinline__ dfl df_grid_add(dfl a, dfl b) {
+    const float h = __fadd_rn(a.hi, b.hi);
+    const float l = __fadd_rn(a.lo, b.lo);
+    const float t = __fsub_rn(__fadd_rn(l, 1.5f), 1.5f);
+    return {__fadd_rn(h, t), __fsub_rn(l, t)};
+}
+
+// a + b for a, b with high words on the grid (a column sum): hi + hi and
+// lo + lo are exact, and a Fast2Sum renormalises the pair -- valid since
+// |hi| >= 2^-23 >= |lo| or hi = 0 -- so that the products see a low word
+// below half an ulp of the high word (with a low word of up to 2^-23 beside a
+// column sum of 0.1, their FMA cross terms would round at 2^-44 of the
+// product).  Five operations instead of a TwoSum's eight.
+__device__ __forceinline__ dfl df_grid_sum(dfl a, dfl b) {
+    const float h = __fadd_rn(a.hi, b.hi);
+    const float l = __fadd_rn(a.lo, b.lo);
+    const float s = __fadd_rn(h, l);
+    return {s, __fsub_rn(l, __fsub_rn(s, h))};
+}
+
+// x (|x| < 2) with its high word on the grid
+__device__ __forceinline__ void df_split_grid(double x, float &hi, float &lo) {
+    hi = static_cast<float>(rint(x * 8388608.0) * 1.1920928955078125e-7);
+    lo = __double2float_rn(x - static_cast<double>(hi));
+}
+
 __device__ __forceinline__ dfl df_split(double x) {
     const float h = __double2float_rn(x);
     return {h, __double2float_rn(x - static_cast<double>(h))};

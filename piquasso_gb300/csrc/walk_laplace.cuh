@@ -715,10 +715,11 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
                     // the whole weight, an exact FP32 integer (checked by the plan)
                     const float w = static_cast<float>(__ldg(&tab[t].wd) * wout);
                     const float4 *d = delta + static_cast<int64_t>(t) * NC;
+                    // column sums: high words on the 2^-23 grid (walk_df.cuh), exact
                     auto col = [&](int j, dfl &cr, dfl &ci) {
                         const float4 v = __ldg(d + j);
-                        cr = df_add_lazy(sr0[j], dfl{v.x, v.y});
-                        ci = df_add_lazy(si0[j], dfl{v.z, v.w});
+                        cr = df_grid_sum(sr0[j], dfl{v.x, v.y});
+                        ci = df_grid_sum(si0[j], dfl{v.z, v.w});
                     };
                     // prefix products: pre_l = prod_{k<l} c_k
                     dfl xr{1.0f, 0.0f}, xi{0.0f, 0.0f};
@@ -784,8 +785,8 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
 #pragma unroll
                     for (int j = 0; j < NC; ++j) {
                         const float4 v = dd[j];
-                        sr0[j] = df_add(sr0[j], dfl{v.x, v.y});
-                        si0[j] = df_add(si0[j], dfl{v.z, v.w});
+                        sr0[j] = df_grid_add(sr0[j], dfl{v.x, v.y});
+                        si0[j] = df_grid_add(si0[j], dfl{v.z, v.w});
                     }
                     wout = outer_weight(pr, st);
                 }

@@ -116,14 +116,18 @@ struct ArDF {
     static constexpr bool kTwoChains = true;
     static constexpr bool kPairSteps = false;  // enough independent work per code already
     static constexpr bool kTwoSeeds = false;   // FMA-pipe bound; its seeds need the registers
-    __device__ __forceinline__ static cs_t from_seed64(double r, double i) { return {df_split(r), df_split(i)}; }
-    __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {r, i}; }
+    // seeds, update rows and prefix-table entries keep their high words on the
+    // grid of multiples of 2^-23 (walk_df.cuh): a column sum is two exact-high adds
+    __device__ __forceinline__ static cs_t from_seed64(double r, double i) {
+        return {df_to_grid(df_split(r)), df_to_grid(df_split(i))};
+    }
+    __device__ __forceinline__ static cs_t from_seed_df(dfl r, dfl i) { return {df_to_grid(r), df_to_grid(i)}; }
     __device__ __forceinline__ static void update(cs_t &c, const d_t &d) {
-        c.r = df_add(c.r, dfl{d.x, d.y});
-        c.i = df_add(c.i, dfl{d.z, d.w});
+        c.r = df_grid_add(c.r, dfl{d.x, d.y});
+        c.i = df_grid_add(c.i, dfl{d.z, d.w});
     }
     __device__ __forceinline__ static cs_t sum(const cs_t &c, const d_t &d) {
-        return {df_add_lazy(c.r, dfl{d.x, d.y}), df_add_lazy(c.i, dfl{d.z, d.w})};
+        return {df_grid_sum(c.r, dfl{d.x, d.y}), df_grid_sum(c.i, dfl{d.z, d.w})};
     }
     // products feed products: unnormalised pairs (df_cmul_lazy); the
     // accumulation renormalises (df_scale, df_add)
@@ -764,7 +768,7 @@ struct PlainDfsCfg {
 };
 
 template <int NC, bool ONES>
-__global__ void __launch_bounds__(PQG_WALK_THREADS, 3) walk_plain_dfs(WalkArgs A) {
+__global__ void __launch_bounds__(PQG_WALK_THREADS, 4) walk_plain_dfs(WalkArgs A) {
     using Ar = ArDF;
     using cs_t = Ar::cs_t;
     extern __shared__ float4 dfs_seed_smem[];
@@ -802,7 +806,8 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 3) walk_plain_dfs(WalkArgs A
                         r = df_add(r, df_scale(dfl{w.x, w.y}, f));
                         i = df_add(i, df_scale(dfl{w.z, w.w}, f));
                     }
-                    seed[j * PQG_WALK_THREADS] = make_float4(r.hi, r.lo, i.hi, i.lo);
+                    const cs_t c = Ar::from_seed_df(r, i);
+                    seed[j * PQG_WALK_THREADS] = make_float4(c.r.hi, c.r.lo, c.i.hi, c.i.lo);
                 }
             }
             double wout = outer_weight(pr, st);
