@@ -44,7 +44,7 @@ def haar_unitary(d, seed):
 
 # DRAM traffic of one n=28 double-float walk launch (bytes, read + write),
 # recorded from an ncu capture of the headline workload on a GB300
-TRAFFIC_N28_DF = 528128
+TRAFFIC_N28_DF = 180992
 TRAFFIC_N28_DF_DATE = "2026-12-04"
 
 
