@@ -170,10 +170,15 @@ __device__ __forceinline__ float df_grid_round(float x) {
 
 // A double-float of magnitude below 1 with its high word moved onto the grid:
 // hi - t is exact (both are multiples of the smaller one's spacing and the
-// difference is the smaller), so only the new low word rounds.
+// difference is the smaller), and so is adding lo for a value on the 2^-47
+// grid.  That low word can reach 1.5 * 2^-24, so its own grid part moves into
+// the high word as in df_grid_add: the low word ends at most 2^-24, which
+// keeps the walk's low-word sums below 2^-23 and exact.
 __device__ __forceinline__ dfl df_to_grid(dfl a) {
     const float t = df_grid_round(a.hi);
-    return {t, __fadd_rn(__fsub_rn(a.hi, t), a.lo)};
+    const float l = __fadd_rn(__fsub_rn(a.hi, t), a.lo);
+    const float u = __fsub_rn(__fadd_rn(l, 1.5f), 1.5f);
+    return {__fadd_rn(t, u), __fsub_rn(l, u)};
 }
 
 // a + b for a, b with high words on the grid and |a + b| < 1: the high words

@@ -101,13 +101,23 @@ def test_seed_update_stays_exact_on_the_grid():
 
 def test_regrid_of_a_double_float_seed_is_exact():
     """df_to_grid: a standard double-float (hi, lo) of a value on the 2^-47 grid
-    below 1 moves onto the grid without rounding (hi - t exact, then one add)."""
+    below 1 moves onto the grid without rounding (hi - t exact, then one add,
+    then the low word's grid part into the high word)."""
     rng = np.random.default_rng(4)
     x = _entries(rng, 20000, 1.0)
     hi = x.astype(F)
     lo = (x - hi.astype(np.float64)).astype(F)
     assert np.all(hi.astype(np.float64) + lo.astype(np.float64) == x)
     t = (np.rint(hi * F(2.0 ** 23)) * GRID).astype(F)
-    nlo = (hi - t) + lo
-    assert np.all(t.astype(np.float64) + nlo.astype(np.float64) == x)
+    l_ = (hi - t) + lo
+    assert np.all(t.astype(np.float64) + l_.astype(np.float64) == x)  # exact, but |l_| up to 1.5 * 2^-24
+    u = (l_ + F(1.5)) - F(1.5)
+    nhi, nlo = t + u, l_ - u
+    assert np.all(nhi.astype(np.float64) + nlo.astype(np.float64) == x)
     assert np.all(np.abs(nlo) <= 2.0 ** -24)
+    # and the regridded seed's column sums stay exact
+    delta = _entries(rng, 20000, 1.0)
+    keep = np.abs(x + delta) < 1.0
+    dh, dl = split_grid(delta[keep])
+    s, lo2, h, l2 = grid_sum(nhi[keep], nlo[keep], dh, dl)
+    assert np.all(s.astype(np.float64) + lo2.astype(np.float64) == x[keep] + delta[keep])
