@@ -37,11 +37,13 @@ extern "C" {
 #define PQG_ERR_HOST 6         /* host-side failure, e.g. out of host memory (no C++ exception leaves the library) */
 
 /* precision modes for the complex128 entry points */
-#define PQG_MODE_AUTO 0 /* default: PQG_MODE_DF where valid (<= 32 particles), else FP64;
-                           the environment variable PQG_C128_MODE=fp64 forces FP64 */
+#define PQG_MODE_AUTO 0 /* default: PQG_MODE_DF where valid (<= 32 particles) and the plan
+                           has more than 2^16 Gray-code steps, else FP64; the environment
+                           variable PQG_C128_MODE=fp64 forces FP64 */
 #define PQG_MODE_FP64 1 /* column sums, updates and products in FP64; double-double sums */
-#define PQG_MODE_DF 2   /* FP64 seeds and double-double sums; updates and products in
-                           double-float (FP32 pairs, ~2^-48 relative per operation) */
+#define PQG_MODE_DF 2   /* double-float on the FP32 pipes: the column-scaled matrix rounded
+                           once to 2^-47 per entry, then exact column sums and seed updates,
+                           double-float products (~2^-48 relative each), double-double sums */
 
 /* Host planning: a call with 2048 or more problems is planned on up to 8
  * host threads (the environment variable PQG_HOST_THREADS caps the count; 1
@@ -65,8 +67,9 @@ int pqg_permanent_c128(const double *matrix, int64_t n_rows, int64_t n_cols, con
                        const int32_t *cols, int32_t mode, double *out, double *out_lo);
 
 /* complex64 variant: FP32 row-sum updates and products, FP32 TwoSum-compensated
- * partial sums folded into per-thread double-double accumulators.  `out`
- * receives 2 floats (re, im). */
+ * partial sums folded into compensated FP32 lane sums (value and error word),
+ * combined across lanes, items and blocks in double-double.  `out` receives 2
+ * floats (re, im). */
 int pqg_permanent_c64(const float *matrix, int64_t n_rows, int64_t n_cols, const int32_t *rows,
                       const int32_t *cols, float *out);
 

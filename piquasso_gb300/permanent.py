@@ -116,7 +116,8 @@ def permanent(matrix, rows, cols):
 def permanent_dd(matrix, rows, cols, mode="auto"):
     """complex128 permanent with its double-double low words: (value, low).
 
-    ``mode``: "auto" (double-float where valid, else FP64), "fp64" or "df"."""
+    ``mode``: "auto" (double-float where valid and the plan is larger than 2^16
+    Gray-code steps, else FP64), "fp64" or "df"."""
     m = _as_matrix(np.asarray(matrix, dtype=np.complex128))
     r = _as_mult(rows, m.shape[0], "rows")
     c = _as_mult(cols, m.shape[1], "cols")
