@@ -35,70 +35,16 @@ __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
     return {h, __fsub_rn(l, __fsub_rn(h, s))};
 }
 
-// a + b without the final renormalisation, for sums that only feed products:
-// TwoSum keeps the rounding error of the high words, so hi + lo is still the
-// sum to about 2^-48 of the operands, and the products' cross terms take the
-// low word through FMAs (8 operations instead of 11).
-__device__ __forceinline__ dfl df_add_lazy(dfl a, dfl b) {
-    const float s = __fadd_rn(a.hi, b.hi);
-    const float v = __fsub_rn(s, a.hi);
-    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
-    return {s, __fadd_rn(__fadd_rn(a.lo, b.lo), e)};
-}
-
-// real part of a product: ah*bh - ch*dh (+ low-order cross terms), with
-// (ah + al), (bh + bl), (ch + cl), (dh + dl) double-float operands
-__device__ __forceinline__ dfl df_mul_sub(dfl a, dfl b, dfl c, dfl d) {
-    const float p1 = __fmul_rn(a.hi, b.hi);
-    const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
-    const float p2 = __fmul_rn(c.hi, d.hi);
-    const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
-    const float s = __fsub_rn(p1, p2);
-    const float v = __fsub_rn(s, p1);
-    const float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(-p2, v));
-    float low = __fadd_rn(__fsub_rn(e1, e2), t);
-    low = __fmaf_rn(a.hi, b.lo, low);
-    low = __fmaf_rn(a.lo, b.hi, low);
-    low = __fmaf_rn(-c.hi, d.lo, low);
-    low = __fmaf_rn(-c.lo, d.hi, low);
-    const float h = __fadd_rn(s, low);
-    return {h, __fsub_rn(low, __fsub_rn(h, s))};
-}
-
-// imaginary part: ah*bh + ch*dh (+ cross terms)
-__device__ __forceinline__ dfl df_mul_add(dfl a, dfl b, dfl c, dfl d) {
-    const float p1 = __fmul_rn(a.hi, b.hi);
-    const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
-    const float p2 = __fmul_rn(c.hi, d.hi);
-    const float e2 = __fmaf_rn(c.hi, d.hi, -p2);
-    const float s = __fadd_rn(p1, p2);
-    const float v = __fsub_rn(s, p1);
-    const float t = __fadd_rn(__fsub_rn(p1, __fsub_rn(s, v)), __fsub_rn(p2, v));
-    float low = __fadd_rn(__fadd_rn(e1, e2), t);
-    low = __fmaf_rn(a.hi, b.lo, low);
-    low = __fmaf_rn(a.lo, b.hi, low);
-    low = __fmaf_rn(c.hi, d.lo, low);
-    low = __fmaf_rn(c.lo, d.hi, low);
-    const float h = __fadd_rn(s, low);
-    return {h, __fsub_rn(low, __fsub_rn(h, s))};
-}
-
-// (xr + i xi) *= (yr + i yi)
-__device__ __forceinline__ void df_cmul(dfl &xr, dfl &xi, dfl yr, dfl yi) {
-    const dfl r = df_mul_sub(xr, yr, xi, yi);
-    const dfl i = df_mul_add(xr, yi, xi, yr);
-    xr = r;
-    xi = i;
-}
-
-// The same product without the final renormalisation of either part, for
-// products that only feed further products: the result pair (s, low) still
+// Real part of a product, ah*bh - ch*dh plus the low-order cross terms, for
+// double-float operands (ah + al) ... (dh + dl): FMA TwoProducts of the high
+// words, a TwoSum of their difference, and the cross terms through FMAs.  The
+// pair is not renormalised -- it only feeds further products: (s, low) still
 // sums to the product to about 2^-48 of its terms (TwoSum kept the rounding
 // error of the high words), and the next product takes the low word through
-// its FMA cross terms, so only the dropped low x low term grows — by the
-// cancellation factor |p1| / |p1 - p2| that the sum already carries.  It
-// takes the two dependent renormalisation operations off the product chain.
-// The pair is renormalised before it is accumulated (df_scale, df_add).
+// its FMA cross terms, so only the dropped low x low term grows -- by the
+// cancellation factor |p1| / |p1 - p2| that the sum already carries.  That
+// keeps two dependent operations off the product chain.  The pair is
+// renormalised before it is accumulated (df_scale, df_add).
 __device__ __forceinline__ dfl df_mul_sub_lazy(dfl a, dfl b, dfl c, dfl d) {
     const float p1 = __fmul_rn(a.hi, b.hi);
     const float e1 = __fmaf_rn(a.hi, b.hi, -p1);
