@@ -680,6 +680,9 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
         const int n_out = pr->n_out;
         const bool full = n_out > NC;
         const bool active = r0 < pr->Q;
+#pragma unroll
+        for (int l = 0; l <= NC; ++l)  // (an idle lane's sums join the lane reduction too)
+            acc.set(l, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         if (active) {
             dfl sr0[NC], si0[NC];  // double-float seed of the current outer position
             OuterState st;
@@ -693,7 +696,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
                     si0[j] = s[j].i;
                 }
             }
-            double wout = outer_weight(pr, st);
+            // the outer weight as a float: the plan checks that every inner
+            // weight times every outer weight is an integer below 2^24, so the
+            // step's whole weight is one exact FP32 product
+            float wout = static_cast<float>(outer_weight(pr, st));
             const int64_t my_R = (pr->Q - r0 < R) ? (pr->Q - r0) : R;
             const float4 *D = reinterpret_cast<const float4 *>(A.arena + pr->off_D);
             const PqgStep *tab = reinterpret_cast<const PqgStep *>(A.arena + pr->off_tab);
@@ -702,8 +708,6 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
             // column multiplicities (repeated-column kernel): read from the
             // problem record (L1, the same for the whole warp), not registers
             const uint8_t *cm = pr->cm;
-#pragma unroll
-            for (int l = 0; l <= NC; ++l) acc.set(l, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
             auto add_to = [&](int l, dfl tr, dfl ti) {
                 const float4 a = acc.get(l);
                 const dfl r = df_add(dfl{a.x, a.y}, tr), i = df_add(dfl{a.z, a.w}, ti);
@@ -713,7 +717,7 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
             for (int64_t seg = 0; seg < my_R; ++seg) {
                 for (int t = 0; t < P; ++t) {
                     // the whole weight, an exact FP32 integer (checked by the plan)
-                    const float w = static_cast<float>(__ldg(&tab[t].wd) * wout);
+                    const float w = __fmul_rn(__ldg(&tab[t].wf), wout);
                     const float4 *d = delta + static_cast<int64_t>(t) * NC;
                     // column sums: high words on the 2^-23 grid (walk_df.cuh), exact
                     auto col = [&](int j, dfl &cr, dfl &ci) {
@@ -788,24 +792,29 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, 2) walk_laplace_df(WalkArgs 
                         sr0[j] = df_grid_add(sr0[j], dfl{v.x, v.y});
                         si0[j] = df_grid_add(si0[j], dfl{v.z, v.w});
                     }
-                    wout = outer_weight(pr, st);
+                    wout = static_cast<float>(outer_weight(pr, st));
                 }
             }
         }
-        for (int l = 0; l < n_out; ++l) {
-            ddv r{0.0, 0.0}, i{0.0, 0.0};
-            if (active) {
-                const float4 a = acc.get(l);
-                r = dd_add_d(ddv{static_cast<double>(a.x), 0.0}, static_cast<double>(a.y));
-                i = dd_add_d(ddv{static_cast<double>(a.z), 0.0}, static_cast<double>(a.w));
+        // lane reduction: lane l sums output l (and l + 32) over the warp's 32
+        // lanes in double-float on the FP32 pipes, reading the slices in a
+        // rotated order (lane l starts at lane l's slot) so that each
+        // quarter-warp's float4 loads hit distinct banks
+        __syncwarp();
+        for (int l = lane; l < n_out; l += 32) {
+            const float4 *src = lap_smem_df + l * PQG_WALK_THREADS + (threadIdx.x & ~31);
+            dfl r{0.0f, 0.0f}, i{0.0f, 0.0f};
+#pragma unroll 4
+            for (int k = 0; k < 32; ++k) {
+                const float4 v = src[(k + lane) & 31];
+                r = df_add(r, dfl{v.x, v.y});
+                i = df_add(i, dfl{v.z, v.w});
             }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                r = dd_add(r, dd_shfl_down(r, off));
-                i = dd_add(i, dd_shfl_down(i, off));
-            }
-            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, r, i);
+            store_partial(A.partials, pr->part_begin + local * n_out + l,
+                          ddv{static_cast<double>(r.hi), static_cast<double>(r.lo)},
+                          ddv{static_cast<double>(i.hi), static_cast<double>(i.lo)});
         }
+        __syncwarp();  // the slices are read before the next item clears them
     }
 }
 
