@@ -208,13 +208,13 @@ struct LaplaceC64Cfg {
     static constexpr bool PRE_SMEM = NC > 16;
     static constexpr size_t smem_bytes =
         (PRE_SMEM ? size_t(NC) * PQG_WALK_THREADS * sizeof(float2) : 0) +
-        size_t(NC + 1) * PQG_WALK_THREADS * sizeof(double2);
+        size_t(NC + 1) * PQG_WALK_THREADS * sizeof(float4);
 };
 
 // Complex64 Laplace walk: seed in double-float rounded to FP32, column sums
 // seed + Delta(t) and products in FP32, FP32 partial sums over 32 codes folded
-// into per-lane FP64 sums held in shared memory, lanes combined in FP64 (the
-// output is complex64).  ONES: every column has multiplicity 1 (the sampler's
+// into per-lane compensated FP32 sums held in shared memory (ff_fold), lanes
+// combined the same way (the output is complex64; no FP64 instruction).  ONES: every column has multiplicity 1 (the sampler's
 // case), so the repeated-factor code is compiled out; a fully unrolled
 // 24-column step with it did not fit the instruction cache (ncu: 9.7
 // no-instruction stalls per issue, 11 % issue).
@@ -223,8 +223,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
     using Cfg = LaplaceC64Cfg<NC>;
     extern __shared__ double2 lap_smem64[];
     const int lane = threadIdx.x & 31;
-    LaneArray<double2, NC + 1, true> acc64;
-    acc64.init(lap_smem64, threadIdx.x);
+    // per-lane compensated FP32 sums of every output, {re, im, re_err, im_err}
+    float4 *const acc_base = reinterpret_cast<float4 *>(lap_smem64);
+    LaneArray<float4, NC + 1, true> acc;
+    acc.init(acc_base, threadIdx.x);
     LaneArray<float2, NC, Cfg::PRE_SMEM> pre;
     pre.init(reinterpret_cast<float2 *>(lap_smem64 + (NC + 1) * PQG_WALK_THREADS), threadIdx.x);
 
@@ -239,6 +241,9 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
         const int n_out = pr->n_out;
         const bool full = n_out > NC;
         const bool active = r0 < pr->Q;
+#pragma unroll
+        for (int l = 0; l <= NC; ++l)  // (an idle lane's sums join the lane reduction too)
+            acc.set(l, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         if (active) {
             float sr0[NC], si0[NC];  // seed of the current outer position (double-float, rounded)
             OuterState st;
@@ -269,11 +274,12 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
             for (int l = 0; l <= NC; ++l) {
                 ar[l] = 0.0f;
                 ai[l] = 0.0f;
-                acc64.set(l, make_double2(0.0, 0.0));
             }
 
             // R consecutive outer positions; the FP32 partial sums fold into
-            // the FP64 accumulators weighted by the current outer weight
+            // the compensated sums weighted by the current outer weight (ff_fold:
+            // the weight as two FP32 words, the product's rounding error by an
+            // FMA, TwoSum -- no FP64 instruction)
             for (int64_t seg = 0; seg < my_R; ++seg) {
             for (int t = 0; t < P; ++t) {
                 const float w = __ldg(&tab[t].wf);
@@ -353,10 +359,10 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
 #pragma unroll
                     for (int l = 0; l <= NC; ++l) {
                         if (l == NC && !full) continue;
-                        double2 a = acc64.get(l);
-                        a.x = __fma_rn(wout, static_cast<double>(ar[l]), a.x);
-                        a.y = __fma_rn(wout, static_cast<double>(ai[l]), a.y);
-                        acc64.set(l, a);
+                        const float4 a = acc.get(l);
+                        float2 fs = make_float2(a.x, a.y), fc = make_float2(a.z, a.w);
+                        ff_fold(fs, fc, ar[l], 0.0f, ai[l], 0.0f, wout);
+                        acc.set(l, make_float4(fs.x, fs.y, fc.x, fc.y));
                         ar[l] = 0.0f;
                         ai[l] = 0.0f;
                     }
@@ -375,20 +381,24 @@ __global__ void __launch_bounds__(PQG_WALK_THREADS, walk_min_blocks_cols<NC>()) 
             }
             }
         }
-        for (int l = 0; l < n_out; ++l) {
-            double r = 0.0, i = 0.0;
-            if (active) {
-                const double2 a = acc64.get(l);
-                r = a.x;
-                i = a.y;
+        // lane reduction: lane l sums output l (and l + 32) over the warp's 32
+        // lanes with TwoSum on the FP32 pipes, reading the slices in a
+        // rotated order so that each quarter-warp's float4 loads hit distinct banks
+        __syncwarp();
+        for (int l = lane; l < n_out; l += 32) {
+            const float4 *src = acc_base + l * PQG_WALK_THREADS + (threadIdx.x & ~31);
+            float2 fs = make_float2(0.0f, 0.0f), fc = fs;
+#pragma unroll 8
+            for (int q = 0; q < 32; ++q) {
+                const float4 v = src[(q + lane) & 31];
+                two_sum_acc2(fs, fc, make_float2(v.x, v.y));
+                fc = __fadd2_rn(fc, make_float2(v.z, v.w));
             }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                r += __shfl_down_sync(PQG_FULL_MASK, r, off);
-                i += __shfl_down_sync(PQG_FULL_MASK, i, off);
-            }
-            if (lane == 0) store_partial(A.partials, pr->part_begin + local * n_out + l, ddv{r, 0.0}, ddv{i, 0.0});
+            store_partial(A.partials, pr->part_begin + local * n_out + l,
+                          ddv{static_cast<double>(fs.x), static_cast<double>(fc.x)},
+                          ddv{static_cast<double>(fs.y), static_cast<double>(fc.y)});
         }
+        __syncwarp();  // the slices are read before the next item clears them
     }
 }
 
