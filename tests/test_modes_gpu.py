@@ -120,3 +120,24 @@ def test_batch_mixed_column_counts(engine):
         for b in range(len(R)):
             dd = oracle.permanent(U, R[b], C[b])
             assert abs(got[b] - dd) <= _tol(U, R[b], C[b], dd), (mode, b)
+
+
+def test_auto_runs_the_fp64_walk_for_small_plans(engine):
+    """Under "auto", a plain complex128 plan of at most 2^16 Gray-code steps runs
+    the FP64 walk (exact to FP64 there, where the double-float walk rounds the
+    scaled matrix to 2^-47); larger plans and an explicit "df" run the
+    double-float walk."""
+    from piquasso_gb300 import _lib
+
+    for n, want in ((10, "plain_fp64_unit"), (17, "plain_fp64_unit"), (18, "plain_df_unit"), (22, "plain_df_unit")):
+        U = haar_unitary(2 * n, 70 + n)[:n, :n].copy()
+        o = np.ones(n, dtype=int)
+        hi, _ = engine.permanent_dd(U, o, o, mode="auto")
+        assert _lib.last_walk_kernel() == (want, n), (n, _lib.last_walk_kernel())
+        dd = oracle.permanent(U, o, o)
+        assert abs(hi - dd) <= _tol(U, o, o, dd)
+    U = haar_unitary(20, 3)[:10, :10].copy()
+    o = np.ones(10, dtype=int)
+    engine.permanent_dd(U, o, o, mode="df")
+    assert _lib.last_walk_kernel() == ("plain_df_unit", 10)
+    assert abs(complex(engine.permanent(np.array([[4.2]]), [1], [1])) - 4.2) <= 4.2e-15
