@@ -231,7 +231,8 @@ def headline_config(n, dtype, world):
     return {"workload": "permanent n=%d %s, leading block of seeded %dx%d Haar unitary (seed 0), unit "
                         "multiplicities, one permanent per step" % (n, "complex128" if dtype == "c128" else
                                                                     "complex64", 2 * n, 2 * n),
-            "n": n, "dtype": dtype, "parallelism": "replicas" if world > 1 else "1gpu"}
+            "n": n, "dtype": dtype, "parallelism": "replicas" if world > 1 else "1gpu",
+            "l2": "GPU arm: L2 flushed before each timed step (a 256 MB write)"}
 
 
 def run_reference(args, world, rank, pg):
