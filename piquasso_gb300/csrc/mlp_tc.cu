@@ -198,30 +198,36 @@ __device__ __forceinline__ float gelu_grad(float x) {
     return cdf + x * pdf;
 }
 
-// One group of 32 (or a last 16) accumulator columns of a warp's 32 rows
-// (row `lane` of the group in v): through the padded 32 x 33 `tile` so that
-// the stores write whole row segments, then the fused epilogue.  rows_base:
-// the global row of the warp's first row; col0: the group's first column.
-__device__ __forceinline__ void epilogue_group(const TcArgs &g, float *tile, const float (&v)[32], int ncol,
-                                               int64_t rows_base, int64_t col0, float *cbase, bool vec_ok,
-                                               int lane) {
-    for (int q = 0; q < ncol; ++q) tile[lane * 33 + q] = v[q];
+// One group of W (32 or 16; the one-tile kernel's last group may hold 16 of
+// 32) accumulator columns of a warp's 32 rows (row `lane` of the group in v):
+// through the padded 32 x (W + 1) `tile` so that the stores write whole row
+// segments, then the fused epilogue.  rows_base: the global row of the warp's
+// first row; col0: the group's first column.  Every element takes the same
+// operations whatever W, so kernels with different W agree bit for bit.
+template <int W>
+__device__ __forceinline__ void epilogue_group_w(const TcArgs &g, float *tile, const float (&v)[W], int ncol,
+                                                 int64_t rows_base, int64_t col0, float *cbase, bool vec_ok,
+                                                 int lane) {
+    constexpr int S = W + 1;       // tile row stride (odd: conflict-free column writes)
+    constexpr int QPR = W / 4;     // column quads per row
+    constexpr int RSTEP = 32 / QPR;  // rows between a lane's rows in the fast path
+    for (int q = 0; q < ncol; ++q) tile[lane * S + q] = v[q];
     __syncwarp();
-    if (ncol == 32 && vec_ok && rows_base + 32 <= g.M && col0 + 32 <= g.N) {
-        // a whole 32 x 32 group: lane takes column quad q = lane % 8 of rows
-        // lane / 8, + 4, ..., + 28 (the same operations per element as below,
+    if (ncol == W && vec_ok && rows_base + 32 <= g.M && col0 + W <= g.N) {
+        // a whole 32 x W group: lane takes column quad q = lane % QPR of rows
+        // lane / QPR, + RSTEP, ... (the same operations per element as below,
         // with the column, its bias and the row stride fixed per lane)
-        const int q = lane & 7, r0 = lane >> 3;
+        const int q = lane % QPR, r0 = lane / QPR;
         const int64_t col = col0 + 4 * q;
         float4 bb = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) bb = *reinterpret_cast<const float4 *>(g.bias + col);
         int64_t at = (rows_base + r0) * g.N + col;
-        const int64_t step = 4 * g.N;
+        const int64_t step = RSTEP * g.N;
 #pragma unroll 2
-        for (int r = r0; r < 32; r += 4, at += step) {
+        for (int r = r0; r < 32; r += RSTEP, at += step) {
             float x[4];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) x[k] = tile[r * 33 + 4 * q + k];
+            for (int k = 0; k < 4; ++k) x[k] = tile[r * S + 4 * q + k];
             if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) {
                 x[0] += bb.x, x[1] += bb.y, x[2] += bb.z, x[3] += bb.w;
             } else if (g.epi == TC_EPI_DGELU) {
@@ -249,7 +255,7 @@ __device__ __forceinline__ void epilogue_group(const TcArgs &g, float *tile, con
         if (row >= g.M || col >= g.N) continue;
         float x[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) x[k] = tile[r * 33 + 4 * q + k];
+        for (int k = 0; k < 4; ++k) x[k] = tile[r * S + 4 * q + k];
         const int64_t at = row * g.N + col;
         if (vec_ok && col + 3 < g.N) {
             if (g.epi == TC_EPI_BIAS_GELU || g.epi == TC_EPI_BIAS_F32) {
@@ -280,6 +286,12 @@ __device__ __forceinline__ void epilogue_group(const TcArgs &g, float *tile, con
             }
         }
     }
+}
+
+__device__ __forceinline__ void epilogue_group(const TcArgs &g, float *tile, const float (&v)[32], int ncol,
+                                               int64_t rows_base, int64_t col0, float *cbase, bool vec_ok,
+                                               int lane) {
+    epilogue_group_w<32>(g, tile, v, ncol, rows_base, col0, cbase, vec_ok, lane);
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -410,12 +422,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //           tile i reads one accumulator while the MMAs of tile i + 1 fill the
 //           other; tcgen05.commit signals a stage's release and an
 //           accumulator's completion;
-//   warps 2-17  epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
+//   warps 2-25  epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
 //           lane quarter its position allows), i.e. those rows of the tile;
-//           the four warps of a quarter take every fourth 32-column group.
-//           Each applies the same epilogue as gemm_tc (epilogue_group) and
-//           hands the accumulator back (one arrival per warp).  Sixteen warps
-//           keep the stores and the GELU's latencies overlapped.
+//           the six warps of a quarter take every sixth 16-column group (at
+//           most three of a 256-column tile, where sixteen warps on 32-column
+//           groups took two of 32: the epilogue's latency, not its issue,
+//           sets the kernel's time).  Each applies the same epilogue as
+//           gemm_tc (epilogue_group_w, 16-column staging tiles) and hands the
+//           accumulator back (one arrival per warp).
 // The MMAs of a tile accumulate the K chunks in gemm_tc's order and the
 // epilogue performs the same operations, so the results are identical bit for
 // bit.  Every wait is bounded; a wait that runs out records an error code, the
@@ -423,8 +437,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // its TMEM the producer waits for the copies it issued and the issuer for its
 // MMAs.
 constexpr int PT_STAGES = 1;
-constexpr int PT_EPI_WARPS = 16;
+constexpr int PT_EPI_WARPS = 24;
 constexpr int PT_THREADS = 32 * (2 + PT_EPI_WARPS);
+constexpr int PT_GROUP = 16;                       // accumulator columns an epilogue step takes
+constexpr int PT_TILE_FLOATS = 32 * (PT_GROUP + 1);  // a warp's staging tile, 32 x 17 floats
 
 __global__ void __launch_bounds__(PT_THREADS, 1)
     gemm_tc_persistent(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
@@ -437,7 +453,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     const uint32_t sB = base;                                       // nkc chunks of BN x 64
     const uint32_t sA = sB + static_cast<uint32_t>(nkc) * b_chunk;  // PT_STAGES x 16 KB
     const uint32_t sT = sA + PT_STAGES * TC_A_BYTES;  // PT_EPI_WARPS x (32 x 33) floats, the epilogue tiles
-    const uint32_t bars = sT + PT_EPI_WARPS * 32 * 33 * 4;
+    const uint32_t bars = sT + PT_EPI_WARPS * PT_TILE_FLOATS * 4;
     // barriers: bfull | full[S] | empty[S] | tfull[2] | tempty[2] | done
     const uint32_t bfull = bars, full0 = bars + 8, empty0 = full0 + 8 * PT_STAGES, tfull0 = empty0 + 8 * PT_STAGES,
                    tempty0 = tfull0 + 16, done = tempty0 + 16;
@@ -534,7 +550,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
         // epilogue warps: TMEM lane quarter q, rows 32 q .. 32 q + 31 of each
         // tile; column groups h, h + 2, ... of 32 columns
         const int q = warp & 3, h = (warp - 2) / 4;
-        float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * 32 * 33;
+        float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * PT_TILE_FLOATS;
         const bool vec_ok = (g.N % 4) == 0;
         uint32_t tl = 0;
         for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++tl) {
@@ -548,18 +564,11 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t taddr =
                 tmem + a * static_cast<uint32_t>(g.tmem_cols) + (static_cast<uint32_t>(q * 32) << 16);
-            for (int j0 = 32 * h; j0 < g.BN; j0 += 32 * (PT_EPI_WARPS / 4)) {
-                const int ncol = g.BN - j0 >= 32 ? 32 : 16;
-                float v[32];
-                if (ncol == 32) {
-                    tmem_ld32(taddr + static_cast<uint32_t>(j0), v);
-                } else {
-                    float hv[16];
-                    tmem_ld16(taddr + static_cast<uint32_t>(j0), hv);
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) v[k] = hv[k];
-                }
-                epilogue_group(g, tile_f, v, ncol, tile * TC_BM + q * 32, j0, g.C, vec_ok, lane);
+            // (BN is a multiple of 16, the MMA's N granularity at M = 128)
+            for (int j0 = PT_GROUP * h; j0 < g.BN; j0 += PT_GROUP * (PT_EPI_WARPS / 4)) {
+                float v[PT_GROUP];
+                tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
+                epilogue_group_w<PT_GROUP>(g, tile_f, v, PT_GROUP, tile * TC_BM + q * 32, j0, g.C, vec_ok, lane);
                 __syncwarp();  // the tile is rewritten by the next group
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -940,7 +949,7 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
     const int sms = device_sms();
     if (epilogue != TC_EPI_SPLITK && N <= 256 && K <= 256 && sms > 0 && row_tiles >= 2 * sms) {
         const size_t psmem = 1024 + static_cast<size_t>((K + TC_BK - 1) / TC_BK) * g.BN * TC_BK * 2 +
-                             PT_STAGES * static_cast<size_t>(TC_A_BYTES) + PT_EPI_WARPS * 32 * 33 * 4 + 128;
+                             PT_STAGES * static_cast<size_t>(TC_A_BYTES) + PT_EPI_WARPS * PT_TILE_FLOATS * 4 + 128;
         static std::once_flag pattr_once;
         static cudaError_t pattr_err = cudaSuccess;
         std::call_once(pattr_once, [] {
