@@ -412,9 +412,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // (one column tile), K <= 256, and many 128-row tiles.  One CTA per SM walks
 // the row tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The whole B operand
 // (BN x K, at most 128 KB) is loaded once per CTA and stays in shared memory;
-// A streams through PT_STAGES 16 KB stages (one: a tile's four chunk loads
-// take a few microseconds, well inside the epilogue of the other
-// accumulator's tile, and the epilogue warps' staging tiles need the room).  Warp roles:
+// A streams through PT_STAGES 16 KB stages (two: with the epilogue on 24
+// warps a second stage measured 10 % faster than one; a third does not fit
+// beside B and the staging tiles).  Warp roles:
 //   warp 0  TMA producer: B once, then A chunk by chunk, each stage refilled
 //           once the MMAs that read it have completed (empty barrier);
 //   warp 1  MMA issuer and TMEM owner: two accumulators of tmem_cols columns
@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // waiting role stops, and the others then run out too; before the CTA frees
 // its TMEM the producer waits for the copies it issued and the issuer for its
 // MMAs.
-constexpr int PT_STAGES = 1;
+constexpr int PT_STAGES = 2;
 constexpr int PT_EPI_WARPS = 24;
 constexpr int PT_THREADS = 32 * (2 + PT_EPI_WARPS);
 constexpr int PT_GROUP = 16;                       // accumulator columns an epilogue step takes
