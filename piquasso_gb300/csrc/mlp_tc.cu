@@ -485,13 +485,37 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
+    // Work units, walked by all three roles in the same order (unit
+    // blockIdx.x, + gridDim.x, ...): whole row tiles, except that when the
+    // last wave would be at most half full (a BN = 256 tile, n_tiles mod
+    // gridDim.x <= gridDim.x / 2), its tiles go as two 128-column halves --
+    // one MMA of N = 128 over the matching half of B each -- so that the last
+    // wave costs about half a tile.  half: -1 whole tile, 0 or 1 the column half.
+    const int64_t grid = gridDim.x;
+    const int64_t rem = n_tiles % grid;
+    const bool split_last = g.BN == 256 && n_tiles > grid && rem > 0 && 2 * rem <= grid;
+    const int64_t n_whole = split_last ? n_tiles - rem : n_tiles;
+    const int64_t n_units = split_last ? n_whole + 2 * rem : n_tiles;
+    auto unit = [&](int64_t u, int64_t &tile, int &half) {
+        if (u < n_whole) {
+            tile = u;
+            half = -1;
+        } else {
+            tile = n_whole + (u - n_whole) / 2;
+            half = static_cast<int>((u - n_whole) & 1);
+        }
+    };
+
     if (warp == 0) {
         if (lane == 0) {
             mbar_expect_tx(bfull, static_cast<uint32_t>(nkc) * b_chunk);
             for (int kc = 0; kc < nkc; ++kc) tma_load_2d(sB + kc * b_chunk, &map_b, kc * TC_BK, 0, bfull);
             uint32_t it = 0;
             bool ok = true;
-            for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x) {
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += grid) {
+                int64_t tile;
+                int half;
+                unit(u, tile, half);
                 for (int kc = 0; kc < nkc; ++kc, ++it) {
                     const uint32_t s = it % PT_STAGES, use = it / PT_STAGES;
                     if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1)) {
@@ -511,11 +535,17 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(g.BN);
+            const uint32_t idesc = idesc_bf16(g.BN), idesc_half = idesc_bf16(128);
             bool ok = mbar_wait(bfull, 0);
             if (!ok) record_error(7);
             uint32_t it = 0, tl = 0;
-            for (int64_t tile = blockIdx.x; tile < n_tiles && ok; tile += gridDim.x, ++tl) {
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += grid, ++tl) {
+                int64_t tile;
+                int half;
+                unit(u, tile, half);
+                // a column half reads B rows 128 half .. + 127: 128 rows of 128 bytes on
+                const uint32_t b_off = half > 0 ? 128u * 128u : 0u;
+                const uint32_t id = half < 0 ? idesc : idesc_half;
                 const uint32_t a = tl & 1, use = tl >> 1;
                 if (use > 0 && !mbar_wait(tempty0 + 8 * a, (use - 1) & 1)) {
                     record_error(8);
@@ -532,11 +562,11 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const uint32_t sa = sA + s * TC_A_BYTES, sb = sB + kc * b_chunk;
+                    const uint32_t sa = sA + s * TC_A_BYTES, sb = sB + kc * b_chunk + b_off;
                     const int64_t kcols = g.K - static_cast<int64_t>(kc) * TC_BK;
                     const int nk = kcols >= TC_BK ? TC_BK / 16 : static_cast<int>((kcols + 15) / 16);
                     for (int kk = 0; kk < nk; ++kk)
-                        umma_bf16(acc, sdesc_sw128(sa + 32u * kk), sdesc_sw128(sb + 32u * kk), idesc,
+                        umma_bf16(acc, sdesc_sw128(sa + 32u * kk), sdesc_sw128(sb + 32u * kk), id,
                                   (kc > 0 || kk > 0) ? 1 : 0);
                     umma_commit(empty0 + 8 * s);
                 }
@@ -553,7 +583,11 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
         float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * PT_TILE_FLOATS;
         const bool vec_ok = (g.N % 4) == 0;
         uint32_t tl = 0;
-        for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++tl) {
+        for (int64_t u = blockIdx.x; u < n_units; u += grid, ++tl) {
+            int64_t tile;
+            int half;
+            unit(u, tile, half);
+            const int ncols = half < 0 ? g.BN : 128, col_base = half > 0 ? 128 : 0;
             const uint32_t a = tl & 1, use = tl >> 1;
             // warp-uniform: the TMEM loads below are .sync.aligned
             const bool have = __all_sync(0xffffffffu, mbar_wait(tfull0 + 8 * a, use & 1));
@@ -565,10 +599,11 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
             const uint32_t taddr =
                 tmem + a * static_cast<uint32_t>(g.tmem_cols) + (static_cast<uint32_t>(q * 32) << 16);
             // (BN is a multiple of 16, the MMA's N granularity at M = 128)
-            for (int j0 = PT_GROUP * h; j0 < g.BN; j0 += PT_GROUP * (PT_EPI_WARPS / 4)) {
+            for (int j0 = PT_GROUP * h; j0 < ncols; j0 += PT_GROUP * (PT_EPI_WARPS / 4)) {
                 float v[PT_GROUP];
                 tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
-                epilogue_group_w<PT_GROUP>(g, tile_f, v, PT_GROUP, tile * TC_BM + q * 32, j0, g.C, vec_ok, lane);
+                epilogue_group_w<PT_GROUP>(g, tile_f, v, PT_GROUP, tile * TC_BM + q * 32, col_base + j0, g.C, vec_ok,
+                                           lane);
                 __syncwarp();  // the tile is rewritten by the next group
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
