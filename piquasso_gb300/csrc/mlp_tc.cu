@@ -110,6 +110,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+// Tile store shared -> global through the bulk-async group of the issuing
+// thread; elements outside the tensor map's extent are not written.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int32_t x, int32_t y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(src), "r"(x), "r"(y)
+                 : "memory");
+}
+
 // Shared-memory matrix descriptor of a K-major operand tile in the 128-byte
 // swizzle layout: rows of 128 bytes, 8-row groups 1024 bytes apart (stride
 // byte offset), the leading byte offset unused (one swizzle atom spans the
@@ -422,7 +431,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //           tile i reads one accumulator while the MMAs of tile i + 1 fill the
 //           other; tcgen05.commit signals a stage's release and an
 //           accumulator's completion;
-//   warps 2-25  epilogue: warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
+//   warps 2-25  epilogue (2-17 in the kStore form below, four a quarter,
+//           every fourth group): warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
 //           lane quarter its position allows), i.e. those rows of the tile;
 //           the six warps of a quarter take every sixth 16-column group (at
 //           most three of a 256-column tile, where sixteen warps on 32-column
@@ -436,26 +446,60 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // waiting role stops, and the others then run out too; before the CTA frees
 // its TMEM the producer waits for the copies it issued and the issuer for its
 // MMAs.
+//
+// kStore (epilogues F32, BIAS_F32 and BIAS_GELU at N a multiple of 16): each
+// lane applies the epilogue to its own row of the 16-column group in
+// registers and writes it to the warp's staging tiles -- FP32 32 x 16 in the
+// 64-byte swizzle layout, BF16 32 x 16 in the 32-byte one, so that the row
+// writes are free of bank conflicts -- and one lane hands the tiles to the TMA
+// unit as tensor stores (rows past M are not written).  The next group's
+// TMEM load and arithmetic run while the store reads the tiles; the tiles are
+// rewritten once it has (wait_group.read).  Per element the operations are
+// those of epilogue_group_w, so the two forms agree bit for bit.  Sixteen
+// warps suffice for it, and their 48 KB of tiles leave room for three A
+// stages beside B (at 65536 x 256 x 256: 35.5 us with the 24-warp form, 33.4
+// with this one on two stages, 31.4 on three; 12 or 20 warps no faster).
 constexpr int PT_STAGES = 2;
+constexpr int PT_STORE_STAGES = 3;
 constexpr int PT_EPI_WARPS = 24;
-constexpr int PT_THREADS = 32 * (2 + PT_EPI_WARPS);
+constexpr int PT_STORE_EPI_WARPS = 16;
 constexpr int PT_GROUP = 16;                       // accumulator columns an epilogue step takes
 constexpr int PT_TILE_FLOATS = 32 * (PT_GROUP + 1);  // a warp's staging tile, 32 x 17 floats
+constexpr int PT_STORE_TILE_BYTES = 32 * PT_GROUP * 4 + 32 * PT_GROUP * 2;  // FP32 + BF16 tiles, 3 KB
 
-__global__ void __launch_bounds__(PT_THREADS, 1)
+template <bool kStore>
+__host__ __device__ constexpr int pt_epi_warps() {
+    return kStore ? PT_STORE_EPI_WARPS : PT_EPI_WARPS;
+}
+
+template <bool kStore>
+__host__ __device__ constexpr int pt_stages() {
+    return kStore ? PT_STORE_STAGES : PT_STAGES;
+}
+
+template <bool kStore>
+__host__ __device__ constexpr size_t pt_tile_bytes() {
+    return kStore ? static_cast<size_t>(PT_STORE_EPI_WARPS) * PT_STORE_TILE_BYTES
+                  : static_cast<size_t>(PT_EPI_WARPS) * PT_TILE_FLOATS * 4;
+}
+
+template <bool kStore>
+__global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
     gemm_tc_persistent(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                       const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_cb,
                        TcArgs g) {
+    constexpr int EW = pt_epi_warps<kStore>(), NS = pt_stages<kStore>();
     extern __shared__ uint8_t tc_smem_raw[];
     const uint32_t raw = smem_u32(tc_smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     const int nkc = static_cast<int>((g.K + TC_BK - 1) / TC_BK);  // K chunks (<= 4)
     const uint32_t b_chunk = static_cast<uint32_t>(g.BN) * TC_BK * 2;
     const uint32_t sB = base;                                       // nkc chunks of BN x 64
-    const uint32_t sA = sB + static_cast<uint32_t>(nkc) * b_chunk;  // PT_STAGES x 16 KB
-    const uint32_t sT = sA + PT_STAGES * TC_A_BYTES;  // PT_EPI_WARPS x (32 x 33) floats, the epilogue tiles
-    const uint32_t bars = sT + PT_EPI_WARPS * PT_TILE_FLOATS * 4;
+    const uint32_t sA = sB + static_cast<uint32_t>(nkc) * b_chunk;  // NS x 16 KB
+    const uint32_t sT = sA + NS * TC_A_BYTES;  // the epilogue warps' staging tiles (1024-byte aligned)
+    const uint32_t bars = sT + static_cast<uint32_t>(pt_tile_bytes<kStore>());
     // barriers: bfull | full[S] | empty[S] | tfull[2] | tempty[2] | done
-    const uint32_t bfull = bars, full0 = bars + 8, empty0 = full0 + 8 * PT_STAGES, tfull0 = empty0 + 8 * PT_STAGES,
+    const uint32_t bfull = bars, full0 = bars + 8, empty0 = full0 + 8 * NS, tfull0 = empty0 + 8 * NS,
                    tempty0 = tfull0 + 16, done = tempty0 + 16;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem_raw + (done + 8 - raw));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -463,13 +507,13 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
 
     if (tid == 0) {
         mbar_init(bfull, 1);
-        for (int s = 0; s < PT_STAGES; ++s) {
+        for (int s = 0; s < NS; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(tfull0 + 8 * a, 1);
-            mbar_init(tempty0 + 8 * a, PT_EPI_WARPS);
+            mbar_init(tempty0 + 8 * a, EW);
         }
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -517,7 +561,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
                 int half;
                 unit(u, tile, half);
                 for (int kc = 0; kc < nkc; ++kc, ++it) {
-                    const uint32_t s = it % PT_STAGES, use = it / PT_STAGES;
+                    const uint32_t s = it % NS, use = it / NS;
                     if (use > 0 && !mbar_wait(empty0 + 8 * s, (use - 1) & 1)) {
                         record_error(5);
                         ok = false;
@@ -529,8 +573,8 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
                 }
             }
             // every copy issued has landed before the CTA can leave
-            for (uint32_t k = it > PT_STAGES ? it - PT_STAGES : 0; k < it; ++k)
-                if (!mbar_wait(full0 + 8 * (k % PT_STAGES), (k / PT_STAGES) & 1)) record_error(6);
+            for (uint32_t k = it > NS ? it - NS : 0; k < it; ++k)
+                if (!mbar_wait(full0 + 8 * (k % NS), (k / NS) & 1)) record_error(6);
             if (!mbar_wait(bfull, 0)) record_error(6);
         }
     } else if (warp == 1) {
@@ -555,8 +599,8 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc = tmem + a * static_cast<uint32_t>(g.tmem_cols);
                 for (int kc = 0; kc < nkc; ++kc, ++it) {
-                    const uint32_t s = it % PT_STAGES;
-                    if (!mbar_wait(full0 + 8 * s, (it / PT_STAGES) & 1)) {
+                    const uint32_t s = it % NS;
+                    if (!mbar_wait(full0 + 8 * s, (it / NS) & 1)) {
                         record_error(9);
                         ok = false;
                         break;
@@ -581,6 +625,7 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
         // tile; column groups h, h + 2, ... of 32 columns
         const int q = warp & 3, h = (warp - 2) / 4;
         float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * PT_TILE_FLOATS;
+        const uint32_t st_c = sT + static_cast<uint32_t>(warp - 2) * PT_STORE_TILE_BYTES, st_b = st_c + 2048;
         const bool vec_ok = (g.N % 4) == 0;
         uint32_t tl = 0;
         for (int64_t u = blockIdx.x; u < n_units; u += grid, ++tl) {
@@ -599,17 +644,68 @@ __global__ void __launch_bounds__(PT_THREADS, 1)
             const uint32_t taddr =
                 tmem + a * static_cast<uint32_t>(g.tmem_cols) + (static_cast<uint32_t>(q * 32) << 16);
             // (BN is a multiple of 16, the MMA's N granularity at M = 128)
-            for (int j0 = PT_GROUP * h; j0 < ncols; j0 += PT_GROUP * (PT_EPI_WARPS / 4)) {
+            for (int j0 = PT_GROUP * h; j0 < ncols; j0 += PT_GROUP * (EW / 4)) {
                 float v[PT_GROUP];
                 tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
-                epilogue_group_w<PT_GROUP>(g, tile_f, v, PT_GROUP, tile * TC_BM + q * 32, col_base + j0, g.C, vec_ok,
-                                           lane);
-                __syncwarp();  // the tile is rewritten by the next group
+                if constexpr (kStore) {
+                    const int col0 = col_base + j0;
+                    const bool bias = g.epi != TC_EPI_F32, act = g.epi == TC_EPI_BIAS_GELU;
+                    if (bias) {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const float4 bb = __ldg(reinterpret_cast<const float4 *>(g.bias + col0) + c);
+                            v[4 * c] += bb.x, v[4 * c + 1] += bb.y, v[4 * c + 2] += bb.z, v[4 * c + 3] += bb.w;
+                        }
+                    }
+                    uint32_t pb[PT_GROUP / 2];
+                    if (act) {
+#pragma unroll
+                        for (int k = 0; k < PT_GROUP / 2; ++k) {
+                            __nv_bfloat162 t2 = __floats2bfloat162_rn(gelu(v[2 * k]), gelu(v[2 * k + 1]));
+                            pb[k] = *reinterpret_cast<uint32_t *>(&t2);
+                        }
+                    }
+                    // the previous group's stores have read the tiles
+                    if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                    __syncwarp();
+                    // row `lane`: 64 bytes of FP32, 16-byte chunk c at c ^ (lane / 2 mod 4)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const uint32_t at = st_c + 64u * lane + ((static_cast<uint32_t>(c) ^ ((lane >> 1) & 3)) << 4);
+                        asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(at), "f"(v[4 * c]),
+                                     "f"(v[4 * c + 1]), "f"(v[4 * c + 2]), "f"(v[4 * c + 3])
+                                     : "memory");
+                    }
+                    // 32 bytes of BF16, chunk c at c ^ (lane / 4 mod 2)
+                    if (act) {
+#pragma unroll
+                        for (int c = 0; c < 2; ++c) {
+                            const uint32_t at = st_b + 32u * lane + ((static_cast<uint32_t>(c) ^ ((lane >> 2) & 1)) << 4);
+                            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(at), "r"(pb[4 * c]),
+                                         "r"(pb[4 * c + 1]), "r"(pb[4 * c + 2]), "r"(pb[4 * c + 3])
+                                         : "memory");
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) {
+                        const int32_t y = static_cast<int32_t>(tile * TC_BM + q * 32);
+                        tma_store_2d(&map_c, st_c, col0, y);
+                        if (act) tma_store_2d(&map_cb, st_b, col0, y);
+                        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                    }
+                } else {
+                    epilogue_group_w<PT_GROUP>(g, tile_f, v, PT_GROUP, tile * TC_BM + q * 32, col_base + j0, g.C,
+                                               vec_ok, lane);
+                    __syncwarp();  // the tile is rewritten by the next group
+                }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(tempty0 + 8 * a);
         }
+        // the tensor stores have completed before the CTA leaves
+        if (kStore && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -920,6 +1016,48 @@ int make_map(CUtensorMap *map, const void *p, int64_t rows, int64_t k, int64_t l
     return PQG_OK;
 }
 
+// Tensor map of the row-major output [rows x cols] (dense rows: stride cols
+// elements, FP32 or BF16) for the persistent kernel's tensor stores: boxes of
+// 16 columns x 32 rows, in the staging tiles' swizzle (64 bytes for FP32, 32
+// for BF16: one box row).
+int make_store_map(CUtensorMap *map, void *p, int64_t rows, int64_t cols, bool bf16) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return fail(PQG_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(cols) * (bf16 ? 2 : 4)};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(PT_GROUP), 32};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, p, dims,
+                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     bf16 ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld output", static_cast<int>(r),
+                 static_cast<long long>(rows), static_cast<long long>(cols));
+        return fail(PQG_ERR_INVALID, buf);
+    }
+    return PQG_OK;
+}
+
+template <bool kStore>
+int launch_persistent(const CUtensorMap &ma, const CUtensorMap &mb, const CUtensorMap &mc, const CUtensorMap &mcb,
+                      const TcArgs &g, int sms, cudaStream_t s) {
+    const size_t psmem = 1024 + static_cast<size_t>((g.K + TC_BK - 1) / TC_BK) * g.BN * TC_BK * 2 +
+                         pt_stages<kStore>() * static_cast<size_t>(TC_A_BYTES) + pt_tile_bytes<kStore>() + 128;
+    static std::once_flag pattr_once;
+    static cudaError_t pattr_err = cudaSuccess;
+    std::call_once(pattr_once, [] {
+        pattr_err = cudaFuncSetAttribute(gemm_tc_persistent<kStore>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         227 * 1024);
+    });
+    if (pattr_err != cudaSuccess) return fail_cuda(pattr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
+    gemm_tc_persistent<kStore>
+        <<<static_cast<unsigned>(sms), 32 * (2 + pt_epi_warps<kStore>()), psmem, s>>>(ma, mb, mc, mcb, g);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_gemm_tc");
+}
+
 }  // namespace
 
 extern "C" {
@@ -983,18 +1121,24 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
     const int64_t row_tiles = (M + TC_BM - 1) / TC_BM;
     const int sms = device_sms();
     if (epilogue != TC_EPI_SPLITK && N <= 256 && K <= 256 && sms > 0 && row_tiles >= 2 * sms) {
-        const size_t psmem = 1024 + static_cast<size_t>((K + TC_BK - 1) / TC_BK) * g.BN * TC_BK * 2 +
-                             PT_STAGES * static_cast<size_t>(TC_A_BYTES) + PT_EPI_WARPS * PT_TILE_FLOATS * 4 + 128;
-        static std::once_flag pattr_once;
-        static cudaError_t pattr_err = cudaSuccess;
-        std::call_once(pattr_once, [] {
-            pattr_err = cudaFuncSetAttribute(gemm_tc_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             227 * 1024);
-        });
-        if (pattr_err != cudaSuccess) return fail_cuda(pattr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
-        gemm_tc_persistent<<<static_cast<unsigned>(sms), PT_THREADS, psmem, s>>>(ma, mb, g);
-        cudaError_t e = cudaGetLastError();
-        return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_gemm_tc");
+        // tensor stores where the outputs allow them: 16-column groups that
+        // end inside the rows, 16-byte aligned bases (and bias, read as float4)
+        const auto al16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+        const bool store = (epilogue == TC_EPI_F32 || epilogue == TC_EPI_BIAS_F32 || epilogue == TC_EPI_BIAS_GELU) &&
+                           N % PT_GROUP == 0 && al16(c) && (epilogue == TC_EPI_F32 || al16(bias)) &&
+                           (epilogue != TC_EPI_BIAS_GELU || al16(c_bf16));
+        if (store) {
+            CUtensorMap mc, mcb;
+            st = make_store_map(&mc, c, M, N, false);
+            if (st) return st;
+            mcb = mc;
+            if (epilogue == TC_EPI_BIAS_GELU) {
+                st = make_store_map(&mcb, c_bf16, M, N, true);
+                if (st) return st;
+            }
+            return launch_persistent<true>(ma, mb, mc, mcb, g, sms, s);
+        }
+        return launch_persistent<false>(ma, mb, ma, ma, g, sms, s);
     }
     dim3 grid(static_cast<unsigned>((N + g.BN - 1) / g.BN), static_cast<unsigned>((M + TC_BM - 1) / TC_BM),
               static_cast<unsigned>(nsplit));

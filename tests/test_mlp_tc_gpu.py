@@ -150,7 +150,7 @@ def test_bias_grad(L, M, N):
 
 
 @pytest.mark.parametrize("M,N,K", [(65536, 256, 256), (40000, 256, 16), (50001, 48, 200), (39000, 8, 256)])
-@pytest.mark.parametrize("epi", [0, 1, 4])
+@pytest.mark.parametrize("epi", [0, 1, 3, 4])
 def test_persistent_kernel_is_bitwise_the_tile_kernel(L, M, N, K, epi):
     """From 2 x SMs row tiles on (K <= 256, N <= 256, no split-K) the GEMM runs
     as the persistent kernel (B resident in shared memory, two TMEM
@@ -171,7 +171,7 @@ def test_persistent_kernel_is_bitwise_the_tile_kernel(L, M, N, K, epi):
             m = min(step, M - r0)
             a = A[r0:r0 + m]
             assert L.pqg_mlp_gemm_tc(_v(a), K, _v(B), K, m, N, K, epi, _f(C[r0:r0 + m]),
-                                     _v(Cb[r0:r0 + m]) if epi else None, _f(bias) if epi == 1 else None,
+                                     _v(Cb[r0:r0 + m]) if epi in (1, 4) else None, _f(bias) if epi in (1, 3) else None,
                                      _f(pre[r0:r0 + m]) if epi == 4 else None, None, 0, None) == 0
         torch.cuda.synchronize()
         assert _status(L) == 0
