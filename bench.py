@@ -557,7 +557,7 @@ def bench_training(args):
                              "gb_per_s": moved / (gms * 1e-3) / 1e9,
                              "hbm_frac": moved / (gms * 1e-3) / 1e9 / hbm_gbs() if hbm_gbs() else None,
                              "l2": "flushed before each launch (256 MB write)",
-                             "kernel": "persistent (65536 rows >= 2 x SMs tiles): B resident, two TMEM accumulators",
+                             "kernel": "persistent (65536 rows >= 2 x SMs tiles): B resident, two TMEM accumulators, TMA tensor-store epilogue",
                              "note": "memory-bound at this shape: 64 flop/byte of operands and outputs"}}
 
 
