@@ -781,7 +781,9 @@ def profile_case(name):
                    graph replays;
       draw2048   — the exact sampler's fused step (Laplace permanents + pmf +
                    draw) for 2048 shots after 16 photons at n=24, d=48, 3 calls;
-      laplace24c128 — laplace24 in complex128 (the double-float Laplace walk)."""
+      laplace24c128 — laplace24 in complex128 (the double-float Laplace walk);
+      train65k   — Adam steps of the learned proposal on a 65536-row batch
+                   (forward, backward, bias gradients, Adam), 4 steps."""
     import ctypes
 
     import __graft_entry__
@@ -806,6 +808,18 @@ def profile_case(name):
         for _ in range(6):
             assert L.pqg_mlp_gemm_tc(vp(A), 256, vp(B), 256, rows, 256, 256, 1, fp(C), vp(Cb), fp(bias), None, None,
                                      0, None) == 0
+        torch.cuda.synchronize()
+    elif name == "train65k":
+        rows = 65536
+        g = torch.Generator(device="cuda").manual_seed(0)
+        X = torch.randn(rows, proposal.F, device="cuda", generator=g).to(torch.bfloat16)
+        hi = torch.full((rows,), proposal.CAP, dtype=torch.int8, device="cuda")
+        lo = torch.zeros(rows, dtype=torch.int8, device="cuda")
+        tgt = torch.randint(0, proposal.CLASSES, (rows,), device="cuda", generator=g).to(torch.int8)
+        mlp = proposal.MLP(seed=0)
+        for _ in range(4):
+            loss, gW, gb = mlp.loss_and_grads(X, lo, hi, tgt)
+            mlp.adam(gW, gb)
         torch.cuda.synchronize()
     elif name == "target1024":
         U = workloads.haar_unitary(48, 3)

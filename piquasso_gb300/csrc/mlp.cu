@@ -39,12 +39,24 @@ __global__ void bias_partial(const float *__restrict__ d, int64_t M, int64_t N, 
     }
 }
 
+// The sum over the row chunks: 32 chunk lanes per column (lane y takes chunks
+// y, y + 32, ...), then the 32 lane sums in order -- a fixed order, and
+// independent loads instead of one thread's chain of `chunks` dependent adds.
+constexpr int BIAS_LANES = 32;
+
 __global__ void bias_final(const float *__restrict__ part, int64_t chunks, int64_t N, float *__restrict__ db) {
-    const int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (c >= N) return;
-    float s = 0.0f;
-    for (int64_t k = 0; k < chunks; ++k) s += part[k * N + c];
-    db[c] = s;
+    __shared__ float s[BIAS_LANES][33];
+    const int64_t c = static_cast<int64_t>(blockIdx.x) * 32 + threadIdx.x;
+    float acc = 0.0f;
+    if (c < N)
+        for (int64_t k = threadIdx.y; k < chunks; k += BIAS_LANES) acc += part[k * N + c];
+    s[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < N) {
+        float t = 0.0f;
+        for (int k = 0; k < BIAS_LANES; ++k) t += s[k][threadIdx.x];
+        db[c] = t;
+    }
 }
 
 // Masked softmax cross-entropy over the first `classes` of `ld` logits per row.
@@ -116,7 +128,7 @@ int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, float *sc
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     bias_partial<<<dim3(static_cast<unsigned>((N + 31) / 32), static_cast<unsigned>(chunks)), dim3(32, 8), 0, s>>>(
         d, M, N, scratch);
-    bias_final<<<static_cast<unsigned>((N + 127) / 128), 128, 0, s>>>(scratch, chunks, N, db);
+    bias_final<<<static_cast<unsigned>((N + 31) / 32), dim3(32, BIAS_LANES), 0, s>>>(scratch, chunks, N, db);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_bias_grad");
 }

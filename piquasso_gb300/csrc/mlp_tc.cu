@@ -447,9 +447,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // its TMEM the producer waits for the copies it issued and the issuer for its
 // MMAs.
 //
-// kStore (epilogues F32, BIAS_F32 and BIAS_GELU at N a multiple of 16): each
-// lane applies the epilogue to its own row of the 16-column group in
-// registers and writes it to the warp's staging tiles -- FP32 32 x 16 in the
+// kStore (every epilogue but split-K, at N a multiple of 16 with 16-byte
+// aligned outputs, bias and pre): each lane applies the epilogue to its own
+// row of the 16-column group in registers (DGELU reads the row's 16 values of
+// pre, 64 contiguous bytes) and writes it to the warp's staging tiles -- FP32 32 x 16 in the
 // 64-byte swizzle layout, BF16 32 x 16 in the 32-byte one, so that the row
 // writes are free of bank conflicts -- and one lane hands the tiles to the TMA
 // unit as tensor stores (rows past M are not written).  The next group's
@@ -646,22 +647,39 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
             // (BN is a multiple of 16, the MMA's N granularity at M = 128)
             for (int j0 = PT_GROUP * h; j0 < ncols; j0 += PT_GROUP * (EW / 4)) {
                 float v[PT_GROUP];
-                tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
                 if constexpr (kStore) {
                     const int col0 = col_base + j0;
-                    const bool bias = g.epi != TC_EPI_F32, act = g.epi == TC_EPI_BIAS_GELU;
+                    const bool bias = g.epi == TC_EPI_BIAS_F32 || g.epi == TC_EPI_BIAS_GELU,
+                               act = g.epi == TC_EPI_BIAS_GELU, dgelu = g.epi == TC_EPI_DGELU;
+                    // DGELU: the lane's own row of pre (64 contiguous bytes), loaded
+                    // before the TMEM load so that the two latencies overlap
+                    float4 pp[4];
+                    if (dgelu) {
+                        const int64_t row = tile * TC_BM + q * 32 + lane;
+                        const float4 *src = reinterpret_cast<const float4 *>(g.pre + row * g.N + col0);
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) pp[c] = row < g.M ? __ldg(src + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                    tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
                     if (bias) {
 #pragma unroll
                         for (int c = 0; c < 4; ++c) {
                             const float4 bb = __ldg(reinterpret_cast<const float4 *>(g.bias + col0) + c);
                             v[4 * c] += bb.x, v[4 * c + 1] += bb.y, v[4 * c + 2] += bb.z, v[4 * c + 3] += bb.w;
                         }
+                    } else if (dgelu) {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            v[4 * c] *= gelu_grad(pp[c].x), v[4 * c + 1] *= gelu_grad(pp[c].y);
+                            v[4 * c + 2] *= gelu_grad(pp[c].z), v[4 * c + 3] *= gelu_grad(pp[c].w);
+                        }
                     }
                     uint32_t pb[PT_GROUP / 2];
-                    if (act) {
+                    if (act || dgelu) {
 #pragma unroll
                         for (int k = 0; k < PT_GROUP / 2; ++k) {
-                            __nv_bfloat162 t2 = __floats2bfloat162_rn(gelu(v[2 * k]), gelu(v[2 * k + 1]));
+                            __nv_bfloat162 t2 = act ? __floats2bfloat162_rn(gelu(v[2 * k]), gelu(v[2 * k + 1]))
+                                                    : __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
                             pb[k] = *reinterpret_cast<uint32_t *>(&t2);
                         }
                     }
@@ -677,7 +695,7 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
                                      : "memory");
                     }
                     // 32 bytes of BF16, chunk c at c ^ (lane / 4 mod 2)
-                    if (act) {
+                    if (act || dgelu) {
 #pragma unroll
                         for (int c = 0; c < 2; ++c) {
                             const uint32_t at = st_b + 32u * lane + ((static_cast<uint32_t>(c) ^ ((lane >> 2) & 1)) << 4);
@@ -691,10 +709,11 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
                     if (lane == 0) {
                         const int32_t y = static_cast<int32_t>(tile * TC_BM + q * 32);
                         tma_store_2d(&map_c, st_c, col0, y);
-                        if (act) tma_store_2d(&map_cb, st_b, col0, y);
+                        if (act || dgelu) tma_store_2d(&map_cb, st_b, col0, y);
                         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                     }
                 } else {
+                    tmem_ld16(taddr + static_cast<uint32_t>(j0), v);
                     epilogue_group_w<PT_GROUP>(g, tile_f, v, PT_GROUP, tile * TC_BM + q * 32, col_base + j0, g.C,
                                                vec_ok, lane);
                     __syncwarp();  // the tile is rewritten by the next group
@@ -728,6 +747,39 @@ __global__ void transpose_bf16(const __nv_bfloat16 *__restrict__ src, int64_t ro
         const int64_t c = c0 + i, r = r0 + threadIdx.x;
         if (r < rows && c < cols) dst[c * ld_dst + r] = t[threadIdx.x][i];
     }
+}
+
+// dst[c][r] = src[r][c] for BF16 matrices of whole 64 x 64 tiles with 16-byte
+// aligned rows: each row of a tile is read as eight 16-byte loads into a
+// padded shared tile (rows of 144 bytes), and each thread writes 32
+// contiguous bytes (one sector) of an output row, gathered down a column of
+// the tile (the warp's lanes on 32 consecutive columns: conflict-free).  The
+// 32 x 32 kernel above, two bytes per access, takes every other shape.
+constexpr int TT_EDGE = 64;
+constexpr int TT_PAD = 72;
+
+__global__ void __launch_bounds__(256) transpose_bf16_64(const uint16_t *__restrict__ src, int64_t ld_src,
+                                                         uint16_t *__restrict__ dst, int64_t ld_dst) {
+    __shared__ __align__(16) uint16_t t[TT_EDGE][TT_PAD];
+    const int64_t r0 = static_cast<int64_t>(blockIdx.y) * TT_EDGE, c0 = static_cast<int64_t>(blockIdx.x) * TT_EDGE;
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int r = tid / 8 + 32 * h, ch = tid % 8;
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(src + (r0 + r) * ld_src + c0) + ch);
+        *reinterpret_cast<uint4 *>(&t[r][8 * ch]) = v;
+    }
+    __syncthreads();
+    // tile column c -> output row c0 + c, its elements 16 p .. 16 p + 15
+    const int lane = tid & 31, warp = tid >> 5;
+    const int c = lane + 32 * (warp & 1), p = warp >> 1;
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        w[k] = static_cast<uint32_t>(t[16 * p + 2 * k][c]) | (static_cast<uint32_t>(t[16 * p + 2 * k + 1][c]) << 16);
+    uint4 *out = reinterpret_cast<uint4 *>(dst + (c0 + c) * ld_dst + r0 + 16 * p);
+    out[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    out[1] = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
 // out[m][n] = sum over splits of part[s][m][n]  (fixed order: deterministic)
@@ -1124,15 +1176,16 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
         // tensor stores where the outputs allow them: 16-column groups that
         // end inside the rows, 16-byte aligned bases (and bias, read as float4)
         const auto al16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
-        const bool store = (epilogue == TC_EPI_F32 || epilogue == TC_EPI_BIAS_F32 || epilogue == TC_EPI_BIAS_GELU) &&
-                           N % PT_GROUP == 0 && al16(c) && (epilogue == TC_EPI_F32 || al16(bias)) &&
-                           (epilogue != TC_EPI_BIAS_GELU || al16(c_bf16));
+        const bool bf16_out = epilogue == TC_EPI_BIAS_GELU || epilogue == TC_EPI_DGELU;
+        const bool store = N % PT_GROUP == 0 && al16(c) &&
+                           ((epilogue != TC_EPI_BIAS_F32 && epilogue != TC_EPI_BIAS_GELU) || al16(bias)) &&
+                           (!bf16_out || al16(c_bf16)) && (epilogue != TC_EPI_DGELU || al16(pre));
         if (store) {
             CUtensorMap mc, mcb;
             st = make_store_map(&mc, c, M, N, false);
             if (st) return st;
             mcb = mc;
-            if (epilogue == TC_EPI_BIAS_GELU) {
+            if (bf16_out) {
                 st = make_store_map(&mcb, c_bf16, M, N, true);
                 if (st) return st;
             }
@@ -1157,9 +1210,18 @@ int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t 
                            void *stream) {
     if (rows <= 0 || cols <= 0 || !src || !dst || ld_src < cols || ld_dst < rows)
         return fail(PQG_ERR_INVALID, "pqg_mlp_transpose_bf16: invalid arguments");
-    dim3 grid(static_cast<unsigned>((cols + 31) / 32), static_cast<unsigned>((rows + 31) / 32));
-    transpose_bf16<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const __nv_bfloat16 *>(src), rows, cols, ld_src, static_cast<__nv_bfloat16 *>(dst), ld_dst);
+    const bool tiles64 = rows % TT_EDGE == 0 && cols % TT_EDGE == 0 && rows / TT_EDGE <= 65535 && ld_src % 8 == 0 &&
+                         ld_dst % 8 == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0 &&
+                         (reinterpret_cast<uintptr_t>(dst) & 15u) == 0;
+    if (tiles64) {
+        dim3 grid(static_cast<unsigned>(cols / TT_EDGE), static_cast<unsigned>(rows / TT_EDGE));
+        transpose_bf16_64<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const uint16_t *>(src), ld_src, static_cast<uint16_t *>(dst), ld_dst);
+    } else {
+        dim3 grid(static_cast<unsigned>((cols + 31) / 32), static_cast<unsigned>((rows + 31) / 32));
+        transpose_bf16<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
+            static_cast<const __nv_bfloat16 *>(src), rows, cols, ld_src, static_cast<__nv_bfloat16 *>(dst), ld_dst);
+    }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_transpose_bf16");
 }

@@ -132,6 +132,23 @@ def test_transpose_and_rejects(L):
     assert L.pqg_mlp_gemm_tc(_v(X), 12, _v(X), 12, 4, 4, 12, 0, _f(C), None, None, None, None, 0, None) != 0
 
 
+@pytest.mark.parametrize("rows,cols,ld_src,ld_dst", [(65536, 256, 256, 65536), (192, 128, 136, 200),
+                                                     (128, 64, 64, 130), (64, 96, 96, 64)])
+def test_transpose_tiles(L, rows, cols, ld_src, ld_dst):
+    """Whole 64 x 64 tiles with 16-byte aligned rows take the tiled kernel
+    (16-byte loads, 32-byte stores); ld_dst = 130 and cols = 96 fall back to
+    the 32 x 32 kernel.  Either way the bits of src^T, and nothing written
+    outside it."""
+    import torch
+
+    X = torch.randn(rows, ld_src, device="cuda").to(torch.bfloat16)
+    Y = torch.full((cols, ld_dst), 7.0, device="cuda", dtype=torch.bfloat16)
+    assert L.pqg_mlp_transpose_bf16(_v(X), rows, cols, ld_src, _v(Y), ld_dst, None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(Y[:, :rows], X[:, :cols].t())
+    assert torch.all(Y[:, rows:] == 7.0)
+
+
 @pytest.mark.parametrize("M,N", [(65536, 256), (300, 8), (1, 40)])
 def test_bias_grad(L, M, N):
     import torch
