@@ -792,6 +792,32 @@ __global__ void tc_splitk_reduce(const float *__restrict__ part, int splits, int
     }
 }
 
+// The same sum for MN a multiple of 4 with 16-byte aligned buffers: a block
+// takes 16 output quads (float4) with 16 split lanes each (lane t sums splits
+// t, t + 16, ... in order), then the 16 lane sums in order -- a fixed order,
+// with every thread's loads independent of one another.
+constexpr int SK_LANES = 16;
+
+__global__ void __launch_bounds__(256) tc_splitk_reduce4(const float4 *__restrict__ part, int splits, int64_t MN4,
+                                                         float4 *__restrict__ out) {
+    __shared__ float4 sm[SK_LANES][16];
+    const int qd = threadIdx.x & 15, kl = threadIdx.x >> 4;
+    const int64_t e = static_cast<int64_t>(blockIdx.x) * 16 + qd;
+    float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (e < MN4)
+        for (int k = kl; k < splits; k += SK_LANES) {
+            const float4 v = __ldg(part + static_cast<int64_t>(k) * MN4 + e);
+            acc.x += v.x, acc.y += v.y, acc.z += v.z, acc.w += v.w;
+        }
+    sm[kl][qd] = acc;
+    __syncthreads();
+    if (kl == 0 && e < MN4) {
+        float4 t = sm[0][qd];
+        for (int k = 1; k < SK_LANES; ++k) t.x += sm[k][qd].x, t.y += sm[k][qd].y, t.z += sm[k][qd].z, t.w += sm[k][qd].w;
+        out[e] = t;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // The learned proposal's whole autoregressive step for output mode j, fused:
 // per tile of 128 chains, the 16 features (FP32, rounded to BF16 as the
@@ -1199,7 +1225,13 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc");
     if (epilogue == TC_EPI_SPLITK) {
-        tc_splitk_reduce<<<256, 256, 0, s>>>(splitk_scratch, nsplit, M * N, c);
+        const int64_t MN = M * N;
+        if (MN % 4 == 0 && (reinterpret_cast<uintptr_t>(splitk_scratch) & 15u) == 0 &&
+            (reinterpret_cast<uintptr_t>(c) & 15u) == 0 && (MN / 4 + 15) / 16 <= 0x7fffffff)
+            tc_splitk_reduce4<<<static_cast<unsigned>((MN / 4 + 15) / 16), 256, 0, s>>>(
+                reinterpret_cast<const float4 *>(splitk_scratch), nsplit, MN / 4, reinterpret_cast<float4 *>(c));
+        else
+            tc_splitk_reduce<<<256, 256, 0, s>>>(splitk_scratch, nsplit, MN, c);
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc (split-K reduction)");
     }

@@ -229,7 +229,7 @@ class MLP:
         if st:
             raise RuntimeError(_lib.last_error())
         grads_W, grads_b = [None] * 4, [None] * 4
-        splits = max(1, min(64, M // 1024))
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         d_out, d_out_b = dz, dzb
         for i in (3, 2, 1, 0):
             fi, fo = self.W[i].shape
@@ -237,6 +237,9 @@ class MLP:
             hT = self._transposed(acts[i])
             dT = self._transposed(d_out_b)
             gW = torch.empty(fi, fo, device=self.device, dtype=torch.float32)
+            # K splits of at least 512 rows, about one CTA per SM over the output tiles
+            tiles = -(-fi // 128) * -(-fo // 256)
+            splits = max(1, min(M // 512, sms // tiles))
             scratch = torch.empty(splits * fi * fo, device=self.device, dtype=torch.float32)
             self._gemm(hT, hT.shape[1], dT, dT.shape[1], fi, fo, M, 2, gW, scratch=scratch, splits=splits)
             gb = torch.empty(fo, device=self.device, dtype=torch.float32)

@@ -100,11 +100,15 @@ def test_gelu_epilogues(L, M, N, K):
     assert torch.all((db.float() - d).abs() <= 2.0 ** -8 * d.abs() + 1e-30)
 
 
-@pytest.mark.parametrize("splits", [1, 3, 16])
-def test_split_k(L, splits):
+@pytest.mark.parametrize("splits", [1, 3, 16, 40])
+@pytest.mark.parametrize("M,N", [(256, 136), (255, 135)])
+def test_split_k(L, splits, M, N):
+    """K not a multiple of the 64-wide chunk; M N a multiple of 4 takes the
+    float4 reduction (16 split lanes), 255 x 135 the one-thread-per-output
+    one."""
     import torch
 
-    M, N, K = 256, 136, 3000  # K not a multiple of the 64-wide chunk
+    K = 3000
     A, B, ref, scale = _operands(torch, M, N, K, splits)
     A2 = torch.zeros(M, 3008, device="cuda", dtype=torch.bfloat16)  # row stride 3008 (16-byte rows)
     A2[:, :K] = A
