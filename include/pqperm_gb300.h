@@ -271,7 +271,12 @@ int pqg_last_walk_kernel(int32_t *table, int32_t *n_cols);
  * per row m, softmax over classes lo[m]..hi[m] of logits (row stride ld),
  * loss = -log p(target), dlogits = (p - onehot) * scale (FP32, and BF16 when
  * dlogits_bf16 is not NULL).  pqg_mlp_adam: one Adam step on FP32 weights
- * (and their BF16 copy, nullable), bias-corrected with `step`. */
+ * (and their BF16 copy, nullable), bias-corrected with `step`.
+ * pqg_mlp_adam_multi: the same step on `count` (1..16) row-major tensors of
+ * rows[i] x cols[i] in one launch, with per tensor an optional BF16 copy
+ * (w_bf16 NULL or w_bf16[i] NULL: none) and an optional transposed BF16 copy
+ * (cols x rows); the arrays are host arrays of device pointers.  The FP32
+ * results equal pqg_mlp_adam's bit for bit. */
 int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                     int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
                     float *splitk_scratch, int32_t splits, void *stream);
@@ -284,6 +289,9 @@ int pqg_mlp_softmax_xent(const float *logits, int64_t M, int32_t ld, int32_t cla
                          void *dlogits_bf16, void *stream);
 int pqg_mlp_adam(float *w, void *w_bf16, const float *g, float *m1, float *m2, int64_t n, float lr, float b1,
                  float b2, float eps, int64_t step, void *stream);
+int pqg_mlp_adam_multi(int32_t count, float *const *w, void *const *w_bf16, void *const *w_bf16_t,
+                       const float *const *g, float *const *m1, float *const *m2, const int64_t *rows,
+                       const int64_t *cols, float lr, float b1, float b2, float eps, int64_t step, void *stream);
 
 /* Autoregressive proposal step for B chains at output mode j (d modes, n
  * photons): pqg_proposal_features writes the 16 BF16 features of mode j and

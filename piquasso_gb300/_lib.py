@@ -69,6 +69,8 @@ SIGNATURES = {
                               ctypes.c_void_p], ctypes.c_int),
     "pqg_mlp_adam": ([_f, ctypes.c_void_p, _f, _f, _f, _I64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                       ctypes.c_float, _I64, ctypes.c_void_p], ctypes.c_int),
+    "pqg_mlp_adam_multi": ([_I32] + [ctypes.POINTER(ctypes.c_void_p)] * 6 + [ctypes.POINTER(ctypes.c_int64)] * 2 +
+                           [ctypes.c_float] * 4 + [_I64, ctypes.c_void_p], ctypes.c_int),
     "pqg_proposal_features": ([_I32, _I32, _I32, _I32, _f, _i32, _f, ctypes.c_void_p, _i8, _i8, ctypes.c_void_p],
                               ctypes.c_int),
     "pqg_proposal_sample": ([_I32, _I32, _I32, _f, _i8, _i8, ctypes.c_uint64, ctypes.c_void_p, _i8, _i32, _f, _f,

@@ -87,20 +87,60 @@ __global__ void softmax_xent(const float *__restrict__ logits, int64_t M, int ld
 }
 
 // Adam on FP32 master weights, refreshing the BF16 copy.
+// One element of an Adam step (moments updated in place; the new weight
+// returned).  Both Adam kernels call it, so that they agree bit for bit.
+__device__ __forceinline__ float adam_elem(float *__restrict__ w, const float *__restrict__ g,
+                                           float *__restrict__ m1, float *__restrict__ m2, int64_t e, float lr,
+                                           float b1, float b2, float eps, float c1, float c2) {
+    const float gi = g[e];
+    const float a = b1 * m1[e] + (1.0f - b1) * gi;
+    const float b = b2 * m2[e] + (1.0f - b2) * gi * gi;
+    m1[e] = a;
+    m2[e] = b;
+    const float upd = lr * (a / c1) / (sqrtf(b / c2) + eps);
+    const float nw = w[e] - upd;
+    w[e] = nw;
+    return nw;
+}
+
 __global__ void adam_step(float *__restrict__ w, __nv_bfloat16 *__restrict__ wb, const float *__restrict__ g,
                           float *__restrict__ m1, float *__restrict__ m2, int64_t n, float lr, float b1, float b2,
                           float eps, float c1, float c2) {
     for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
          e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const float gi = g[e];
-        const float a = b1 * m1[e] + (1.0f - b1) * gi;
-        const float b = b2 * m2[e] + (1.0f - b2) * gi * gi;
-        m1[e] = a;
-        m2[e] = b;
-        const float upd = lr * (a / c1) / (sqrtf(b / c2) + eps);
-        const float nw = w[e] - upd;
-        w[e] = nw;
+        const float nw = adam_elem(w, g, m1, m2, e, lr, b1, b2, eps, c1, c2);
         if (wb) wb[e] = __float2bfloat16(nw);
+    }
+}
+
+// Every parameter tensor of a network in one launch (blockIdx.y: the tensor),
+// each with an optional BF16 copy and an optional transposed BF16 copy
+// (cols x rows): the step's separate Adam launches and weight transposes,
+// each a few microseconds of latency, in one.
+constexpr int ADAM_MAX = 16;
+
+struct AdamSet {
+    float *w[ADAM_MAX];
+    __nv_bfloat16 *wb[ADAM_MAX];
+    __nv_bfloat16 *wbt[ADAM_MAX];
+    const float *g[ADAM_MAX];
+    float *m1[ADAM_MAX];
+    float *m2[ADAM_MAX];
+    int64_t rows[ADAM_MAX], cols[ADAM_MAX];
+};
+
+__global__ void adam_multi(const __grid_constant__ AdamSet s, float lr, float b1, float b2, float eps, float c1,
+                           float c2) {
+    const int t = blockIdx.y;
+    const int64_t rows = s.rows[t], cols = s.cols[t], n = rows * cols;
+    for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < n;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float nw = adam_elem(s.w[t], s.g[t], s.m1[t], s.m2[t], e, lr, b1, b2, eps, c1, c2);
+        if (s.wb[t]) s.wb[t][e] = __float2bfloat16(nw);
+        if (s.wbt[t]) {
+            const int64_t r = e / cols, c = e - r * cols;
+            s.wbt[t][c * rows + r] = __float2bfloat16(nw);
+        }
     }
 }
 
@@ -150,6 +190,36 @@ int pqg_mlp_adam(float *w, void *w_bf16, const float *g, float *m1, float *m2, i
                                                                   n, lr, b1, b2, eps, c1, c2);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_adam");
+}
+
+int pqg_mlp_adam_multi(int32_t count, float *const *w, void *const *w_bf16, void *const *w_bf16_t,
+                       const float *const *g, float *const *m1, float *const *m2, const int64_t *rows,
+                       const int64_t *cols, float lr, float b1, float b2, float eps, int64_t step, void *stream) {
+    if (count < 1 || count > ADAM_MAX || !w || !g || !m1 || !m2 || !rows || !cols) {
+        pqg::set_last_error("pqg_mlp_adam_multi: invalid arguments (1 <= count <= 16, non-null arrays)");
+        return PQG_ERR_INVALID;
+    }
+    AdamSet set{};
+    for (int i = 0; i < count; ++i) {
+        if (!w[i] || !g[i] || !m1[i] || !m2[i] || rows[i] <= 0 || cols[i] <= 0) {
+            pqg::set_last_error("pqg_mlp_adam_multi: invalid tensor");
+            return PQG_ERR_INVALID;
+        }
+        set.w[i] = w[i];
+        set.wb[i] = w_bf16 ? static_cast<__nv_bfloat16 *>(w_bf16[i]) : nullptr;
+        set.wbt[i] = w_bf16_t ? static_cast<__nv_bfloat16 *>(w_bf16_t[i]) : nullptr;
+        set.g[i] = g[i];
+        set.m1[i] = m1[i];
+        set.m2[i] = m2[i];
+        set.rows[i] = rows[i];
+        set.cols[i] = cols[i];
+    }
+    const float c1 = 1.0f - powf(b1, static_cast<float>(step));
+    const float c2 = 1.0f - powf(b2, static_cast<float>(step));
+    adam_multi<<<dim3(64, static_cast<unsigned>(count)), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        set, lr, b1, b2, eps, c1, c2);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_adam_multi");
 }
 
 }  // extern "C"

@@ -260,17 +260,21 @@ class MLP:
         return loss, grads_W, grads_b
 
     def adam(self, grads_W, grads_b, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        """One Adam step on every weight and bias, with the BF16 copies (Wb)
+        and transposed copies (WbT) of the weights: one launch
+        (pqg_mlp_adam_multi)."""
         L = _lib.load()
         self.step += 1
-        fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float))  # noqa: E731
-        for i in range(4):
-            st = L.pqg_mlp_adam(fp(self.W[i]), _ptr(self.Wb[i]), fp(grads_W[i]), fp(self.mW[i]), fp(self.vW[i]),
-                                self.W[i].numel(), lr, b1, b2, eps, self.step, None)
-            st |= L.pqg_mlp_adam(fp(self.b[i]), None, fp(grads_b[i]), fp(self.mb[i]), fp(self.vb[i]),
-                                 self.b[i].numel(), lr, b1, b2, eps, self.step, None)
-            if st:
-                raise RuntimeError(_lib.last_error())
-            self._transpose(self.Wb[i], self.WbT[i])
+        ts = [(self.W[i], self.Wb[i], self.WbT[i], grads_W[i], self.mW[i], self.vW[i]) for i in range(4)]
+        ts += [(self.b[i], None, None, grads_b[i], self.mb[i], self.vb[i]) for i in range(4)]
+        P = ctypes.c_void_p * len(ts)
+        arr = [P(*[(t[k].data_ptr() if t[k] is not None else None) for t in ts]) for k in range(6)]
+        R = ctypes.c_int64 * len(ts)
+        rows = R(*[t[0].shape[0] if t[0].dim() == 2 else 1 for t in ts])
+        cols = R(*[t[0].shape[-1] for t in ts])
+        st = L.pqg_mlp_adam_multi(len(ts), *arr, rows, cols, lr, b1, b2, eps, self.step, None)
+        if st:
+            raise RuntimeError(_lib.last_error())
 
 
 DEFAULT_WEIGHTS = __import__("os").path.join(__import__("os").path.dirname(__file__), "data", "proposal_weights.npz")

@@ -201,3 +201,53 @@ def test_persistent_kernel_is_bitwise_the_tile_kernel(L, M, N, K, epi):
     assert torch.equal(outs[0][1], outs[1][1])
     if epi == 0:
         assert torch.all((outs[0][0] - ref).abs() <= 1e-5 * scale + 1e-6)
+
+
+def test_adam_multi_matches_per_tensor(L):
+    """pqg_mlp_adam_multi: every tensor's step in one launch, with the BF16
+    copy and the transposed BF16 copy, equal bit for bit to pqg_mlp_adam per
+    tensor (and the transposed copy to the copy's transpose); tensors without
+    copies (biases) and a NULL copy array."""
+    import torch
+
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    shapes = [(256, 256), (16, 256), (256, 8), (1, 256), (3, 5)]
+    base = []
+    for r, c in shapes:
+        base.append([torch.randn(r, c, device="cuda", generator=gen), torch.randn(r, c, device="cuda", generator=gen),
+                     0.1 * torch.randn(r, c, device="cuda", generator=gen),
+                     torch.rand(r, c, device="cuda", generator=gen)])
+    lr, b1, b2, eps, step = 1e-3, 0.9, 0.999, 1e-8, 3
+    one = [[t.clone() for t in x] for x in base]
+    wb1 = [torch.empty(r, c, device="cuda", dtype=torch.bfloat16) for r, c in shapes]
+    for i, (w, g, m1, m2) in enumerate(one):
+        assert L.pqg_mlp_adam(_f(w), _v(wb1[i]) if i < 3 else None, _f(g), _f(m1), _f(m2), w.numel(), lr, b1, b2,
+                              eps, step, None) == 0
+    multi = [[t.clone() for t in x] for x in base]
+    wb2 = [torch.empty(r, c, device="cuda", dtype=torch.bfloat16) for r, c in shapes]
+    wbt2 = [torch.empty(c, r, device="cuda", dtype=torch.bfloat16) for r, c in shapes]
+    n = len(shapes)
+    P = ctypes.c_void_p * n
+    R = ctypes.c_int64 * n
+    arrs = [P(*[x[k].data_ptr() for x in multi]) for k in range(4)]
+    wb_arr = P(*[wb2[i].data_ptr() if i < 3 else None for i in range(n)])
+    wbt_arr = P(*[wbt2[i].data_ptr() if i < 3 else None for i in range(n)])
+    rows, cols = R(*[r for r, _ in shapes]), R(*[c for _, c in shapes])
+    assert L.pqg_mlp_adam_multi(n, arrs[0], wb_arr, wbt_arr, arrs[1], arrs[2], arrs[3], rows, cols, lr, b1, b2, eps,
+                                step, None) == 0
+    torch.cuda.synchronize()
+    for i in range(n):
+        for k in (0, 2, 3):  # weights and both moments
+            assert torch.equal(one[i][k], multi[i][k]), (i, k)
+        if i < 3:
+            assert torch.equal(wb1[i], wb2[i])
+            assert torch.equal(wbt2[i], wb2[i].t())
+    # no copy arrays at all: the FP32 step alone
+    again = [[t.clone() for t in x] for x in base]
+    arrs = [P(*[x[k].data_ptr() for x in again]) for k in range(4)]
+    assert L.pqg_mlp_adam_multi(n, arrs[0], None, None, arrs[1], arrs[2], arrs[3], rows, cols, lr, b1, b2, eps,
+                                step, None) == 0
+    torch.cuda.synchronize()
+    assert all(torch.equal(one[i][0], again[i][0]) for i in range(n))
+    assert L.pqg_mlp_adam_multi(17, arrs[0], None, None, arrs[1], arrs[2], arrs[3], rows, cols, lr, b1, b2, eps,
+                                step, None) != 0
