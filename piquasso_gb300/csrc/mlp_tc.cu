@@ -44,6 +44,7 @@ namespace {
 constexpr int TC_BM = 128;      // UMMA M (cta_group::1)
 constexpr int TC_BK = 64;       // K chunk: one 128-byte swizzle row of BF16
 constexpr int TC_STAGES = 2;
+constexpr int TC_SPLITK_STAGES = 4;
 constexpr int TC_THREADS = 128;
 constexpr uint32_t TC_A_BYTES = TC_BM * TC_BK * 2;  // 16 KB per stage
 constexpr long long TC_WAIT_LIMIT = 1ll << 22;       // try_wait rounds before giving up
@@ -303,6 +304,10 @@ __device__ __forceinline__ void epilogue_group(const TcArgs &g, float *tile, con
     epilogue_group_w<32>(g, tile, v, ncol, rows_base, col0, cbase, vec_ok, lane);
 }
 
+// NS: TMA stages (2; 4 for split-K, whose CTAs each walk a long K range: the
+// issuing thread refills a stage only once its MMAs have completed, so the
+// stages in flight are the loads that overlap).
+template <int NS>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, TcArgs g) {
     extern __shared__ uint8_t tc_smem_raw[];
@@ -311,9 +316,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t base = (raw + 1023u) & ~1023u;
     const uint32_t b_bytes = static_cast<uint32_t>(g.BN) * TC_BK * 2;
     const uint32_t stage_bytes = TC_A_BYTES + b_bytes;
-    const uint32_t bar0 = base + TC_STAGES * stage_bytes;  // full[s] at bar0 + 8s, empty[s] at +16+8s, done at +32
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem_raw + (bar0 + 40 - raw));
-    const uint32_t full0 = bar0, empty0 = bar0 + 8 * TC_STAGES, done = bar0 + 16 * TC_STAGES;
+    const uint32_t bar0 = base + NS * stage_bytes;  // full[s] at bar0 + 8s, empty[s] at + 8 NS + 8s, then done
+    const uint32_t full0 = bar0, empty0 = bar0 + 8 * NS, done = bar0 + 16 * NS;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem_raw + (done + 8 - raw));
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t m0 = static_cast<int64_t>(blockIdx.y) * TC_BM, n0 = static_cast<int64_t>(blockIdx.x) * g.BN;
@@ -322,7 +327,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int nchunks = static_cast<int>((k_hi - k_lo + TC_BK - 1) / TC_BK);
 
     if (tid == 0) {
-        for (int s = 0; s < TC_STAGES; ++s) {
+        for (int s = 0; s < NS; ++s) {
             mbar_init(full0 + 8 * s, 1);
             mbar_init(empty0 + 8 * s, 1);
         }
@@ -343,18 +348,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (tid == 0) {
         const uint32_t idesc = idesc_bf16(g.BN);
         auto issue = [&](int c) {
-            const int s = c % TC_STAGES;
+            const int s = c % NS;
             const uint32_t sa = base + s * stage_bytes, sb = sa + TC_A_BYTES;
             const int32_t kx = static_cast<int32_t>(k_lo + static_cast<int64_t>(c) * TC_BK);  // multiple of 64
             mbar_expect_tx(full0 + 8 * s, stage_bytes);
             tma_load_2d(sa, &map_a, kx, static_cast<int32_t>(m0), full0 + 8 * s);
             tma_load_2d(sb, &map_b, kx, static_cast<int32_t>(n0), full0 + 8 * s);
         };
-        for (int c = 0; c < TC_STAGES && c < nchunks; ++c) issue(c);
+        for (int c = 0; c < NS && c < nchunks; ++c) issue(c);
         bool ok = true;
         for (int c = 0; c < nchunks && ok; ++c) {
-            const int s = c % TC_STAGES;
-            const uint32_t parity = static_cast<uint32_t>((c / TC_STAGES) & 1);
+            const int s = c % NS;
+            const uint32_t parity = static_cast<uint32_t>((c / NS) & 1);
             if (!mbar_wait(full0 + 8 * s, parity)) {
                 record_error(1);
                 ok = false;
@@ -367,14 +372,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             for (int kk = 0; kk < nk; ++kk)
                 umma_bf16(tmem, sdesc_sw128(sa + 32u * kk), sdesc_sw128(sb + 32u * kk), idesc, (c > 0 || kk > 0) ? 1 : 0);
             umma_commit(empty0 + 8 * s);
-            if (c + TC_STAGES < nchunks) {
+            if (c + NS < nchunks) {
                 // the stage is refilled once its MMAs have read it
                 if (!mbar_wait(empty0 + 8 * s, parity)) {
                     record_error(2);
                     ok = false;
                     break;
                 }
-                issue(c + TC_STAGES);
+                issue(c + NS);
             }
         }
         umma_commit(done);  // arrives when every MMA issued above has completed
@@ -1182,15 +1187,20 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
     if (st) return st;
     st = make_map(&mb, b, N, K, ldb, g.BN);
     if (st) return st;
-    // shared memory: two stages, the barriers, and the slack that aligns the
-    // stages to 1024 bytes; a CTA holding 256 TMEM columns asks for enough
-    // shared memory that at most two share an SM (512 columns)
-    size_t smem = 1024 + TC_STAGES * (static_cast<size_t>(TC_A_BYTES) + static_cast<size_t>(g.BN) * TC_BK * 2) + 64;
+    // shared memory: the stages, the barriers (16 bytes a stage, 8 for done,
+    // the TMEM slot: at most 76 bytes), and the slack that aligns the stages
+    // to 1024 bytes; a CTA holding 256 TMEM columns asks for enough shared
+    // memory that at most two share an SM (512 columns)
+    const int stages = epilogue == TC_EPI_SPLITK ? TC_SPLITK_STAGES : TC_STAGES;
+    size_t smem = 1024 + stages * (static_cast<size_t>(TC_A_BYTES) + static_cast<size_t>(g.BN) * TC_BK * 2) + 128;
     if (g.tmem_cols > 128 && smem < 80 * 1024) smem = 80 * 1024;
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(attr_once, [] {
-        attr_err = cudaFuncSetAttribute(gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_err = cudaFuncSetAttribute(gemm_tc<TC_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(gemm_tc<TC_SPLITK_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            200 * 1024);
     });
     if (attr_err != cudaSuccess) return fail_cuda(attr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1221,7 +1231,10 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
     }
     dim3 grid(static_cast<unsigned>((N + g.BN - 1) / g.BN), static_cast<unsigned>((M + TC_BM - 1) / TC_BM),
               static_cast<unsigned>(nsplit));
-    gemm_tc<<<grid, TC_THREADS, smem, s>>>(ma, mb, g);
+    if (stages == TC_SPLITK_STAGES)
+        gemm_tc<TC_SPLITK_STAGES><<<grid, TC_THREADS, smem, s>>>(ma, mb, g);
+    else
+        gemm_tc<TC_STAGES><<<grid, TC_THREADS, smem, s>>>(ma, mb, g);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc");
     if (epilogue == TC_EPI_SPLITK) {
