@@ -280,6 +280,14 @@ int pqg_last_walk_kernel(int32_t *table, int32_t *n_cols);
 int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                     int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
                     float *splitk_scratch, int32_t splits, void *stream);
+/* pqg_mlp_gemm_tc_t: pqg_mlp_gemm_tc with a BF16 epilogue (1 or 4) that also
+ * writes the BF16 output transposed, c_bf16_t = c_bf16^T (N x M, row stride
+ * ld_t >= M, a multiple of 8): the K-major operand of a weight gradient over
+ * the rows.  The persistent kernel writes it from its epilogue; other shapes
+ * run the transpose kernel after the GEMM.  Same bits either way. */
+int pqg_mlp_gemm_tc_t(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                      int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, void *c_bf16_t,
+                      int64_t ld_t, void *stream);
 int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
                            void *stream);
 int pqg_mlp_tc_status(int32_t *code);

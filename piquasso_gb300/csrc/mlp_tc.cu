@@ -465,6 +465,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // warps suffice for it, and their 48 KB of tiles leave room for three A
 // stages beside B (at 65536 x 256 x 256: 35.5 us with the 24-warp form, 33.4
 // with this one on two stages, 31.4 on three; 12 or 20 warps no faster).
+//
+// kForm 2 adds the transposed BF16 output (N x M, the operand layout a
+// weight gradient over the rows needs): each lane also writes its row's 16
+// BF16 values down a column of a 16 x 32 staging tile (two-byte stores, the
+// warp's lanes on consecutive elements) and a third tensor store writes the
+// tile at (rows, columns) swapped.  Its 64 KB of tiles leave room for two A
+// stages.
 constexpr int PT_STAGES = 2;
 constexpr int PT_STORE_STAGES = 3;
 constexpr int PT_EPI_WARPS = 24;
@@ -472,29 +479,37 @@ constexpr int PT_STORE_EPI_WARPS = 16;
 constexpr int PT_GROUP = 16;                       // accumulator columns an epilogue step takes
 constexpr int PT_TILE_FLOATS = 32 * (PT_GROUP + 1);  // a warp's staging tile, 32 x 17 floats
 constexpr int PT_STORE_TILE_BYTES = 32 * PT_GROUP * 4 + 32 * PT_GROUP * 2;  // FP32 + BF16 tiles, 3 KB
+constexpr int PT_TRANS_TILE_BYTES = PT_STORE_TILE_BYTES + 1024;             // + the 16 x 32 BF16 transposed tile
 
-template <bool kStore>
+// kForm: 0 register stores, 1 tensor stores, 2 tensor stores and the transposed BF16 output
+template <int kForm>
 __host__ __device__ constexpr int pt_epi_warps() {
-    return kStore ? PT_STORE_EPI_WARPS : PT_EPI_WARPS;
+    return kForm ? PT_STORE_EPI_WARPS : PT_EPI_WARPS;
 }
 
-template <bool kStore>
+template <int kForm>
 __host__ __device__ constexpr int pt_stages() {
-    return kStore ? PT_STORE_STAGES : PT_STAGES;
+    return kForm == 1 ? PT_STORE_STAGES : PT_STAGES;
 }
 
-template <bool kStore>
+template <int kForm>
+__host__ __device__ constexpr uint32_t pt_warp_tile_bytes() {
+    return kForm == 2 ? PT_TRANS_TILE_BYTES : PT_STORE_TILE_BYTES;
+}
+
+template <int kForm>
 __host__ __device__ constexpr size_t pt_tile_bytes() {
-    return kStore ? static_cast<size_t>(PT_STORE_EPI_WARPS) * PT_STORE_TILE_BYTES
-                  : static_cast<size_t>(PT_EPI_WARPS) * PT_TILE_FLOATS * 4;
+    return kForm ? static_cast<size_t>(PT_STORE_EPI_WARPS) * pt_warp_tile_bytes<kForm>()
+                 : static_cast<size_t>(PT_EPI_WARPS) * PT_TILE_FLOATS * 4;
 }
 
-template <bool kStore>
-__global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
+template <int kForm>
+__global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kForm>()), 1)
     gemm_tc_persistent(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                        const __grid_constant__ CUtensorMap map_c, const __grid_constant__ CUtensorMap map_cb,
-                       TcArgs g) {
-    constexpr int EW = pt_epi_warps<kStore>(), NS = pt_stages<kStore>();
+                       const __grid_constant__ CUtensorMap map_ct, TcArgs g) {
+    constexpr bool kStore = kForm >= 1, kTrans = kForm == 2;
+    constexpr int EW = pt_epi_warps<kForm>(), NS = pt_stages<kForm>();
     extern __shared__ uint8_t tc_smem_raw[];
     const uint32_t raw = smem_u32(tc_smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
@@ -503,7 +518,7 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
     const uint32_t sB = base;                                       // nkc chunks of BN x 64
     const uint32_t sA = sB + static_cast<uint32_t>(nkc) * b_chunk;  // NS x 16 KB
     const uint32_t sT = sA + NS * TC_A_BYTES;  // the epilogue warps' staging tiles (1024-byte aligned)
-    const uint32_t bars = sT + static_cast<uint32_t>(pt_tile_bytes<kStore>());
+    const uint32_t bars = sT + static_cast<uint32_t>(pt_tile_bytes<kForm>());
     // barriers: bfull | full[S] | empty[S] | tfull[2] | tempty[2] | done
     const uint32_t bfull = bars, full0 = bars + 8, empty0 = full0 + 8 * NS, tfull0 = empty0 + 8 * NS,
                    tempty0 = tfull0 + 16, done = tempty0 + 16;
@@ -631,7 +646,8 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
         // tile; column groups h, h + 2, ... of 32 columns
         const int q = warp & 3, h = (warp - 2) / 4;
         float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * PT_TILE_FLOATS;
-        const uint32_t st_c = sT + static_cast<uint32_t>(warp - 2) * PT_STORE_TILE_BYTES, st_b = st_c + 2048;
+        const uint32_t st_c = sT + static_cast<uint32_t>(warp - 2) * pt_warp_tile_bytes<kForm>(), st_b = st_c + 2048,
+                       st_t = st_c + 3072;
         const bool vec_ok = (g.N % 4) == 0;
         uint32_t tl = 0;
         for (int64_t u = blockIdx.x; u < n_units; u += grid, ++tl) {
@@ -709,12 +725,25 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kStore>()), 1)
                                          : "memory");
                         }
                     }
+                    // the transposed tile: column k of the group is its row k (32
+                    // BF16, 64 bytes), this lane's value at element `lane`
+                    if (kTrans) {
+#pragma unroll
+                        for (int k = 0; k < PT_GROUP / 2; ++k) {
+                            const uint32_t at = st_t + 2u * lane + 128u * k;
+                            asm volatile("st.shared.u16 [%0], %1;" ::"r"(at), "h"(static_cast<uint16_t>(pb[k] & 0xffffu))
+                                         : "memory");
+                            asm volatile("st.shared.u16 [%0], %1;" ::"r"(at + 64u), "h"(static_cast<uint16_t>(pb[k] >> 16))
+                                         : "memory");
+                        }
+                    }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) {
                         const int32_t y = static_cast<int32_t>(tile * TC_BM + q * 32);
                         tma_store_2d(&map_c, st_c, col0, y);
                         if (act || dgelu) tma_store_2d(&map_cb, st_b, col0, y);
+                        if (kTrans) tma_store_2d(&map_ct, st_t, y, col0);
                         asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                     }
                 } else {
@@ -1123,31 +1152,71 @@ int make_store_map(CUtensorMap *map, void *p, int64_t rows, int64_t cols, bool b
     return PQG_OK;
 }
 
-template <bool kStore>
+// Tensor map of the transposed BF16 output [cols x rows] (row stride ld
+// elements, a multiple of 8) for the kForm 2 stores: boxes of 32 rows of the
+// GEMM (the inner coordinate) x 16 columns, unswizzled 64-byte box rows.
+int make_trans_map(CUtensorMap *map, void *p, int64_t rows, int64_t cols, int64_t ld) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return fail(PQG_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows), static_cast<cuuint64_t>(cols)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+    const cuuint32_t box[2] = {32, static_cast<cuuint32_t>(PT_GROUP)};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, p, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "cuTensorMapEncodeTiled failed (%d) for a %lld x %lld transposed output",
+                 static_cast<int>(r), static_cast<long long>(cols), static_cast<long long>(rows));
+        return fail(PQG_ERR_INVALID, buf);
+    }
+    return PQG_OK;
+}
+
+template <int kForm>
 int launch_persistent(const CUtensorMap &ma, const CUtensorMap &mb, const CUtensorMap &mc, const CUtensorMap &mcb,
-                      const TcArgs &g, int sms, cudaStream_t s) {
+                      const CUtensorMap &mct, const TcArgs &g, int sms, cudaStream_t s) {
     const size_t psmem = 1024 + static_cast<size_t>((g.K + TC_BK - 1) / TC_BK) * g.BN * TC_BK * 2 +
-                         pt_stages<kStore>() * static_cast<size_t>(TC_A_BYTES) + pt_tile_bytes<kStore>() + 128;
+                         pt_stages<kForm>() * static_cast<size_t>(TC_A_BYTES) + pt_tile_bytes<kForm>() + 128;
     static std::once_flag pattr_once;
     static cudaError_t pattr_err = cudaSuccess;
     std::call_once(pattr_once, [] {
-        pattr_err = cudaFuncSetAttribute(gemm_tc_persistent<kStore>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        pattr_err = cudaFuncSetAttribute(gemm_tc_persistent<kForm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          227 * 1024);
     });
     if (pattr_err != cudaSuccess) return fail_cuda(pattr_err, "pqg_mlp_gemm_tc (shared memory attribute)");
-    gemm_tc_persistent<kStore>
-        <<<static_cast<unsigned>(sms), 32 * (2 + pt_epi_warps<kStore>()), psmem, s>>>(ma, mb, mc, mcb, g);
+    gemm_tc_persistent<kForm>
+        <<<static_cast<unsigned>(sms), 32 * (2 + pt_epi_warps<kForm>()), psmem, s>>>(ma, mb, mc, mcb, mct, g);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_gemm_tc");
 }
 
-}  // namespace
+// dst (cols x ld_dst) = src (rows x cols, row stride ld_src)^T, BF16: the
+// 64 x 64 kernel for whole aligned tiles, else the 32 x 32 one.
+int transpose_launch(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
+                     cudaStream_t s) {
+    const bool tiles64 = rows % TT_EDGE == 0 && cols % TT_EDGE == 0 && rows / TT_EDGE <= 65535 && ld_src % 8 == 0 &&
+                         ld_dst % 8 == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0 &&
+                         (reinterpret_cast<uintptr_t>(dst) & 15u) == 0;
+    if (tiles64) {
+        dim3 grid(static_cast<unsigned>(cols / TT_EDGE), static_cast<unsigned>(rows / TT_EDGE));
+        transpose_bf16_64<<<grid, 256, 0, s>>>(static_cast<const uint16_t *>(src), ld_src,
+                                                static_cast<uint16_t *>(dst), ld_dst);
+    } else {
+        dim3 grid(static_cast<unsigned>((cols + 31) / 32), static_cast<unsigned>((rows + 31) / 32));
+        transpose_bf16<<<grid, dim3(32, 8), 0, s>>>(static_cast<const __nv_bfloat16 *>(src), rows, cols, ld_src,
+                                                     static_cast<__nv_bfloat16 *>(dst), ld_dst);
+    }
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_transpose_bf16");
+}
 
-extern "C" {
-
-int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
-                    int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
-                    float *splitk_scratch, int32_t splits, void *stream) {
+// The GEMM behind both entry points; c_bf16_t (nullable): the transposed
+// BF16 output, N x M with row stride ld_t.
+int gemm_tc_impl(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                 int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, float *splitk_scratch,
+                 int32_t splits, void *c_bf16_t, int64_t ld_t, void *stream) {
     if (M <= 0 || N <= 0 || K <= 0 || !a || !b || !c || lda < K || ldb < K || epilogue < 0 || epilogue > 4)
         return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: invalid arguments");
     if ((lda % 8) || (ldb % 8) || (reinterpret_cast<uintptr_t>(a) % 16) || (reinterpret_cast<uintptr_t>(b) % 16))
@@ -1217,7 +1286,7 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
                            ((epilogue != TC_EPI_BIAS_F32 && epilogue != TC_EPI_BIAS_GELU) || al16(bias)) &&
                            (!bf16_out || al16(c_bf16)) && (epilogue != TC_EPI_DGELU || al16(pre));
         if (store) {
-            CUtensorMap mc, mcb;
+            CUtensorMap mc, mcb, mct;
             st = make_store_map(&mc, c, M, N, false);
             if (st) return st;
             mcb = mc;
@@ -1225,9 +1294,20 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
                 st = make_store_map(&mcb, c_bf16, M, N, true);
                 if (st) return st;
             }
-            return launch_persistent<true>(ma, mb, mc, mcb, g, sms, s);
+            // a tensor store writes a partial 16-byte chunk at the end of a row
+            // whole (measured: the seven padding columns of M = 50001 were
+            // written), so the transposed rows, M long, take it at M % 8 == 0
+            if (c_bf16_t && al16(c_bf16_t) && M % 8 == 0) {
+                st = make_trans_map(&mct, c_bf16_t, M, N, ld_t);
+                if (st) return st;
+                return launch_persistent<2>(ma, mb, mc, mcb, mct, g, sms, s);
+            }
+            st = launch_persistent<1>(ma, mb, mc, mcb, mc, g, sms, s);
+        } else {
+            st = launch_persistent<0>(ma, mb, ma, ma, ma, g, sms, s);
         }
-        return launch_persistent<false>(ma, mb, ma, ma, g, sms, s);
+        if (st || !c_bf16_t) return st;
+        return transpose_launch(c_bf16, M, N, N, c_bf16_t, ld_t, s);
     }
     dim3 grid(static_cast<unsigned>((N + g.BN - 1) / g.BN), static_cast<unsigned>((M + TC_BM - 1) / TC_BM),
               static_cast<unsigned>(nsplit));
@@ -1248,27 +1328,36 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc (split-K reduction)");
     }
+    if (c_bf16_t) return transpose_launch(c_bf16, M, N, N, c_bf16_t, ld_t, s);
     return PQG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                    int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
+                    float *splitk_scratch, int32_t splits, void *stream) {
+    return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, splitk_scratch, splits, nullptr, 0,
+                        stream);
+}
+
+int pqg_mlp_gemm_tc_t(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                      int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, void *c_bf16_t,
+                      int64_t ld_t, void *stream) {
+    if ((epilogue != TC_EPI_BIAS_GELU && epilogue != TC_EPI_DGELU) || !c_bf16_t || ld_t < M || ld_t % 8)
+        return fail(PQG_ERR_INVALID,
+                    "pqg_mlp_gemm_tc_t: needs a BF16 epilogue (1 or 4) and a transposed output with ld_t >= M, "
+                    "ld_t % 8 == 0");
+    return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, nullptr, 0, c_bf16_t, ld_t, stream);
 }
 
 int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
                            void *stream) {
     if (rows <= 0 || cols <= 0 || !src || !dst || ld_src < cols || ld_dst < rows)
         return fail(PQG_ERR_INVALID, "pqg_mlp_transpose_bf16: invalid arguments");
-    const bool tiles64 = rows % TT_EDGE == 0 && cols % TT_EDGE == 0 && rows / TT_EDGE <= 65535 && ld_src % 8 == 0 &&
-                         ld_dst % 8 == 0 && (reinterpret_cast<uintptr_t>(src) & 15u) == 0 &&
-                         (reinterpret_cast<uintptr_t>(dst) & 15u) == 0;
-    if (tiles64) {
-        dim3 grid(static_cast<unsigned>(cols / TT_EDGE), static_cast<unsigned>(rows / TT_EDGE));
-        transpose_bf16_64<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
-            static_cast<const uint16_t *>(src), ld_src, static_cast<uint16_t *>(dst), ld_dst);
-    } else {
-        dim3 grid(static_cast<unsigned>((cols + 31) / 32), static_cast<unsigned>((rows + 31) / 32));
-        transpose_bf16<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(
-            static_cast<const __nv_bfloat16 *>(src), rows, cols, ld_src, static_cast<__nv_bfloat16 *>(dst), ld_dst);
-    }
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_transpose_bf16");
+    return transpose_launch(src, rows, cols, ld_src, dst, ld_dst, static_cast<cudaStream_t>(stream));
 }
 
 int pqg_proposal_step_tc(int32_t j, int32_t B, int32_t d, int32_t n, const float *mode_stats, const void *w1t,

@@ -173,6 +173,19 @@ class MLP:
         if st:
             raise RuntimeError("pqg_mlp_gemm_tc failed: " + _lib.last_error())
 
+    def _gemm_t(self, A, lda, B, ldb, M, N, K, epi, C, Cb, bias=None, pre=None, stream=None):
+        """_gemm with a BF16 epilogue that also returns Cb^T (N x Mp, rows
+        padded to a multiple of 8 elements), written by the GEMM itself."""
+        L = _lib.load()
+        Mp = (M + 7) // 8 * 8
+        CbT = self.torch.empty(N, Mp, device=self.device, dtype=self.torch.bfloat16)
+        fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float)) if t is not None else None  # noqa
+        st = L.pqg_mlp_gemm_tc_t(_ptr(A), lda, _ptr(B), ldb, M, N, K, epi, fp(C), _ptr(Cb), fp(bias), fp(pre),
+                                 _ptr(CbT), Mp, stream)
+        if st:
+            raise RuntimeError("pqg_mlp_gemm_tc_t failed: " + _lib.last_error())
+        return CbT
+
     def _transpose(self, src, dst):
         """dst (cols x ld) = src (rows x cols)^T, BF16."""
         rows, cols = src.shape
@@ -195,20 +208,25 @@ class MLP:
         torch = self.torch
         M = Xb.shape[0]
         acts = [Xb]
+        actsT = [None]
         pres = []
         h = Xb
         for i in range(3):
             pre = torch.empty(M, HIDDEN, device=self.device, dtype=torch.float32)
             act = torch.empty(M, HIDDEN, device=self.device, dtype=torch.bfloat16)
             fi = h.shape[1]
-            self._gemm(h, fi, self.WbT[i], fi, M, HIDDEN, fi, 1, pre, Cb=act, bias=self.b[i], stream=stream)
+            if keep:  # the backward pass's weight gradient wants the activation transposed too
+                actsT.append(self._gemm_t(h, fi, self.WbT[i], fi, M, HIDDEN, fi, 1, pre, act, bias=self.b[i],
+                                          stream=stream))
+            else:
+                self._gemm(h, fi, self.WbT[i], fi, M, HIDDEN, fi, 1, pre, Cb=act, bias=self.b[i], stream=stream)
             pres.append(pre)
             acts.append(act)
             h = act
         logits = torch.empty(M, LD, device=self.device, dtype=torch.float32)
         self._gemm(h, HIDDEN, self.WbT[3], HIDDEN, M, LD, HIDDEN, 3, logits, bias=self.b[3], stream=stream)
         if keep:
-            return logits, acts, pres
+            return logits, acts, actsT, pres
         return logits
 
     def loss_and_grads(self, Xb, lo, hi, target):
@@ -216,7 +234,7 @@ class MLP:
         torch = self.torch
         L = _lib.load()
         M = Xb.shape[0]
-        logits, acts, pres = self.forward(Xb, keep=True)
+        logits, acts, actsT, pres = self.forward(Xb, keep=True)
         loss = torch.empty(M, device=self.device, dtype=torch.float32)
         dz = torch.empty(M, LD, device=self.device, dtype=torch.float32)
         dzb = torch.empty(M, LD, device=self.device, dtype=torch.bfloat16)
@@ -230,12 +248,13 @@ class MLP:
             raise RuntimeError(_lib.last_error())
         grads_W, grads_b = [None] * 4, [None] * 4
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-        d_out, d_out_b = dz, dzb
+        d_out, d_out_b, d_out_t = dz, dzb, None
         for i in (3, 2, 1, 0):
             fi, fo = self.W[i].shape
-            # dW = h_in^T d_out: K = M (split over the batch), both operands transposed to K-major
-            hT = self._transposed(acts[i])
-            dT = self._transposed(d_out_b)
+            # dW = h_in^T d_out: K = M (split over the batch), both operands K-major: the
+            # transposed copies the GEMMs wrote (the features and the head's gradient: a transpose)
+            hT = actsT[i] if actsT[i] is not None else self._transposed(acts[i])
+            dT = d_out_t if d_out_t is not None else self._transposed(d_out_b)
             gW = torch.empty(fi, fo, device=self.device, dtype=torch.float32)
             # K splits of at least 512 rows, about one CTA per SM over the output tiles
             tiles = -(-fi // 128) * -(-fo // 256)
@@ -255,8 +274,8 @@ class MLP:
             # d h_in = d_out W^T, through GELU'(pre) in the epilogue (FP32 and BF16)
             dh = torch.empty(M, fi, device=self.device, dtype=torch.float32)
             dhb = torch.empty(M, fi, device=self.device, dtype=torch.bfloat16)
-            self._gemm(d_out_b, fo, self.Wb[i], fo, M, fi, fo, 4, dh, Cb=dhb, pre=pres[i - 1])
-            d_out, d_out_b = dh, dhb
+            dht = self._gemm_t(d_out_b, fo, self.Wb[i], fo, M, fi, fo, 4, dh, dhb, pre=pres[i - 1])
+            d_out, d_out_b, d_out_t = dh, dhb, dht
         return loss, grads_W, grads_b
 
     def adam(self, grads_W, grads_b, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):

@@ -251,3 +251,47 @@ def test_adam_multi_matches_per_tensor(L):
     assert all(torch.equal(one[i][0], again[i][0]) for i in range(n))
     assert L.pqg_mlp_adam_multi(17, arrs[0], None, None, arrs[1], arrs[2], arrs[3], rows, cols, lr, b1, b2, eps,
                                 step, None) != 0
+
+
+@pytest.mark.parametrize("M,N,K", [(65536, 256, 256), (50008, 48, 200), (50001, 48, 200), (1000, 256, 256),
+                                   (40000, 40, 64)])
+@pytest.mark.parametrize("epi", [1, 4])
+def test_gemm_with_transposed_output(L, M, N, K, epi):
+    """pqg_mlp_gemm_tc_t: the same C and BF16 output as pqg_mlp_gemm_tc, bit
+    for bit, plus that BF16 output transposed (N x ld_t, ld_t >= M).  The
+    persistent kernel writes it from its epilogue at M a multiple of 8 (65536
+    rows, and 50008 with a last tile of 88 rows); 50001 rows, 1000 rows (the
+    one-tile kernel) and N = 40 (the register-store form) run the transpose
+    after the GEMM.  Columns of the transposed output past M stay untouched."""
+    import torch
+
+    A, B, ref, scale = _operands(torch, M, N, K, M + N + epi)
+    bias = torch.randn(N, device="cuda")
+    pre = torch.randn(M, N, device="cuda")
+    ld_t = (M + 7) // 8 * 8 + 8
+    outs = []
+    for with_t in (False, True):
+        # 40 sentinel rows after each output: the row dimension is clipped exactly
+        C_all = torch.full((M + 40, N), float("nan"), device="cuda")
+        Cb_all = torch.full((M + 40, N), 5.0, device="cuda", dtype=torch.bfloat16)
+        C, Cb = C_all[:M], Cb_all[:M]
+        CbT = torch.full((N, ld_t), 3.0, device="cuda", dtype=torch.bfloat16)
+        args = (_v(A), K, _v(B), K, M, N, K, epi, _f(C), _v(Cb), _f(bias) if epi == 1 else None,
+                _f(pre) if epi == 4 else None)
+        if with_t:
+            assert L.pqg_mlp_gemm_tc_t(*args, _v(CbT), ld_t, None) == 0
+        else:
+            assert L.pqg_mlp_gemm_tc(*args, None, 0, None) == 0
+        torch.cuda.synchronize()
+        assert _status(L) == 0
+        assert torch.all(torch.isnan(C_all[M:])) and torch.all(Cb_all[M:] == 5.0)
+        outs.append((C, Cb, CbT))
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[1][2][:, :M], outs[1][1].t())
+    assert torch.all(outs[1][2][:, M:] == 3.0)
+    # only the BF16 epilogues, and a transposed row stride of at least M in multiples of 8
+    C = torch.empty(M, N, device="cuda")
+    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, 0, _f(C), None, None, None, _v(CbT), ld_t, None) != 0
+    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, epi, _f(C), _v(Cb), _f(bias), _f(pre), _v(CbT), ld_t - 4,
+                               None) != 0
