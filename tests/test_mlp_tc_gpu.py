@@ -123,6 +123,26 @@ def test_split_k(L, splits, M, N):
     assert torch.all((C - ref).abs() <= 1e-5 * scale + 1e-6)
 
 
+@pytest.mark.parametrize("K", [12, 20, 3])
+def test_k_not_a_multiple_of_8_ignores_the_row_padding(L, K):
+    """K below the row stride (16-byte rows) with NaN in the padding: the TMA
+    loads must fill the chunk past K with zeros, not read the padding."""
+    import torch
+
+    M, N = 300, 64
+    A, B, ref, scale = _operands(torch, M, N, K, K)
+    ld = (K + 7) // 8 * 8 + 8
+    A2 = torch.full((M, ld), float("nan"), device="cuda").to(torch.bfloat16)
+    B2 = torch.full((N, ld), float("nan"), device="cuda").to(torch.bfloat16)
+    A2[:, :K] = A
+    B2[:, :K] = B
+    C = torch.empty(M, N, device="cuda")
+    assert L.pqg_mlp_gemm_tc(_v(A2), ld, _v(B2), ld, M, N, K, 0, _f(C), None, None, None, None, 0, None) == 0
+    torch.cuda.synchronize()
+    assert _status(L) == 0
+    assert torch.all((C - ref).abs() <= 1e-5 * scale + 1e-6)
+
+
 def test_transpose_and_rejects(L):
     import torch
 
