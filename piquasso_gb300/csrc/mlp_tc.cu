@@ -426,9 +426,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // (one column tile), K <= 256, and many 128-row tiles.  One CTA per SM walks
 // the row tiles blockIdx.x, blockIdx.x + gridDim.x, ...  The whole B operand
 // (BN x K, at most 128 KB) is loaded once per CTA and stays in shared memory;
-// A streams through PT_STAGES 16 KB stages (two: with the epilogue on 24
-// warps a second stage measured 10 % faster than one; a third does not fit
-// beside B and the staging tiles).  Warp roles:
+// A streams through 16 KB stages (kForm 0, register stores: two -- with the
+// epilogue on 24 warps a second stage measured 10 % faster than one, and a
+// third does not fit beside B and the staging tiles; kForm 1: three; kForm 2:
+// two).  Warp roles:
 //   warp 0  TMA producer: B once, then A chunk by chunk, each stage refilled
 //           once the MMAs that read it have completed (empty barrier);
 //   warp 1  MMA issuer and TMEM owner: two accumulators of tmem_cols columns
@@ -436,7 +437,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //           tile i reads one accumulator while the MMAs of tile i + 1 fill the
 //           other; tcgen05.commit signals a stage's release and an
 //           accumulator's completion;
-//   warps 2-25  epilogue (2-17 in the kStore form below, four a quarter,
+//   warps 2-25  epilogue (2-17 in kForms 1 and 2 below, four a quarter,
 //           every fourth group): warp w reads TMEM lanes 32 (w mod 4) .. + 31 (the
 //           lane quarter its position allows), i.e. those rows of the tile;
 //           the six warps of a quarter take every sixth 16-column group (at
@@ -452,11 +453,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // its TMEM the producer waits for the copies it issued and the issuer for its
 // MMAs.
 //
-// kStore (every epilogue but split-K, at N a multiple of 16 with 16-byte
-// aligned outputs, bias and pre): each lane applies the epilogue to its own
-// row of the 16-column group in registers (DGELU reads the row's 16 values of
-// pre, 64 contiguous bytes) and writes it to the warp's staging tiles -- FP32 32 x 16 in the
-// 64-byte swizzle layout, BF16 32 x 16 in the 32-byte one, so that the row
+// kForm 1, tensor stores (every epilogue but split-K, at N a multiple of 16
+// with 16-byte aligned outputs, bias and pre): each lane applies the epilogue
+// to its own row of the 16-column group in registers (DGELU reads the row's 16
+// values of pre, 64 contiguous bytes) and writes it to the warp's staging
+// tiles -- FP32 32 x 16 in the 64-byte swizzle layout, BF16 32 x 16 in the 32-byte one, so that the row
 // writes are free of bank conflicts -- and one lane hands the tiles to the TMA
 // unit as tensor stores (rows past M are not written).  The next group's
 // TMEM load and arithmetic run while the store reads the tiles; the tiles are
@@ -467,7 +468,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // with this one on two stages, 31.4 on three; 12 or 20 warps no faster).
 //
 // kForm 2 adds the transposed BF16 output (N x M, the operand layout a
-// weight gradient over the rows needs): each lane also writes its row's 16
+// weight gradient over the rows needs; at M a multiple of 8, because a tensor
+// store writes the partial 16-byte chunk at the end of a row whole): each lane also writes its row's 16
 // BF16 values down a column of a 16 x 32 staging tile (two-byte stores, the
 // warp's lanes on consecutive elements) and a third tensor store writes the
 // tile at (rows, columns) swapped.  Its 64 KB of tiles leave room for two A
@@ -643,7 +645,7 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kForm>()), 1)
         }
     } else {
         // epilogue warps: TMEM lane quarter q, rows 32 q .. 32 q + 31 of each
-        // tile; column groups h, h + 2, ... of 32 columns
+        // tile; 16-column groups h, h + EW / 4, ...
         const int q = warp & 3, h = (warp - 2) / 4;
         float *tile_f = reinterpret_cast<float *>(tc_smem_raw + (sT - raw)) + (warp - 2) * PT_TILE_FLOATS;
         const uint32_t st_c = sT + static_cast<uint32_t>(warp - 2) * pt_warp_tile_bytes<kForm>(), st_b = st_c + 2048,
