@@ -283,11 +283,14 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
 /* pqg_mlp_gemm_tc_t: pqg_mlp_gemm_tc with a BF16 epilogue (1 or 4) that also
  * writes the BF16 output transposed, c_bf16_t = c_bf16^T (N x M, row stride
  * ld_t >= M, a multiple of 8): the K-major operand of a weight gradient over
- * the rows.  The persistent kernel writes it from its epilogue; other shapes
- * run the transpose kernel after the GEMM.  Same bits either way. */
+ * the rows; and, when col_sums is not NULL, the column sums of the FP32 output
+ * c (the next layer's bias gradient) through col_scratch (4 ceil(M/128) N
+ * floats), deterministic.  The persistent kernel writes both from its
+ * epilogue; other shapes run the transpose and the bias-gradient kernels
+ * after the GEMM.  The same bits of c, c_bf16 and c_bf16_t either way. */
 int pqg_mlp_gemm_tc_t(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                       int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, void *c_bf16_t,
-                      int64_t ld_t, void *stream);
+                      int64_t ld_t, float *col_sums, float *col_scratch, void *stream);
 int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
                            void *stream);
 int pqg_mlp_tc_status(int32_t *code);

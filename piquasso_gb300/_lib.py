@@ -62,7 +62,7 @@ SIGNATURES = {
     "pqg_mlp_gemm_tc": ([ctypes.c_void_p, _I64, ctypes.c_void_p, _I64, _I64, _I64, _I64, _I32, _f,
                          ctypes.c_void_p, _f, _f, _f, _I32, ctypes.c_void_p], ctypes.c_int),
     "pqg_mlp_gemm_tc_t": ([ctypes.c_void_p, _I64, ctypes.c_void_p, _I64, _I64, _I64, _I64, _I32, _f,
-                           ctypes.c_void_p, _f, _f, ctypes.c_void_p, _I64, ctypes.c_void_p], ctypes.c_int),
+                           ctypes.c_void_p, _f, _f, ctypes.c_void_p, _I64, _f, _f, ctypes.c_void_p], ctypes.c_int),
     "pqg_mlp_transpose_bf16": ([ctypes.c_void_p, _I64, _I64, _I64, ctypes.c_void_p, _I64, ctypes.c_void_p],
                                ctypes.c_int),
     "pqg_mlp_tc_status": ([_i32], ctypes.c_int),

@@ -153,6 +153,16 @@ int fail_cuda(cudaError_t e, const char *what) {
 
 }  // namespace
 
+namespace pqg {
+
+int mlp_column_sums_final(const float *part, int64_t chunks, int64_t N, float *out, cudaStream_t s) {
+    bias_final<<<static_cast<unsigned>((N + 31) / 32), dim3(32, BIAS_LANES), 0, s>>>(part, chunks, N, out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_mlp_gemm_tc_t (column sums)");
+}
+
+}  // namespace pqg
+
 extern "C" {
 
 int pqg_mlp_bias_grad(const float *d, int64_t M, int64_t N, float *db, float *scratch, void *stream) {

@@ -37,6 +37,8 @@
 
 namespace pqg {
 void set_last_error(const char *msg);
+// out[n] = sum over chunks of part[chunk][n], in chunk order (mlp.cu)
+int mlp_column_sums_final(const float *part, int64_t chunks, int64_t N, float *out, cudaStream_t s);
 }
 
 namespace {
@@ -66,7 +68,8 @@ struct TcArgs {
     __nv_bfloat16 *Cb;
     const float *bias;
     const float *pre;
-    int BN;         // tile columns (UMMA N)
+    float *col_part;  // nullable: the persistent tensor-store forms' column sums of C per 32-row block
+    int BN;           // tile columns (UMMA N)
     int tmem_cols;  // power of two >= max(32, BN)
     int epi;
     int pad;
@@ -741,6 +744,23 @@ __global__ void __launch_bounds__(32 * (2 + pt_epi_warps<kForm>()), 1)
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
+                    // column sums of the block's rows below M (lane c: column c, rows in
+                    // order), read from the FP32 tile beside the tensor store's read
+                    if (g.col_part && lane < PT_GROUP) {
+                        const int64_t r0 = tile * TC_BM + q * 32;
+                        const int nr = g.M - r0 >= 32 ? 32 : static_cast<int>(g.M > r0 ? g.M - r0 : 0);
+                        const uint32_t cq = static_cast<uint32_t>(lane >> 2), cw = static_cast<uint32_t>(lane & 3) * 4u;
+                        float sum = 0.0f;
+                        for (int r = 0; r < nr; ++r) {
+                            float x;
+                            asm volatile("ld.shared.f32 %0, [%1];"
+                                         : "=f"(x)
+                                         : "r"(st_c + 64u * r + ((cq ^ ((static_cast<uint32_t>(r) >> 1) & 3u)) << 4) + cw)
+                                         : "memory");
+                            sum += x;
+                        }
+                        g.col_part[(tile * 4 + q) * g.N + col0 + lane] = sum;
+                    }
                     if (lane == 0) {
                         const int32_t y = static_cast<int32_t>(tile * TC_BM + q * 32);
                         tma_store_2d(&map_c, st_c, col0, y);
@@ -1218,7 +1238,7 @@ int transpose_launch(const void *src, int64_t rows, int64_t cols, int64_t ld_src
 // BF16 output, N x M with row stride ld_t.
 int gemm_tc_impl(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                  int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, float *splitk_scratch,
-                 int32_t splits, void *c_bf16_t, int64_t ld_t, void *stream) {
+                 int32_t splits, void *c_bf16_t, int64_t ld_t, float *col_sums, float *col_scratch, void *stream) {
     if (M <= 0 || N <= 0 || K <= 0 || !a || !b || !c || lda < K || ldb < K || epilogue < 0 || epilogue > 4)
         return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc: invalid arguments");
     if ((lda % 8) || (ldb % 8) || (reinterpret_cast<uintptr_t>(a) % 16) || (reinterpret_cast<uintptr_t>(b) % 16))
@@ -1296,18 +1316,25 @@ int gemm_tc_impl(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t
                 st = make_store_map(&mcb, c_bf16, M, N, true);
                 if (st) return st;
             }
+            // column sums from the epilogue: per 32-row block, then the blocks in order
+            if (col_sums) g.col_part = col_scratch;
             // a tensor store writes a partial 16-byte chunk at the end of a row
             // whole (measured: the seven padding columns of M = 50001 were
             // written), so the transposed rows, M long, take it at M % 8 == 0
-            if (c_bf16_t && al16(c_bf16_t) && M % 8 == 0) {
+            const bool trans = c_bf16_t && al16(c_bf16_t) && M % 8 == 0;
+            if (trans) {
                 st = make_trans_map(&mct, c_bf16_t, M, N, ld_t);
                 if (st) return st;
-                return launch_persistent<2>(ma, mb, mc, mcb, mct, g, sms, s);
+                st = launch_persistent<2>(ma, mb, mc, mcb, mct, g, sms, s);
+            } else {
+                st = launch_persistent<1>(ma, mb, mc, mcb, mc, g, sms, s);
             }
-            st = launch_persistent<1>(ma, mb, mc, mcb, mc, g, sms, s);
-        } else {
-            st = launch_persistent<0>(ma, mb, ma, ma, ma, g, sms, s);
+            if (!st && col_sums) st = pqg::mlp_column_sums_final(col_scratch, row_tiles * 4, N, col_sums, s);
+            if (st || trans || !c_bf16_t) return st;
+            return transpose_launch(c_bf16, M, N, N, c_bf16_t, ld_t, s);
         }
+        st = launch_persistent<0>(ma, mb, ma, ma, ma, g, sms, s);
+        if (!st && col_sums) st = pqg_mlp_bias_grad(c, M, N, col_sums, col_scratch, stream);
         if (st || !c_bf16_t) return st;
         return transpose_launch(c_bf16, M, N, N, c_bf16_t, ld_t, s);
     }
@@ -1330,6 +1357,10 @@ int gemm_tc_impl(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail_cuda(e, "pqg_mlp_gemm_tc (split-K reduction)");
     }
+    if (col_sums) {
+        const int cs = pqg_mlp_bias_grad(c, M, N, col_sums, col_scratch, stream);
+        if (cs) return cs;
+    }
     if (c_bf16_t) return transpose_launch(c_bf16, M, N, N, c_bf16_t, ld_t, s);
     return PQG_OK;
 }
@@ -1342,17 +1373,20 @@ int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int6
                     int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
                     float *splitk_scratch, int32_t splits, void *stream) {
     return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, splitk_scratch, splits, nullptr, 0,
-                        stream);
+                        nullptr, nullptr, stream);
 }
 
 int pqg_mlp_gemm_tc_t(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                       int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, void *c_bf16_t,
-                      int64_t ld_t, void *stream) {
+                      int64_t ld_t, float *col_sums, float *col_scratch, void *stream) {
     if ((epilogue != TC_EPI_BIAS_GELU && epilogue != TC_EPI_DGELU) || !c_bf16_t || ld_t < M || ld_t % 8)
         return fail(PQG_ERR_INVALID,
                     "pqg_mlp_gemm_tc_t: needs a BF16 epilogue (1 or 4) and a transposed output with ld_t >= M, "
                     "ld_t % 8 == 0");
-    return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, nullptr, 0, c_bf16_t, ld_t, stream);
+    if (col_sums && !col_scratch)
+        return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc_t: column sums need a scratch of 4 ceil(M/128) N floats");
+    return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, nullptr, 0, c_bf16_t, ld_t,
+                        col_sums, col_scratch, stream);
 }
 
 int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,

@@ -173,15 +173,20 @@ class MLP:
         if st:
             raise RuntimeError("pqg_mlp_gemm_tc failed: " + _lib.last_error())
 
-    def _gemm_t(self, A, lda, B, ldb, M, N, K, epi, C, Cb, bias=None, pre=None, stream=None):
+    def _gemm_t(self, A, lda, B, ldb, M, N, K, epi, C, Cb, bias=None, pre=None, col_sums=None, stream=None):
         """_gemm with a BF16 epilogue that also returns Cb^T (N x Mp, rows
-        padded to a multiple of 8 elements), written by the GEMM itself."""
+        padded to a multiple of 8 elements), written by the GEMM itself, and
+        fills `col_sums` (N floats, when given) with the column sums of C."""
+        torch = self.torch
         L = _lib.load()
         Mp = (M + 7) // 8 * 8
-        CbT = self.torch.empty(N, Mp, device=self.device, dtype=self.torch.bfloat16)
+        CbT = torch.empty(N, Mp, device=self.device, dtype=torch.bfloat16)
+        scratch = None
+        if col_sums is not None:
+            scratch = torch.empty(4 * ((M + 127) // 128) * N, device=self.device, dtype=torch.float32)
         fp = lambda t: ctypes.cast(t.data_ptr(), ctypes.POINTER(ctypes.c_float)) if t is not None else None  # noqa
         st = L.pqg_mlp_gemm_tc_t(_ptr(A), lda, _ptr(B), ldb, M, N, K, epi, fp(C), _ptr(Cb), fp(bias), fp(pre),
-                                 _ptr(CbT), Mp, stream)
+                                 _ptr(CbT), Mp, fp(col_sums), fp(scratch), stream)
         if st:
             raise RuntimeError("pqg_mlp_gemm_tc_t failed: " + _lib.last_error())
         return CbT
@@ -248,7 +253,7 @@ class MLP:
             raise RuntimeError(_lib.last_error())
         grads_W, grads_b = [None] * 4, [None] * 4
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-        d_out, d_out_b, d_out_t = dz, dzb, None
+        d_out, d_out_b, d_out_t, d_out_sums = dz, dzb, None, None
         for i in (3, 2, 1, 0):
             fi, fo = self.W[i].shape
             # dW = h_in^T d_out: K = M (split over the batch), both operands K-major: the
@@ -261,21 +266,25 @@ class MLP:
             splits = max(1, min(M // 512, sms // tiles))
             scratch = torch.empty(splits * fi * fo, device=self.device, dtype=torch.float32)
             self._gemm(hT, hT.shape[1], dT, dT.shape[1], fi, fo, M, 2, gW, scratch=scratch, splits=splits)
-            gb = torch.empty(fo, device=self.device, dtype=torch.float32)
-            part = torch.empty(((M + 255) // 256) * fo, device=self.device, dtype=torch.float32)
-            st = L.pqg_mlp_bias_grad(ctypes.cast(d_out.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, fo,
-                                     ctypes.cast(gb.data_ptr(), ctypes.POINTER(ctypes.c_float)),
-                                     ctypes.cast(part.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
-            if st:
-                raise RuntimeError(_lib.last_error())
+            if d_out_sums is not None:  # the column sums the data-gradient GEMM gave with d_out
+                gb = d_out_sums
+            else:
+                gb = torch.empty(fo, device=self.device, dtype=torch.float32)
+                part = torch.empty(((M + 255) // 256) * fo, device=self.device, dtype=torch.float32)
+                st = L.pqg_mlp_bias_grad(ctypes.cast(d_out.data_ptr(), ctypes.POINTER(ctypes.c_float)), M, fo,
+                                         ctypes.cast(gb.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                                         ctypes.cast(part.data_ptr(), ctypes.POINTER(ctypes.c_float)), None)
+                if st:
+                    raise RuntimeError(_lib.last_error())
             grads_W[i], grads_b[i] = gW, gb
             if i == 0:
                 break
             # d h_in = d_out W^T, through GELU'(pre) in the epilogue (FP32 and BF16)
             dh = torch.empty(M, fi, device=self.device, dtype=torch.float32)
             dhb = torch.empty(M, fi, device=self.device, dtype=torch.bfloat16)
-            dht = self._gemm_t(d_out_b, fo, self.Wb[i], fo, M, fi, fo, 4, dh, dhb, pre=pres[i - 1])
-            d_out, d_out_b, d_out_t = dh, dhb, dht
+            sums = torch.empty(fi, device=self.device, dtype=torch.float32)  # layer i - 1's bias gradient
+            dht = self._gemm_t(d_out_b, fo, self.Wb[i], fo, M, fi, fo, 4, dh, dhb, pre=pres[i - 1], col_sums=sums)
+            d_out, d_out_b, d_out_t, d_out_sums = dh, dhb, dht, sums
         return loss, grads_W, grads_b
 
     def adam(self, grads_W, grads_b, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):

@@ -278,7 +278,8 @@ def test_adam_multi_matches_per_tensor(L):
 @pytest.mark.parametrize("epi", [1, 4])
 def test_gemm_with_transposed_output(L, M, N, K, epi):
     """pqg_mlp_gemm_tc_t: the same C and BF16 output as pqg_mlp_gemm_tc, bit
-    for bit, plus that BF16 output transposed (N x ld_t, ld_t >= M).  The
+    for bit, plus that BF16 output transposed (N x ld_t, ld_t >= M) and the
+    column sums of C (deterministic, against a float64 sum).  The
     persistent kernel writes it from its epilogue at M a multiple of 8 (65536
     rows, and 50008 with a last tile of 88 rows); 50001 rows, 1000 rows (the
     one-tile kernel) and N = 40 (the register-store form) run the transpose
@@ -299,19 +300,32 @@ def test_gemm_with_transposed_output(L, M, N, K, epi):
         args = (_v(A), K, _v(B), K, M, N, K, epi, _f(C), _v(Cb), _f(bias) if epi == 1 else None,
                 _f(pre) if epi == 4 else None)
         if with_t:
-            assert L.pqg_mlp_gemm_tc_t(*args, _v(CbT), ld_t, None) == 0
+            sums = torch.empty(N, device="cuda")
+            scratch = torch.empty(4 * ((M + 127) // 128) * N, device="cuda")
+            assert L.pqg_mlp_gemm_tc_t(*args, _v(CbT), ld_t, _f(sums), _f(scratch), None) == 0
         else:
             assert L.pqg_mlp_gemm_tc(*args, None, 0, None) == 0
         torch.cuda.synchronize()
         assert _status(L) == 0
         assert torch.all(torch.isnan(C_all[M:])) and torch.all(Cb_all[M:] == 5.0)
         outs.append((C, Cb, CbT))
+    # the column sums of C (FP32 sums in a fixed order), and the same bits again
+    want = outs[1][0].double().sum(dim=0)
+    assert torch.all((sums.double() - want).abs() <= 1e-5 * outs[1][0].abs().double().sum(dim=0) + 1e-6)
+    sums2 = torch.empty(N, device="cuda")
+    assert L.pqg_mlp_gemm_tc_t(*args, _v(CbT), ld_t, _f(sums2), _f(scratch), None) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(sums, sums2)
     assert torch.equal(outs[0][0], outs[1][0])
     assert torch.equal(outs[0][1], outs[1][1])
     assert torch.equal(outs[1][2][:, :M], outs[1][1].t())
     assert torch.all(outs[1][2][:, M:] == 3.0)
     # only the BF16 epilogues, and a transposed row stride of at least M in multiples of 8
     C = torch.empty(M, N, device="cuda")
-    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, 0, _f(C), None, None, None, _v(CbT), ld_t, None) != 0
-    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, epi, _f(C), _v(Cb), _f(bias), _f(pre), _v(CbT), ld_t - 4,
+    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, 0, _f(C), None, None, None, _v(CbT), ld_t, None, None,
                                None) != 0
+    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, epi, _f(C), _v(Cb), _f(bias), _f(pre), _v(CbT), ld_t - 4,
+                               None, None, None) != 0
+    # column sums without a scratch
+    assert L.pqg_mlp_gemm_tc_t(_v(A), K, _v(B), K, M, N, K, epi, _f(C), _v(Cb), _f(bias), _f(pre), _v(CbT), ld_t,
+                               _f(sums2), None, None) != 0
