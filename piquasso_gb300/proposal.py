@@ -118,7 +118,11 @@ class MLP:
     tcgen05 kernel (pqg_mlp_gemm_tc): the forward pass reads the BF16 weights
     transposed (WbT[i], fan_out x fan_in), the data gradient reads them as
     stored (Wb[i]), and the weight gradient reads transposed copies of the
-    activations and of the output gradient (pqg_mlp_transpose_bf16)."""
+    activations and of the output gradient, which the GEMMs producing them
+    write beside their outputs (pqg_mlp_gemm_tc_t; the features and the
+    head's gradient go through pqg_mlp_transpose_bf16).  The data-gradient
+    GEMMs also give the next layer's bias gradient (their output's column
+    sums); Adam updates every tensor and the BF16 copies in one launch."""
 
     def __init__(self, seed=0, device="cuda"):
         import torch
