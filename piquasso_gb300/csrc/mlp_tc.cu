@@ -1102,6 +1102,16 @@ int fail_cuda(cudaError_t e, const char *what) {
     return PQG_ERR_CUDA;
 }
 
+// The catch clause of the entry points below that take a std::call_once (and
+// set the error text through a std::string): no C++ exception crosses the C ABI.
+int host_failure(const char *what) noexcept {
+    try {
+        pqg::set_last_error(what);
+    } catch (...) {
+    }
+    return PQG_ERR_HOST;
+}
+
 // SM count of the current device (0 if it cannot be read), looked up once.
 int device_sms() {
     static std::once_flag once;
@@ -1371,14 +1381,16 @@ extern "C" {
 
 int pqg_mlp_gemm_tc(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                     int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre,
-                    float *splitk_scratch, int32_t splits, void *stream) {
+                    float *splitk_scratch, int32_t splits, void *stream) try {
     return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, splitk_scratch, splits, nullptr, 0,
                         nullptr, nullptr, stream);
+} catch (...) {
+    return host_failure("pqg_mlp_gemm_tc: host-side failure");
 }
 
 int pqg_mlp_gemm_tc_t(const void *a, int64_t lda, const void *b, int64_t ldb, int64_t M, int64_t N, int64_t K,
                       int32_t epilogue, float *c, void *c_bf16, const float *bias, const float *pre, void *c_bf16_t,
-                      int64_t ld_t, float *col_sums, float *col_scratch, void *stream) {
+                      int64_t ld_t, float *col_sums, float *col_scratch, void *stream) try {
     if ((epilogue != TC_EPI_BIAS_GELU && epilogue != TC_EPI_DGELU) || !c_bf16_t || ld_t < M || ld_t % 8)
         return fail(PQG_ERR_INVALID,
                     "pqg_mlp_gemm_tc_t: needs a BF16 epilogue (1 or 4) and a transposed output with ld_t >= M, "
@@ -1387,6 +1399,8 @@ int pqg_mlp_gemm_tc_t(const void *a, int64_t lda, const void *b, int64_t ldb, in
         return fail(PQG_ERR_INVALID, "pqg_mlp_gemm_tc_t: column sums need a scratch of 4 ceil(M/128) N floats");
     return gemm_tc_impl(a, lda, b, ldb, M, N, K, epilogue, c, c_bf16, bias, pre, nullptr, 0, c_bf16_t, ld_t,
                         col_sums, col_scratch, stream);
+} catch (...) {
+    return host_failure("pqg_mlp_gemm_tc_t: host-side failure");
 }
 
 int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t ld_src, void *dst, int64_t ld_dst,
@@ -1399,7 +1413,7 @@ int pqg_mlp_transpose_bf16(const void *src, int64_t rows, int64_t cols, int64_t 
 int pqg_proposal_step_tc(int32_t j, int32_t B, int32_t d, int32_t n, const float *mode_stats, const void *w1t,
                          const void *w2t, const void *w3t, const void *w4t, const float *b1, const float *b2,
                          const float *b3, const float *b4, uint64_t seed, const uint64_t *seed_dev, int8_t *samples,
-                         int32_t *n_rem, float *shift, const float *C, float *logq, void *stream) {
+                         int32_t *n_rem, float *shift, const float *C, float *logq, void *stream) try {
     if (B <= 0 || d <= 0 || n <= 0 || j < 0 || j >= d || !mode_stats || !w1t || !w2t || !w3t || !w4t || !b1 ||
         !b2 || !b3 || !b4 || !samples || !n_rem || !shift || !C || !logq)
         return fail(PQG_ERR_INVALID, "pqg_proposal_step_tc: invalid arguments");
@@ -1441,6 +1455,8 @@ int pqg_proposal_step_tc(int32_t j, int32_t B, int32_t d, int32_t n, const float
                        static_cast<cudaStream_t>(stream)>>>(m1, m2, m3, m4, g);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? PQG_OK : fail_cuda(e, "pqg_proposal_step_tc");
+} catch (...) {
+    return host_failure("pqg_proposal_step_tc: host-side failure");
 }
 
 int pqg_mlp_tc_status(int32_t *code) {
