@@ -106,3 +106,36 @@ def test_status_codes_match_the_header():
     assert "PQG_ERR_HOST" in codes
     for name, value in codes.items():
         assert getattr(_lib, name) == int(value), name
+
+
+def test_mlp_entry_points_reject_on_the_host(lib):
+    """The MLP GEMM with the transposed output and the one-launch Adam check
+    their arguments before any device work (placeholder pointers are never
+    read): a non-BF16 epilogue, a transposed row stride below M or not a
+    multiple of 8, column sums without a scratch; a tensor count outside
+    1..16, a missing tensor."""
+    from piquasso_gb300 import _lib
+
+    bad = _lib.PQG_ERR_INVALID
+    p = ctypes.c_void_p(256)
+    f = ctypes.cast(p, ctypes.POINTER(ctypes.c_float))
+    M, N, K = 1024, 256, 256
+    args = (p, K, p, K, M, N, K)
+    assert lib.pqg_mlp_gemm_tc_t(*args, 0, f, None, None, None, p, M, None, None, None) == bad
+    assert lib.pqg_mlp_gemm_tc_t(*args, 1, f, p, f, None, None, M, None, None, None) == bad
+    assert lib.pqg_mlp_gemm_tc_t(*args, 1, f, p, f, None, p, M - 8, None, None, None) == bad
+    assert lib.pqg_mlp_gemm_tc_t(*args, 4, f, p, None, f, p, M + 4, None, None, None) == bad
+    assert lib.pqg_mlp_gemm_tc_t(*args, 4, f, p, None, f, p, M, f, None, None) == bad
+    P = ctypes.c_void_p * 2
+    R = ctypes.c_int64 * 2
+    ptrs = P(256, 512)
+    rc = R(4, 4)
+    assert lib.pqg_mlp_adam_multi(0, ptrs, None, None, ptrs, ptrs, ptrs, rc, rc, 1e-3, 0.9, 0.999, 1e-8, 1,
+                                  None) == bad
+    assert lib.pqg_mlp_adam_multi(17, ptrs, None, None, ptrs, ptrs, ptrs, rc, rc, 1e-3, 0.9, 0.999, 1e-8, 1,
+                                  None) == bad
+    holes = P(256, None)
+    assert lib.pqg_mlp_adam_multi(2, holes, None, None, ptrs, ptrs, ptrs, rc, rc, 1e-3, 0.9, 0.999, 1e-8, 1,
+                                  None) == bad
+    assert lib.pqg_mlp_adam_multi(2, ptrs, None, None, ptrs, ptrs, ptrs, rc, R(4, 0), 1e-3, 0.9, 0.999, 1e-8, 1,
+                                  None) == bad
